@@ -1,0 +1,295 @@
+/*
+ * smg.h — C ABI of the GB300-native subgraph-matching library (libsmg).
+ *
+ * The library counts (and optionally lists) the injective, label-preserving,
+ * non-induced embeddings of a small labelled query graph in a large labelled
+ * undirected data graph, with the same semantics and the same host-side
+ * query preprocessing as ClusterSM:
+ *
+ *   reference seam                         replaced here by
+ *   -------------------------------------  ---------------------------------
+ *   readGraphToCPU2   io.cu:24-108          smg_read_graph / smg_read_query
+ *   copyMeta + copyGraphToGPU io.cu:235,265 smg_graph_upload
+ *   decycle decycle.cpp:6, clustering       smg_plan_create (host C++)
+ *     filter.cu:127, getBFSEdgeOrder
+ *     order.cpp:150, encodingMeta::init
+ *     structure.cu:219
+ *   clusterFilter  filter.cuh:130-144       smg_filter_inspect (filter only)
+ *   clusterFilter + join  main.cu:123-172   smg_match (one query per call)
+ *   runClusterSM.sh:9-13 (one process per   smg_match_batch (many queries,
+ *     query)                                  one persistent launch)
+ *   (none: no serving mode)                 smg_server_*
+ *
+ * Conventions: every call returns an smg_status; no call exits the process.
+ * Vertex ids are uint32, offsets and counts uint64.  A context is bound to
+ * one device and one CUDA stream; it is thread-compatible, not thread-safe.
+ * Objects returned through an out-pointer are owned by the caller and freed
+ * with the matching *_free / *_destroy call.
+ */
+#ifndef SMG_H
+#define SMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef int32_t smg_status;
+#define SMG_OK 0
+#define SMG_ERR_INVALID 1    /* bad argument (null pointer, size mismatch)       */
+#define SMG_ERR_IO 2         /* cannot open / read / write a file (io.cu:29-33)  */
+#define SMG_ERR_FORMAT 3     /* malformed .in text (io.cu:37-41)                 */
+#define SMG_ERR_QUERY 4      /* unsupported query: disconnected, <2 or >32
+                                vertices, self-loop or repeated edge           */
+#define SMG_ERR_LIMIT 5      /* a size limit of this build was exceeded          */
+#define SMG_ERR_CUDA 6       /* a CUDA runtime call failed                       */
+#define SMG_ERR_OOM 7        /* device or host allocation failed                 */
+#define SMG_ERR_TIMEOUT 8    /* a bounded device-side wait gave up               */
+#define SMG_ERR_NO_DEVICE 9  /* no usable CUDA device                            */
+#define SMG_ERR_BUDGET 10    /* request exceeds the server memory budget         */
+#define SMG_ERR_CANCELLED 11 /* request cancelled before it ran                  */
+#define SMG_ERR_NOT_READY 12 /* request still in flight (smg_server_poll)        */
+#define SMG_ERR_INTERNAL 13  /* invariant violated inside the library            */
+
+/* Static string for a status code; never NULL. */
+const char *smg_strerror(smg_status s);
+/* Detail text of the last error raised on this host thread ("" if none). */
+const char *smg_last_error(void);
+
+/* Limits of this build. */
+#define SMG_MAX_QUERY_VERTICES 32u /* u-bitmasks are 32 bits (filter.cu:501) */
+#define SMG_MAX_QUERY_EDGES 496u   /* complete graph on 32 vertices          */
+
+/* ------------------------------------------------------- host-side graphs */
+/* Read-only view of an undirected labelled graph in CSR form (host memory).
+ * neighbors holds every undirected edge twice, once in each endpoint's list. */
+typedef struct smg_csr {
+  uint32_t num_vertices;
+  uint64_t num_edges;        /* undirected edges                          */
+  const uint64_t *offsets;   /* [num_vertices + 1]                        */
+  const uint32_t *neighbors; /* [2 * num_edges]                           */
+  const uint32_t *labels;    /* [num_vertices]                            */
+} smg_csr;
+
+/* Read-only view of a query graph: labels plus the undirected edge list in
+ * file order.  File order matters: it fixes neighbour order in the query CSR,
+ * which fixes the spanning tree, the clusters and the matching order. */
+typedef struct smg_query_desc {
+  uint32_t num_vertices;
+  uint32_t num_edges;
+  const uint32_t *labels; /* [num_vertices]                                  */
+  const uint32_t *edges;  /* [2 * num_edges]: (a0,b0, a1,b1, ...) file order */
+} smg_query_desc;
+
+typedef struct smg_host_graph smg_host_graph; /* library-owned host CSR   */
+typedef struct smg_host_query smg_host_query; /* library-owned query      */
+
+/* Parse a .in data graph: "t n m", then "v id label deg" lines, then
+ * "e a b" once per undirected edge (io.cu:24-108).  Declared degrees must
+ * match the edges.  Neighbour lists keep file order. */
+smg_status smg_read_graph(const char *path, smg_host_graph **out);
+/* Parse a .in query graph (same format), keeping the edge list in file order. */
+smg_status smg_read_query(const char *path, smg_host_query **out);
+/* Write a graph / query in the same .in dialect. */
+smg_status smg_write_graph(const char *path, const smg_csr *g);
+smg_status smg_write_query(const char *path, const smg_query_desc *q);
+
+/* Views into library-owned objects (valid until the object is freed). */
+smg_status smg_host_graph_view(const smg_host_graph *g, smg_csr *out);
+smg_status smg_host_query_view(const smg_host_query *q, smg_query_desc *out);
+/* Build a host graph from a caller's CSR (copies; neighbour lists are
+ * sorted and checked for self-loops / duplicates / asymmetry). */
+smg_status smg_host_graph_from_csr(const smg_csr *in, smg_host_graph **out);
+void smg_host_graph_free(smg_host_graph *g);
+void smg_host_query_free(smg_host_query *q);
+
+/* Seeded synthetic inputs (deterministic on every host: integer-only RNG).
+ * label_dist: SMG_LABELS_UNIFORM or SMG_LABELS_ZIPF1 (P(l) ~ 1/(l+1)).     */
+#define SMG_LABELS_UNIFORM 0
+#define SMG_LABELS_ZIPF1 1
+/* Erdos-Renyi G(n, m): m distinct unordered pairs, no self-loops. */
+smg_status smg_gen_er(uint32_t n, uint64_t m, uint32_t num_labels,
+                      uint32_t label_dist, uint64_t seed, smg_host_graph **out);
+/* R-MAT (a,b,c,d)=(0.57,0.19,0.19,0.05), 2^scale vertices, scale*... :
+ * n*avg_degree/2 edge draws, symmetrised, self-loops and duplicates dropped,
+ * neighbour lists sorted.  threads<=0 uses all host cores. */
+smg_status smg_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels,
+                        uint32_t label_dist, uint64_t seed, int threads,
+                        smg_host_graph **out);
+/* Random-walk query extraction: k distinct vertices reached by a seeded walk,
+ * labels copied, so at least one embedding exists.  shape: */
+#define SMG_SHAPE_TREE 0   /* first-visit edges only                       */
+#define SMG_SHAPE_SPARSE 1 /* tree + 2 random induced non-tree edges       */
+#define SMG_SHAPE_DENSE 2  /* all induced edges, average query degree >= 3 */
+smg_status smg_gen_query(const smg_csr *g, uint32_t k, uint32_t shape,
+                         uint64_t seed, smg_host_query **out,
+                         uint32_t *out_data_vertices /* [k] or NULL */);
+
+/* ------------------------------------------------------------ query plans */
+typedef struct smg_plan smg_plan;
+
+/* Host-side preprocessing of one query: spanning tree (decycle.cpp:6-134),
+ * minimum vertex cover (filter.cu:23-112), clustering (filter.cu:127-401),
+ * cluster CSR (structure.cu:219-239), BFS edge order (order.cpp:150-206)
+ * from the core of the last cluster (main.cu:144). */
+smg_status smg_plan_create(const smg_query_desc *q, smg_plan **out);
+void smg_plan_free(smg_plan *p);
+
+/* Read-only view of a plan (arrays owned by the plan). */
+typedef struct smg_plan_view {
+  uint32_t k;              /* query vertices                                 */
+  uint32_t num_edges;      /* query edges                                    */
+  uint32_t nvlq;           /* largest query label + 1 (io.cu:269)            */
+  uint32_t root;           /* first vertex of the matching order             */
+  const uint32_t *labels;  /* [k]                                            */
+  const uint32_t *degrees; /* [k] full-query degrees                         */
+  const uint32_t *nlc;     /* [k * nvlq] neighbour-label counts (filter.cu:555) */
+  /* spanning tree CSR (decycle) */
+  const uint32_t *tree_offsets;   /* [k + 1]                               */
+  const uint32_t *tree_neighbors; /* [tree_offsets[k]]                     */
+  /* vertex cover in selection order */
+  uint32_t cover_size;
+  const uint32_t *cover;
+  /* cluster CSR (encodingMeta) */
+  uint32_t num_clusters;
+  uint32_t num_slots;              /* num_total_us                          */
+  uint32_t num_words;              /* ceil(num_slots / 32), num_blocks      */
+  const uint32_t *cluster_offsets; /* [num_clusters + 1]                    */
+  const uint32_t *slots;           /* [num_slots] query vertex per slot     */
+  const uint32_t *cluster_layer;   /* [num_clusters]                        */
+  const uint32_t *cluster_kind;    /* [num_clusters] 0 star, 1 merge, 2 combine */
+  uint32_t num_layers;
+  /* merge records, one per merge cluster, in cluster order */
+  uint32_t num_merges;
+  const uint32_t *merge_cluster; /* [num_merges] cluster index created      */
+  const uint32_t *merge_left;    /* [num_merges]                            */
+  const uint32_t *merge_right;   /* [num_merges]                            */
+  const uint32_t *merge_vertex;  /* [num_merges] connection vertex          */
+  /* combine records in creation order */
+  uint32_t num_combines;
+  const uint32_t *combine_out;          /* [num_combines]                   */
+  const uint32_t *combine_type;         /* [num_combines] 0 new, 1 in-place  */
+  const uint32_t *combine_layer;        /* [num_combines]                   */
+  const uint32_t *combine_other_offsets;/* [num_combines + 1]               */
+  const uint32_t *combine_others;       /* [combine_other_offsets[n]]       */
+  const uint32_t *last_slot;            /* [k] slot read for candidates     */
+  /* reference edge order: directed edges (first -> second), first mapped */
+  const uint32_t *edge_order_first;  /* [num_edges]                        */
+  const uint32_t *edge_order_second; /* [num_edges]                        */
+  /* vertex-level matching order derived from the edge order */
+  const uint32_t *order;         /* [k] query vertex matched at each level  */
+  const uint32_t *anchor_level;  /* [k] level of the tree parent (0 for root) */
+  const uint32_t *back_mask;     /* [k] bit j: edge to the vertex of level j<i */
+} smg_plan_view;
+smg_status smg_plan_get(const smg_plan *p, smg_plan_view *out);
+
+/* ---------------------------------------------------- device context/graph */
+typedef struct smg_ctx smg_ctx;
+typedef struct smg_graph smg_graph;
+
+/* Bind a context to CUDA device `device` (main.cu:36-43) on its own stream. */
+smg_status smg_open(int device, smg_ctx **out);
+void smg_close(smg_ctx *ctx);
+
+/* Upload a data graph: CSR with sorted neighbour lists, labels and the
+ * per-vertex neighbour-label counts become device-resident until freed. */
+smg_status smg_graph_upload(smg_ctx *ctx, const smg_csr *g, smg_graph **out);
+void smg_graph_free(smg_graph *g);
+
+typedef struct smg_graph_stats {
+  uint32_t num_vertices;
+  uint64_t num_edges;
+  uint32_t num_labels;   /* largest label + 1                              */
+  uint32_t max_degree;
+  uint64_t device_bytes; /* HBM held by the resident graph               */
+} smg_graph_stats;
+smg_status smg_graph_get_stats(const smg_graph *g, smg_graph_stats *out);
+
+/* ------------------------------------------------------------------ match */
+#define SMG_FLAG_EMIT 1u      /* write embeddings to opts->embeddings        */
+#define SMG_FLAG_PROFILE 2u   /* record per-phase device times (adds syncs)  */
+
+typedef struct smg_match_opts {
+  uint32_t flags;
+  uint32_t bfs_depth;     /* levels expanded breadth-first before the
+                             depth-first phase; 0 = autotuned             */
+  uint32_t root_chunk;    /* root candidates per initial task; 0 = auto    */
+  uint32_t reserved;
+  uint64_t max_embeddings; /* rows of k ids the embeddings buffer can hold */
+  uint32_t *embeddings;    /* host buffer [max_embeddings * k], row r holds
+                              the data vertex of query vertex 0..k-1       */
+} smg_match_opts;
+
+typedef struct smg_match_result {
+  uint64_t count;               /* exact number of embeddings             */
+  uint64_t embeddings_written;  /* rows written (<= max_embeddings)       */
+  uint32_t overflow;            /* 1 if more embeddings than rows         */
+  uint32_t num_candidates_root; /* candidates of the first matched vertex */
+  uint64_t candidates_total;    /* sum over u of |C(u)| after the filter  */
+  float filter_ms;              /* device time of the filter (PROFILE)    */
+  float join_ms;                /* device time of the join (PROFILE)      */
+  uint64_t tasks;               /* depth-first tasks processed            */
+  uint64_t filter_bytes;        /* algorithmic bytes of the filter        */
+  uint64_t join_bytes;          /* algorithmic bytes of the join          */
+} smg_match_result;
+
+/* Plain path: one query, filter then join, synchronous. */
+smg_status smg_match(smg_ctx *ctx, const smg_graph *g, const smg_plan *p,
+                     const smg_match_opts *opts, smg_match_result *out);
+
+/* Batched path: all queries in one persistent launch fed by a device work
+ * queue; counts[i] receives the exact count of plans[i]. */
+typedef struct smg_batch_stats {
+  float filter_ms;
+  float join_ms;
+  uint64_t tasks;
+  uint64_t total_embeddings;
+} smg_batch_stats;
+smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
+                           const smg_plan *const *plans, uint32_t n,
+                           const smg_match_opts *opts, uint64_t *counts,
+                           smg_batch_stats *stats);
+
+/* Filter only (for inspection): copies to host the per-vertex initial
+ * candidate masks (bit u, filter.cu:529-535), the cluster bitmap
+ * (num_vertices x num_words words, filter.cu:585-873) and the final
+ * per-vertex candidate masks (filter.cu:1158-1232).  Any pointer may be
+ * NULL. */
+smg_status smg_filter_inspect(smg_ctx *ctx, const smg_graph *g,
+                              const smg_plan *p, uint32_t *vmask0,
+                              uint32_t *encodings, uint32_t *candmask);
+
+/* ---------------------------------------------------------------- serving */
+typedef struct smg_server smg_server;
+typedef struct smg_server_config {
+  uint64_t memory_budget_bytes; /* HBM for per-request state; 0 = auto      */
+  uint32_t max_inflight;        /* queries resident at once; 0 = auto        */
+  uint32_t reserved;
+} smg_server_config;
+typedef struct smg_request_result {
+  smg_status status;
+  uint32_t reserved;
+  uint64_t count;
+  double submit_s;   /* host clock at submit                              */
+  double start_s;    /* host clock at admission                           */
+  double finish_s;   /* host clock when the count was read back           */
+} smg_request_result;
+smg_status smg_server_create(smg_ctx *ctx, const smg_graph *g,
+                             const smg_server_config *cfg, smg_server **out);
+smg_status smg_server_submit(smg_server *s, const smg_plan *p, uint64_t *ticket);
+/* SMG_ERR_NOT_READY while the request is queued or running. */
+smg_status smg_server_poll(smg_server *s, uint64_t ticket, smg_request_result *out);
+smg_status smg_server_cancel(smg_server *s, uint64_t ticket);
+/* Drive the server until every submitted request has finished. */
+smg_status smg_server_drain(smg_server *s);
+/* Make progress once without blocking (admit, launch, retire). */
+smg_status smg_server_step(smg_server *s);
+void smg_server_destroy(smg_server *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMG_H */

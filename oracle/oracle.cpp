@@ -1,0 +1,354 @@
+// oracle.cpp — CPU restatement of the reference's filter and join semantics.
+// TEST INFRASTRUCTURE ONLY: the checker for tests/, smoke() and the CPU
+// baseline of bench.py.  The product library never links or calls this file.
+#include "oracle.h"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct QueryInfo {
+  uint32_t k = 0;
+  std::vector<uint32_t> label, deg;
+  uint32_t adj[32] = {0};          // adjacency bitmask per query vertex
+  std::vector<uint32_t> order;      // matching order of the oracle
+  std::vector<uint32_t> level_of;
+  std::vector<uint32_t> back;       // per level: mask of earlier levels adjacent
+};
+
+// The oracle's own order: start at the vertex of largest degree, then keep
+// adding the unmapped vertex with the most mapped neighbours (ties: larger
+// degree, then smaller id).  Independent of the library's plan.
+bool make_query(const smg_query_desc *q, QueryInfo &Q) {
+  if (!q || q->num_vertices < 1 || q->num_vertices > 32) return false;
+  Q.k = q->num_vertices;
+  Q.label.assign(q->labels, q->labels + Q.k);
+  Q.deg.assign(Q.k, 0);
+  for (uint32_t i = 0; i < q->num_edges; ++i) {
+    uint32_t a = q->edges[2 * i], b = q->edges[2 * i + 1];
+    if (a >= Q.k || b >= Q.k || a == b) return false;
+    Q.adj[a] |= 1u << b;
+    Q.adj[b] |= 1u << a;
+  }
+  for (uint32_t u = 0; u < Q.k; ++u) Q.deg[u] = __builtin_popcount(Q.adj[u]);
+  uint32_t start = 0;
+  for (uint32_t u = 1; u < Q.k; ++u)
+    if (Q.deg[u] > Q.deg[start]) start = u;
+  Q.order = {start};
+  uint32_t mapped = 1u << start;
+  while (Q.order.size() < Q.k) {
+    int best = -1, best_c = -1;
+    for (uint32_t u = 0; u < Q.k; ++u) {
+      if (mapped >> u & 1) continue;
+      int c = __builtin_popcount(Q.adj[u] & mapped);
+      if (c == 0) continue;
+      if (c > best_c || (c == best_c && Q.deg[u] > Q.deg[best])) {
+        best = static_cast<int>(u);
+        best_c = c;
+      }
+    }
+    if (best < 0) return false;  // disconnected
+    Q.order.push_back(static_cast<uint32_t>(best));
+    mapped |= 1u << best;
+  }
+  Q.level_of.assign(Q.k, 0);
+  for (uint32_t i = 0; i < Q.k; ++i) Q.level_of[Q.order[i]] = i;
+  Q.back.assign(Q.k, 0);
+  for (uint32_t i = 0; i < Q.k; ++i)
+    for (uint32_t j = 0; j < i; ++j)
+      if (Q.adj[Q.order[i]] >> Q.order[j] & 1) Q.back[i] |= 1u << j;
+  return true;
+}
+
+inline bool has_edge(const smg_csr *g, uint32_t a, uint32_t b) {
+  const uint32_t *lo = g->neighbors + g->offsets[a], *hi = g->neighbors + g->offsets[a + 1];
+  return std::binary_search(lo, hi, b);
+}
+
+struct Matcher {
+  const smg_csr *g;
+  const QueryInfo &Q;
+  const uint32_t *candmask;
+  uint32_t m[32];  // image per level
+  uint64_t count = 0;
+  std::vector<uint32_t> *rows = nullptr;
+  uint64_t max_rows = 0;
+
+  bool ok_vertex(uint32_t lvl, uint32_t v) const {
+    uint32_t u = Q.order[lvl];
+    if (g->labels[v] != Q.label[u]) return false;
+    if (g->offsets[v + 1] - g->offsets[v] < Q.deg[u]) return false;
+    if (candmask && !(candmask[v] >> u & 1)) return false;
+    return true;
+  }
+
+  void extend(uint32_t lvl) {
+    // pivot: mapped neighbour whose image has the fewest neighbours
+    uint32_t bm = Q.back[lvl], pivot = 0;
+    uint64_t best = ~0ull;
+    for (uint32_t b = bm; b; b &= b - 1) {
+      uint32_t j = __builtin_ctz(b);
+      uint64_t d = g->offsets[m[j] + 1] - g->offsets[m[j]];
+      if (d < best) {
+        best = d;
+        pivot = j;
+      }
+    }
+    const uint32_t pv = m[pivot];
+    for (uint64_t e = g->offsets[pv]; e < g->offsets[pv + 1]; ++e) {
+      uint32_t w = g->neighbors[e];
+      if (!ok_vertex(lvl, w)) continue;
+      bool good = true;
+      for (uint32_t j = 0; j < lvl && good; ++j) good = m[j] != w;
+      for (uint32_t b = bm & ~(1u << pivot); b && good; b &= b - 1)
+        good = has_edge(g, m[__builtin_ctz(b)], w);
+      if (!good) continue;
+      m[lvl] = w;
+      if (lvl + 1 == Q.k) {
+        ++count;
+        if (rows && rows->size() / Q.k < max_rows) {
+          for (uint32_t u = 0; u < Q.k; ++u) rows->push_back(m[Q.level_of[u]]);
+        }
+      } else {
+        extend(lvl + 1);
+      }
+    }
+  }
+};
+
+void root_candidates(const smg_csr *g, const QueryInfo &Q, const uint32_t *candmask,
+                     std::vector<uint32_t> &roots) {
+  Matcher mt{g, Q, candmask};
+  for (uint32_t v = 0; v < g->num_vertices; ++v)
+    if (mt.ok_vertex(0, v)) roots.push_back(v);
+}
+
+uint64_t count_range(const smg_csr *g, const QueryInfo &Q, const uint32_t *candmask,
+                     const std::vector<uint32_t> &roots, uint64_t lo, uint64_t hi, int threads) {
+  uint64_t total = 0;
+  if (Q.k == 1) return hi - lo;
+  int nt = threads;
+#ifdef _OPENMP
+  if (nt <= 0) nt = omp_get_max_threads();
+#else
+  nt = 1;
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total) num_threads(nt)
+  for (int64_t r = static_cast<int64_t>(lo); r < static_cast<int64_t>(hi); ++r) {
+    Matcher mt{g, Q, candmask};
+    mt.m[0] = roots[r];
+    mt.extend(1);
+    total += mt.count;
+  }
+  return total;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_count(const smg_csr *g, const smg_query_desc *q, const uint32_t *candmask, int threads,
+                 uint64_t *count) {
+  QueryInfo Q;
+  if (!g || !count || !make_query(q, Q)) return 1;
+  std::vector<uint32_t> roots;
+  root_candidates(g, Q, candmask, roots);
+  *count = count_range(g, Q, candmask, roots, 0, roots.size(), threads);
+  return 0;
+}
+
+int oracle_count_roots(const smg_csr *g, const smg_query_desc *q, int threads, uint64_t root_lo,
+                       uint64_t root_hi, uint64_t *count, uint64_t *num_roots) {
+  QueryInfo Q;
+  if (!g || !count || !make_query(q, Q)) return 1;
+  std::vector<uint32_t> roots;
+  root_candidates(g, Q, nullptr, roots);
+  if (num_roots) *num_roots = roots.size();
+  root_hi = std::min<uint64_t>(root_hi, roots.size());
+  root_lo = std::min(root_lo, root_hi);
+  *count = count_range(g, Q, nullptr, roots, root_lo, root_hi, threads);
+  return 0;
+}
+
+int oracle_embeddings(const smg_csr *g, const smg_query_desc *q, uint64_t max_rows, uint32_t *emb,
+                      uint64_t *rows, uint64_t *count) {
+  QueryInfo Q;
+  if (!g || !count || !make_query(q, Q)) return 1;
+  std::vector<uint32_t> roots;
+  root_candidates(g, Q, nullptr, roots);
+  std::vector<uint32_t> all;
+  Matcher mt{g, Q, nullptr};
+  mt.rows = &all;
+  mt.max_rows = ~0ull;
+  for (uint32_t r : roots) {
+    mt.m[0] = r;
+    if (Q.k == 1) {
+      ++mt.count;
+      all.push_back(r);
+    } else {
+      mt.extend(1);
+    }
+  }
+  *count = mt.count;
+  const uint32_t k = Q.k;
+  const uint64_t n = all.size() / k;
+  std::vector<uint64_t> idx(n);
+  for (uint64_t i = 0; i < n; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](uint64_t a, uint64_t b) {
+    return std::lexicographical_compare(all.begin() + a * k, all.begin() + a * k + k,
+                                        all.begin() + b * k, all.begin() + b * k + k);
+  });
+  uint64_t w = std::min<uint64_t>(n, max_rows);
+  if (emb)
+    for (uint64_t i = 0; i < w; ++i) std::memcpy(emb + i * k, all.data() + idx[i] * k, k * sizeof(uint32_t));
+  if (rows) *rows = emb ? w : 0;
+  return 0;
+}
+
+// filter.cu:404-539 restated: one pass over the data vertices.
+int oracle_nlc_filter(const smg_csr *g, const smg_plan_view *p, uint32_t *vmask0) {
+  if (!g || !p || !vmask0) return 1;
+  const uint32_t nvlq = p->nvlq, k = p->k;
+#pragma omp parallel
+  {
+    std::vector<uint32_t> nlc(nvlq);
+#pragma omp for schedule(dynamic, 4096)
+    for (int64_t vi = 0; vi < static_cast<int64_t>(g->num_vertices); ++vi) {
+      const uint32_t v = static_cast<uint32_t>(vi);
+      uint32_t mask = 0;
+      const uint32_t lv = g->labels[v];
+      if (lv < nvlq) {  // filter.cu:463-467
+        std::fill(nlc.begin(), nlc.end(), 0);
+        for (uint64_t e = g->offsets[v]; e < g->offsets[v + 1]; ++e) {
+          uint32_t l = g->labels[g->neighbors[e]];
+          if (l < nvlq) ++nlc[l];
+        }
+        const uint64_t dv = g->offsets[v + 1] - g->offsets[v];
+        for (uint32_t u = 0; u < k; ++u) {
+          if (p->degrees[u] > dv || p->labels[u] != lv) continue;  // filter.cu:489-490
+          bool ok = true;
+          for (uint32_t l = 0; l < nvlq && ok; ++l) ok = nlc[l] >= p->nlc[u * nvlq + l];
+          if (ok) mask |= 1u << u;
+        }
+      }
+      vmask0[v] = mask;
+    }
+  }
+  return 0;
+}
+
+int oracle_encode(const smg_csr *g, const smg_plan_view *p, const uint32_t *vmask0, uint32_t *enc,
+                  uint32_t *candmask) {
+  if (!g || !p || !vmask0 || !enc) return 1;
+  const uint32_t n = g->num_vertices, B = p->num_words, k = p->k;
+  std::memset(enc, 0, sizeof(uint32_t) * static_cast<size_t>(n) * B);
+  auto bit = [&](uint32_t v, uint32_t s) -> bool { return enc[static_cast<size_t>(v) * B + s / 32] >> (s % 32) & 1; };
+  auto set = [&](uint32_t v, uint32_t s) { enc[static_cast<size_t>(v) * B + s / 32] |= 1u << (s % 32); };
+  auto clr = [&](uint32_t v, uint32_t s) { enc[static_cast<size_t>(v) * B + s / 32] &= ~(1u << (s % 32)); };
+  // candidate lists of the initial filter; merges punch holes (filter.cu:718)
+  std::vector<std::vector<char>> alive(k, std::vector<char>(n, 0));
+  for (uint32_t v = 0; v < n; ++v)
+    for (uint32_t u = 0; u < k; ++u)
+      if (vmask0[v] >> u & 1) alive[u][v] = 1;
+  // neighbour slots of cluster c set on w when w passed the initial filter
+  // for that slot's vertex (filter.cu:633-647, 724-740)
+  auto spread = [&](uint32_t c, uint32_t v) {
+    const uint32_t s0 = p->cluster_offsets[c], s1 = p->cluster_offsets[c + 1];
+    for (uint64_t e = g->offsets[v]; e < g->offsets[v + 1]; ++e) {
+      uint32_t w = g->neighbors[e];
+      for (uint32_t s = s0 + 1; s < s1; ++s)
+        if (vmask0[w] >> p->slots[s] & 1) set(w, s);
+    }
+  };
+  const uint32_t C = p->num_clusters;
+  // merge record per cluster
+  std::vector<int64_t> merge_of(C, -1);
+  for (uint32_t r = 0; r < p->num_merges; ++r) merge_of[p->merge_cluster[r]] = r;
+  for (uint32_t layer = 0; layer < p->num_layers; ++layer) {
+    for (uint32_t c = 0; c < C; ++c) {
+      if (p->cluster_layer[c] != layer) continue;
+      const uint32_t s0 = p->cluster_offsets[c], core = p->slots[s0];
+      if (p->cluster_kind[c] == 0) {  // encodeKernel filter.cu:585-653
+        for (uint32_t v = 0; v < n; ++v) {
+          if (!alive[core][v]) continue;
+          set(v, s0);
+          spread(c, v);
+        }
+      } else if (p->cluster_kind[c] == 1) {  // mergeKernel filter.cu:656-746
+        const int64_t r = merge_of[c];
+        if (r < 0) return 2;
+        uint32_t lp = 0, rp = 0;
+        for (uint32_t s = p->cluster_offsets[p->merge_left[r]];; ++s)
+          if (p->slots[s] == core) { lp = s; break; }
+        for (uint32_t s = p->cluster_offsets[p->merge_right[r]];; ++s)
+          if (p->slots[s] == core) { rp = s; break; }
+        for (uint32_t v = 0; v < n; ++v) {
+          if (!alive[core][v]) continue;
+          if (bit(v, lp) && bit(v, rp)) {
+            set(v, s0);
+            spread(c, v);
+          } else {
+            alive[core][v] = 0;
+          }
+        }
+      }
+    }
+    // combines of this layer (filter.cu:749-873 with the intended semantics:
+    // a slot of the combined cluster holds the AND of the same vertex's slots
+    // in the other clusters of the group)
+    for (uint32_t r = 0; r < p->num_combines; ++r) {
+      if (p->combine_layer[r] != layer) continue;
+      const uint32_t out = p->combine_out[r], type = p->combine_type[r];
+      const uint32_t s0 = p->cluster_offsets[out], s1 = p->cluster_offsets[out + 1], core = p->slots[s0];
+      const uint32_t *oth = p->combine_others + p->combine_other_offsets[r];
+      const uint32_t no = p->combine_other_offsets[r + 1] - p->combine_other_offsets[r];
+      // slot of target vertex in each other cluster (or none)
+      std::vector<std::vector<uint32_t>> tslots(s1 - s0);
+      for (uint32_t s = s0 + 1; s < s1; ++s)
+        for (uint32_t o = 0; o < no; ++o)
+          for (uint32_t t = p->cluster_offsets[oth[o]]; t < p->cluster_offsets[oth[o] + 1]; ++t)
+            if (p->slots[t] == p->slots[s]) {
+              tslots[s - s0].push_back(t);
+              break;
+            }
+      for (uint32_t v = 0; v < n; ++v) {
+        if (!alive[core][v]) continue;
+        bool all = true;
+        for (uint32_t o = 0; o < no; ++o) all = all && bit(v, p->cluster_offsets[oth[o]]);
+        if (type == 0) {
+          if (all) set(v, s0);
+        } else if (!all) {
+          clr(v, s0);
+        }
+        for (uint64_t e = g->offsets[v]; e < g->offsets[v + 1]; ++e) {
+          uint32_t w = g->neighbors[e];
+          for (uint32_t s = s0 + 1; s < s1; ++s) {
+            bool fin = true;
+            for (uint32_t t : tslots[s - s0]) fin = fin && bit(w, t);
+            if (type == 0) {
+              if (fin) set(w, s);
+            } else if (!fin) {
+              clr(w, s);
+            }
+          }
+        }
+      }
+    }
+  }
+  if (candmask)  // collectCandidatesKernel filter.cu:1158-1232
+    for (uint32_t v = 0; v < n; ++v) {
+      uint32_t m = 0;
+      for (uint32_t u = 0; u < k; ++u)
+        if (bit(v, p->last_slot[u])) m |= 1u << u;
+      candmask[v] = m;
+    }
+  return 0;
+}
+
+}  // extern "C"
