@@ -1,0 +1,587 @@
+// api.cu — the C ABI of libsmg: device context, resident graph, plain and
+// batched matching, filter inspection.
+//
+// The reference's main (main.cu:24-175) runs one query per process: it reads
+// both graphs, copies them to the device, filters, joins and prints
+// num_res.  Here the data graph is uploaded once and stays resident; a query
+// costs one filter pass (filter.cu) and one persistent join launch (join.cu)
+// on the context's stream, with scratch taken from a grow-only device arena
+// instead of per-query cudaMalloc/cudaMemset of 2 x k x 2 GB result tables
+// (join.cu:313-319).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+
+#include "api_internal.cuh"
+#include "filter.cuh"
+#include "join.cuh"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace smg {
+
+smg_status cuda_fail(cudaError_t e, const char *what) {
+  cudaGetLastError();  // clear a sticky-free error so the context stays usable
+  const smg_status s = (e == cudaErrorMemoryAllocation) ? SMG_ERR_OOM
+                       : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? SMG_ERR_NO_DEVICE
+                                                                                        : SMG_ERR_CUDA;
+  return fail(s, std::string(what) + ": " + cudaGetErrorName(e) + " " + cudaGetErrorString(e));
+}
+
+// ------------------------------------------------------------------ arena
+smg_status Arena::reserve(size_t bytes) {
+  if (bytes <= cap) return SMG_OK;
+  if (base) cudaFree(base);
+  base = nullptr;
+  cap = 0;
+  const size_t want = bytes + bytes / 4 + (1 << 20);
+  cudaError_t e = cudaMalloc(&base, want);
+  if (e != cudaSuccess) {
+    e = cudaMalloc(&base, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(arena)");
+    cap = bytes;
+  } else {
+    cap = want;
+  }
+  return SMG_OK;
+}
+
+Arena::~Arena() {
+  if (base) cudaFree(base);
+}
+
+uint64_t time_limit_ns() {
+  const char *s = std::getenv("SMG_TIME_LIMIT_S");
+  double v = s ? std::atof(s) : 120.0;
+  if (v <= 0) v = 120.0;
+  return static_cast<uint64_t>(v * 1e9);
+}
+
+}  // namespace smg
+
+using namespace smg;
+
+extern "C" {
+
+smg_status smg_open(int device, smg_ctx **out) {
+  if (!out) return fail(SMG_ERR_INVALID, "null out");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(SMG_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  if (device < 0 || device >= count) return fail(SMG_ERR_INVALID, "device index out of range");
+  std::unique_ptr<smg_ctx> c(new smg_ctx);
+  c->device = device;
+  SMG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  SMG_CUDA(cudaGetDeviceProperties(&prop, device));
+  c->num_sms = prop.multiProcessorCount;
+  SMG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  SMG_CUDA(cudaEventCreate(&c->ev[0]));
+  SMG_CUDA(cudaEventCreate(&c->ev[1]));
+  SMG_CUDA(cudaEventCreate(&c->ev[2]));
+  SMG_CUDA(cudaMallocHost(&c->pinned, kPinnedBytes));
+  *out = c.release();
+  return SMG_OK;
+}
+
+void smg_close(smg_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->arena.~Arena();
+  new (&c->arena) Arena();
+  c->fdev.reset();
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+smg_status smg_graph_upload(smg_ctx *c, const smg_csr *in, smg_graph **out) {
+  if (!c || !in || !out) return fail(SMG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const uint32_t n = in->num_vertices;
+  const uint64_t m2 = 2 * in->num_edges;
+  if (n && (!in->offsets || !in->labels || (m2 && !in->neighbors))) return fail(SMG_ERR_INVALID, "null arrays");
+  if (m2 >= (1ull << 32)) return fail(SMG_ERR_LIMIT, "more than 2^32-1 adjacency entries");
+  if (n == 0xFFFFFFFFu) return fail(SMG_ERR_LIMIT, "too many vertices");
+  if (in->offsets[0] != 0 || in->offsets[n] != m2) return fail(SMG_ERR_INVALID, "offsets do not span 2*num_edges");
+  SMG_CUDA(cudaSetDevice(c->device));
+  std::unique_ptr<smg_graph> G(new smg_graph);
+  DevGraph &g = G->g;
+  g.n = n;
+  g.m2 = m2;
+  // host checks and the sorted copy the device needs
+  std::vector<uint32_t> off32(static_cast<size_t>(n) + 1);
+  bool bad = false, unsorted = false;
+  uint32_t maxl = 0, maxd = 0;
+#pragma omp parallel for schedule(static) reduction(|| : bad) reduction(max : maxl, maxd)
+  for (int64_t v = 0; v < static_cast<int64_t>(n); ++v) {
+    const uint64_t a = in->offsets[v], b = in->offsets[v + 1];
+    off32[v] = static_cast<uint32_t>(a);
+    if (b < a) {
+      bad = true;
+      continue;
+    }
+    maxd = std::max<uint32_t>(maxd, static_cast<uint32_t>(b - a));
+    maxl = std::max(maxl, in->labels[v]);
+  }
+  off32[n] = static_cast<uint32_t>(m2);
+  if (bad) return fail(SMG_ERR_INVALID, "offsets are not monotone");
+#pragma omp parallel for schedule(dynamic, 4096) reduction(|| : bad, unsorted)
+  for (int64_t v = 0; v < static_cast<int64_t>(n); ++v) {
+    for (uint64_t e = in->offsets[v]; e < in->offsets[v + 1]; ++e) {
+      const uint32_t w = in->neighbors[e];
+      if (w >= n || w == static_cast<uint32_t>(v)) bad = true;
+      if (e > in->offsets[v] && in->neighbors[e - 1] >= w) unsorted = true;
+    }
+  }
+  if (bad) return fail(SMG_ERR_INVALID, "neighbour id out of range or self-loop");
+  std::vector<uint32_t> sorted;
+  const uint32_t *adj_src = in->neighbors;
+  if (unsorted) {
+    sorted.assign(in->neighbors, in->neighbors + m2);
+#pragma omp parallel for schedule(dynamic, 4096) reduction(|| : bad)
+    for (int64_t v = 0; v < static_cast<int64_t>(n); ++v) {
+      auto b = sorted.begin() + static_cast<int64_t>(in->offsets[v]);
+      auto e = sorted.begin() + static_cast<int64_t>(in->offsets[v + 1]);
+      std::sort(b, e);
+      if (std::adjacent_find(b, e) != e) bad = true;
+    }
+    if (bad) return fail(SMG_ERR_INVALID, "repeated edge");
+    adj_src = sorted.data();
+  }
+  g.num_labels = n ? maxl + 1 : 0;
+  g.max_degree = maxd;
+  g.label_count.assign(std::min<uint32_t>(g.num_labels, kMaxLabels), 0);
+  for (uint32_t v = 0; v < n; ++v)
+    if (in->labels[v] < kMaxLabels) ++g.label_count[in->labels[v]];
+  const uint32_t ncols = std::min<uint32_t>(g.num_labels, kMaxLabels);
+  g.nlc_stride = std::max<uint32_t>(16, (ncols + 15) & ~15u);
+  const size_t b_off = (static_cast<size_t>(n) + 1) * 4, b_adj = std::max<uint64_t>(m2, 1) * 4,
+               b_lab = std::max<size_t>(n, 1) * 4, b_nlc = std::max<size_t>(n, 1) * g.nlc_stride;
+  SMG_CUDA(cudaMalloc(&g.off, b_off));
+  SMG_CUDA(cudaMalloc(&g.adj, b_adj));
+  SMG_CUDA(cudaMalloc(&g.label, b_lab));
+  SMG_CUDA(cudaMalloc(&g.nlc, b_nlc));
+  g.bytes = b_off + b_adj + b_lab + b_nlc;
+  SMG_CUDA(cudaMemcpyAsync(g.off, off32.data(), b_off, cudaMemcpyHostToDevice, c->stream));
+  if (m2) SMG_CUDA(cudaMemcpyAsync(g.adj, adj_src, m2 * 4, cudaMemcpyHostToDevice, c->stream));
+  if (n) SMG_CUDA(cudaMemcpyAsync(g.label, in->labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
+  smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
+  if (st) return st;
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
+  G->device = c->device;
+  *out = G.release();
+  return SMG_OK;
+}
+
+void smg_graph_free(smg_graph *G) {
+  if (!G) return;
+  cudaSetDevice(G->device);
+  DevGraph &g = G->g;
+  if (g.off) cudaFree(g.off);
+  if (g.adj) cudaFree(g.adj);
+  if (g.label) cudaFree(g.label);
+  if (g.nlc) cudaFree(g.nlc);
+  delete G;
+}
+
+smg_status smg_graph_get_stats(const smg_graph *G, smg_graph_stats *out) {
+  if (!G || !out) return fail(SMG_ERR_INVALID, "null argument");
+  out->num_vertices = G->g.n;
+  out->num_edges = G->g.m2 / 2;
+  out->num_labels = G->g.num_labels;
+  out->max_degree = G->g.max_degree;
+  out->device_bytes = G->g.bytes;
+  return SMG_OK;
+}
+
+}  // extern "C"
+
+namespace smg {
+namespace {
+
+inline size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Device layout of one chunk of queries inside the arena.  Everything that
+// must start at zero (queue state, ready flags, counters, cluster bitmaps) is
+// one contiguous region cleared with a single memset.
+struct Chunk {
+  uint32_t a = 0, b = 0, kmax = 0, cap = 0;
+  size_t zero_bytes = 0, total = 0;
+  QueueState *qs = nullptr;
+  uint32_t *ready = nullptr, *tasks = nullptr, *emb = nullptr;
+  QCounters *counters = nullptr;
+  FilterQuery *fq = nullptr;
+  JoinQuery *jq = nullptr;
+  std::vector<uint32_t *> vmask, enc, cand, roots;
+  std::vector<uint64_t> cand_total;
+};
+
+size_t query_bytes(const DevGraph &g, const Plan &P, uint64_t &cand_total) {
+  cand_total = 0;
+  for (uint32_t u = 0; u < P.k; ++u)
+    cand_total += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
+  const uint64_t rc = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
+  return al(static_cast<size_t>(g.n) * 4) + al(static_cast<size_t>(g.n) * P.num_words * 4) + al(cand_total * 4) +
+         al(rc * 4) + sizeof(QCounters) + al(sizeof(FilterQuery)) + al(sizeof(JoinQuery));
+}
+
+uint32_t seed_tasks(const smg_ctx *c, const RunOpts &o, uint32_t nq) {
+  if (o.max_seed_tasks) return o.max_seed_tasks;
+  const uint32_t warps = static_cast<uint32_t>(c->num_sms) * 64;
+  return std::max<uint32_t>(16, (8 * warps) / std::max<uint32_t>(nq, 1));
+}
+
+smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Chunk &ch, const RunOpts &o) {
+  const uint32_t nq = ch.b - ch.a;
+  ch.kmax = 0;
+  for (uint32_t i = ch.a; i < ch.b; ++i) ch.kmax = std::max(ch.kmax, plans[i]->k);
+  const uint32_t seeds = seed_tasks(c, o, nq);
+  const uint64_t cap64 = static_cast<uint64_t>(nq) * seeds + (2u << 20);
+  ch.cap = static_cast<uint32_t>(std::min<uint64_t>(cap64, 0x7FFFFFFFu));
+  ch.cand_total.resize(nq);
+  // zero region
+  size_t off = 0;
+  const size_t o_qs = off;
+  off += al(sizeof(QueueState));
+  const size_t o_ready = off;
+  off += al(static_cast<size_t>(ch.cap) * 4);
+  const size_t o_cnt = off;
+  off += al(nq * sizeof(QCounters));
+  std::vector<size_t> o_enc(nq), o_vm(nq), o_cand(nq), o_root(nq);
+  for (uint32_t i = 0; i < nq; ++i) {
+    o_enc[i] = off;
+    off += al(static_cast<size_t>(g.n) * plans[ch.a + i]->num_words * 4);
+  }
+  ch.zero_bytes = off;
+  for (uint32_t i = 0; i < nq; ++i) {
+    const Plan &P = *plans[ch.a + i];
+    query_bytes(g, P, ch.cand_total[i]);
+    o_vm[i] = off;
+    off += al(static_cast<size_t>(g.n) * 4);
+    o_cand[i] = off;
+    off += al(ch.cand_total[i] * 4);
+    o_root[i] = off;
+    const uint64_t rc = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
+    off += al(std::max<uint64_t>(rc, 1) * 4);
+  }
+  const size_t o_tasks = off;
+  off += al(static_cast<size_t>(ch.cap) * (4 + ch.kmax) * 4);
+  const size_t o_fq = off;
+  off += al(nq * sizeof(FilterQuery));
+  const size_t o_jq = off;
+  off += al(nq * sizeof(JoinQuery));
+  const size_t o_emb = off;
+  if (o.emb_host && o.emb_cap) off += al(o.emb_cap * ch.kmax * 4);
+  ch.total = off;
+  smg_status st = c->arena.reserve(ch.total);
+  if (st) return st;
+  char *B = c->arena.base;
+  ch.qs = reinterpret_cast<QueueState *>(B + o_qs);
+  ch.ready = reinterpret_cast<uint32_t *>(B + o_ready);
+  ch.counters = reinterpret_cast<QCounters *>(B + o_cnt);
+  ch.tasks = reinterpret_cast<uint32_t *>(B + o_tasks);
+  ch.fq = reinterpret_cast<FilterQuery *>(B + o_fq);
+  ch.jq = reinterpret_cast<JoinQuery *>(B + o_jq);
+  ch.emb = (o.emb_host && o.emb_cap) ? reinterpret_cast<uint32_t *>(B + o_emb) : nullptr;
+  ch.vmask.resize(nq);
+  ch.enc.resize(nq);
+  ch.cand.resize(nq);
+  ch.roots.resize(nq);
+  for (uint32_t i = 0; i < nq; ++i) {
+    ch.enc[i] = reinterpret_cast<uint32_t *>(B + o_enc[i]);
+    ch.vmask[i] = reinterpret_cast<uint32_t *>(B + o_vm[i]);
+    ch.cand[i] = reinterpret_cast<uint32_t *>(B + o_cand[i]);
+    ch.roots[i] = reinterpret_cast<uint32_t *>(B + o_root[i]);
+  }
+  return SMG_OK;
+}
+
+// Host-side query records of a chunk, staged in pinned memory and uploaded.
+smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Chunk &ch, const RunOpts &o) {
+  const uint32_t nq = ch.b - ch.a;
+  const size_t need = nq * (sizeof(FilterQuery) + sizeof(JoinQuery));
+  if (need > kPinnedBytes) return fail(SMG_ERR_INTERNAL, "chunk exceeds the pinned staging buffer");
+  FilterQuery *hf = static_cast<FilterQuery *>(c->pinned);
+  JoinQuery *hj = reinterpret_cast<JoinQuery *>(static_cast<char *>(c->pinned) + nq * sizeof(FilterQuery));
+  FilterBatch fb;
+  for (uint32_t i = 0; i < nq; ++i) {
+    const Plan &P = *plans[ch.a + i];
+    FilterQuery &f = hf[i];
+    smg_status st = fill_filter_query(P, g, f);
+    if (st) return st;
+    uint64_t acc = 0;
+    for (uint32_t u = 0; u < P.k; ++u) {
+      f.cand_off[u] = acc;
+      acc += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
+    }
+    f.cand_off[P.k] = acc;
+    f.vmask = ch.vmask[i];
+    f.enc = ch.enc[i];
+    f.cand = ch.cand[i];
+    f.cand_cnt = ch.counters[i].cand_cnt;
+    f.roots = ch.roots[i];
+    f.num_roots = &ch.counters[i].num_roots;
+    f.stat = ch.counters[i].stat;
+    st = append_filter_steps(P, i, fb);
+    if (st) return st;
+    JoinQuery &j = hj[i];
+    std::memset(&j, 0, sizeof(j));
+    j.k = P.k;
+    for (uint32_t l = 0; l < P.k; ++l) {
+      j.order[l] = P.order[l];
+      j.back_mask[l] = P.back_mask[l];
+      j.same_label[l] = P.same_label_mask[l];
+    }
+    j.candmask = ch.vmask[i];
+    j.roots = ch.roots[i];
+    j.num_roots = &ch.counters[i].num_roots;
+    j.count = &ch.counters[i].count;
+    j.emb = ch.emb;
+    j.emb_cap = ch.emb ? o.emb_cap : 0;
+    j.emb_count = &ch.counters[i].emb_count;
+  }
+  if (!c->fdev) c->fdev.reset(new FilterDev);
+  smg_status st = c->fdev->upload(fb, c->stream);
+  if (st) return st;
+  SMG_CUDA(cudaMemcpyAsync(ch.fq, hf, nq * sizeof(FilterQuery), cudaMemcpyHostToDevice, c->stream));
+  SMG_CUDA(cudaMemcpyAsync(ch.jq, hj, nq * sizeof(JoinQuery), cudaMemcpyHostToDevice, c->stream));
+  SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
+  // the staging buffer is reused by the read-back: finish the copies first
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
+  return SMG_OK;
+}
+
+smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Chunk &ch, const RunOpts &o,
+                     QueryOut *out, RunStats *st) {
+  const uint32_t nq = ch.b - ch.a;
+  smg_status s = stage_chunk(c, g, plans, ch, o);
+  if (s) return s;
+  JoinLaunch jl;
+  std::memset(&jl, 0, sizeof(jl));
+  jl.off = g.off;
+  jl.adj = g.adj;
+  jl.queries = ch.jq;
+  jl.nq = nq;
+  jl.kmax = ch.kmax;
+  jl.qs = ch.qs;
+  jl.tasks = ch.tasks;
+  jl.ready = ch.ready;
+  jl.cap = ch.cap;
+  jl.root_chunk = o.root_chunk;
+  jl.max_seed_tasks = seed_tasks(c, o, nq);
+  jl.donate_min = 33;
+  jl.time_limit_ns = time_limit_ns();
+  jl.emit = ch.emb != nullptr;
+  if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[0], c->stream));
+  s = launch_filter(g, ch.fq, nq, *c->fdev, c->stream, c->num_sms);
+  if (s) return s;
+  if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[1], c->stream));
+  s = launch_join(jl, c->stream, c->num_sms);
+  if (s) return s;
+  if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[2], c->stream));
+  QCounters *hc = static_cast<QCounters *>(c->pinned);
+  QueueState *hq = reinterpret_cast<QueueState *>(static_cast<char *>(c->pinned) + al(nq * sizeof(QCounters)));
+  SMG_CUDA(cudaMemcpyAsync(hc, ch.counters, nq * sizeof(QCounters), cudaMemcpyDeviceToHost, c->stream));
+  SMG_CUDA(cudaMemcpyAsync(hq, ch.qs, sizeof(QueueState), cudaMemcpyDeviceToHost, c->stream));
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
+  if (hq->error) {
+    const char *why = hq->error == JOIN_ERR_DEADLINE ? "join exceeded its time limit (SMG_TIME_LIMIT_S)"
+                      : hq->error == JOIN_ERR_IDLE_TIMEOUT ? "join made no progress for too long"
+                                                            : "a queued task was never published";
+    return fail(SMG_ERR_TIMEOUT, why);
+  }
+  if (hq->pending != 0) return fail(SMG_ERR_INTERNAL, "join ended with pending tasks");
+  for (uint32_t i = 0; i < nq; ++i) {
+    QueryOut &q = out[ch.a + i];
+    q.count = hc[i].count;
+    q.num_roots = hc[i].num_roots;
+    q.cands = hc[i].stat[0];
+    q.walk_entries = hc[i].stat[1];
+    q.initial_cands = 0;
+    for (uint32_t u = 0; u < plans[ch.a + i]->k; ++u) q.initial_cands += hc[i].cand_cnt[u];
+    q.emb_written = ch.emb ? std::min<uint64_t>(hc[i].emb_count, o.emb_cap) : 0;
+    q.overflow = ch.emb ? (hc[i].emb_count > o.emb_cap) : 0;
+    // algorithmic bytes of the filter (see the design doc for the model)
+    const Plan &P = *plans[ch.a + i];
+    uint64_t lab = 0;
+    std::vector<char> seen(kMaxLabels, 0);
+    for (uint32_t u = 0; u < P.k; ++u)
+      if (P.label[u] < g.label_count.size() && !seen[P.label[u]]) {
+        seen[P.label[u]] = 1;
+        lab += g.label_count[P.label[u]];
+      }
+    st->filter_bytes += 12ull * g.n + lab * (8 + 32) + 8ull * q.initial_cands + 8ull * q.walk_entries +
+                        4ull * q.num_roots;
+  }
+  st->tasks += hq->tasks_done;
+  st->donations += hq->donations;
+  st->scanned += hq->scanned;
+  st->descents += hq->descents;
+  st->probes += hq->probes;
+  st->join_bytes += 8ull * hq->scanned + 8ull * hq->descents + 4ull * hq->probes;
+  if (o.profile) {
+    float f = 0, j = 0;
+    cudaEventElapsedTime(&f, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&j, c->ev[1], c->ev[2]);
+    st->filter_ms += f;
+    st->join_ms += j;
+  }
+  if (ch.emb) {
+    const uint64_t rows = out[ch.a].emb_written;
+    if (rows) SMG_CUDA(cudaMemcpy(o.emb_host, ch.emb, rows * plans[ch.a]->k * 4, cudaMemcpyDeviceToHost));
+  }
+  ++st->chunks;
+  return SMG_OK;
+}
+
+}  // namespace
+
+smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, uint32_t nq, const RunOpts &o,
+                       QueryOut *out, RunStats *st) {
+  SMG_CUDA(cudaSetDevice(c->device));
+  if (o.emb_host && nq != 1) return fail(SMG_ERR_INVALID, "embeddings are returned by the plain path only");
+  size_t free_b = 0, total_b = 0;
+  SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const size_t budget = c->arena.cap + (free_b > (2ull << 30) ? free_b - (2ull << 30) : free_b / 2);
+  const size_t per_chunk_fixed = (64ull << 20) * 4;  // queue storage of a chunk (bound)
+  const size_t max_q = kPinnedBytes / (sizeof(FilterQuery) + sizeof(JoinQuery) + sizeof(QCounters));
+  uint32_t a = 0;
+  while (a < nq) {
+    uint32_t b = a;
+    size_t used = per_chunk_fixed;
+    while (b < nq && b - a < max_q) {
+      uint64_t ct;
+      const size_t qb = query_bytes(g, *plans[b], ct);
+      if (b > a && used + qb > budget) break;
+      used += qb;
+      ++b;
+    }
+    Chunk ch;
+    ch.a = a;
+    ch.b = b;
+    smg_status s = layout_chunk(c, g, plans, ch, o);
+    if (s) return s;
+    s = run_chunk(c, g, plans, ch, o, out, st);
+    if (s) return s;
+    a = b;
+  }
+  return SMG_OK;
+}
+
+}  // namespace smg
+
+extern "C" {
+
+smg_status smg_match(smg_ctx *c, const smg_graph *G, const smg_plan *p, const smg_match_opts *opts,
+                     smg_match_result *out) {
+  if (!c || !G || !p || !out) return fail(SMG_ERR_INVALID, "null argument");
+  if (G->device != c->device) return fail(SMG_ERR_INVALID, "graph lives on another device");
+  std::memset(out, 0, sizeof(*out));
+  RunOpts o;
+  if (opts) {
+    o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
+    o.root_chunk = opts->root_chunk;
+    if (opts->flags & SMG_FLAG_EMIT) {
+      if (!opts->embeddings && opts->max_embeddings) return fail(SMG_ERR_INVALID, "null embeddings buffer");
+      o.emb_host = opts->embeddings;
+      o.emb_cap = opts->max_embeddings;
+    }
+  }
+  const Plan *pl = &p->p;
+  QueryOut q;
+  RunStats st;
+  smg_status s = run_queries(c, G->g, &pl, 1, o, &q, &st);
+  if (s) return s;
+  out->count = q.count;
+  out->embeddings_written = q.emb_written;
+  out->overflow = q.overflow;
+  out->num_candidates_root = q.num_roots;
+  out->candidates_total = q.cands;
+  out->filter_ms = st.filter_ms;
+  out->join_ms = st.join_ms;
+  out->tasks = st.tasks;
+  out->filter_bytes = st.filter_bytes;
+  out->join_bytes = st.join_bytes;
+  return SMG_OK;
+}
+
+smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const *plans, uint32_t n,
+                           const smg_match_opts *opts, uint64_t *counts, smg_batch_stats *stats) {
+  if (!c || !G || (n && (!plans || !counts))) return fail(SMG_ERR_INVALID, "null argument");
+  if (G->device != c->device) return fail(SMG_ERR_INVALID, "graph lives on another device");
+  if (opts && (opts->flags & SMG_FLAG_EMIT)) return fail(SMG_ERR_INVALID, "the batched path returns counts only");
+  std::vector<const Plan *> pl(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!plans[i]) return fail(SMG_ERR_INVALID, "null plan in batch");
+    pl[i] = &plans[i]->p;
+  }
+  RunOpts o;
+  if (opts) {
+    o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
+    o.root_chunk = opts->root_chunk;
+  }
+  std::vector<QueryOut> q(n);
+  RunStats st;
+  smg_status s = run_queries(c, G->g, pl.data(), n, o, q.data(), &st);
+  if (s) return s;
+  uint64_t tot = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    counts[i] = q[i].count;
+    tot += q[i].count;
+  }
+  if (stats) {
+    stats->filter_ms = st.filter_ms;
+    stats->join_ms = st.join_ms;
+    stats->tasks = st.tasks;
+    stats->total_embeddings = tot;
+  }
+  return SMG_OK;
+}
+
+smg_status smg_filter_inspect(smg_ctx *c, const smg_graph *G, const smg_plan *p, uint32_t *vmask0,
+                              uint32_t *encodings, uint32_t *candmask) {
+  if (!c || !G || !p) return fail(SMG_ERR_INVALID, "null argument");
+  SMG_CUDA(cudaSetDevice(c->device));
+  const Plan *pl = &p->p;
+  const DevGraph &g = G->g;
+  RunOpts o;
+  Chunk ch;
+  ch.a = 0;
+  ch.b = 1;
+  smg_status s = layout_chunk(c, g, &pl, ch, o);
+  if (s) return s;
+  s = stage_chunk(c, g, &pl, ch, o);
+  if (s) return s;
+  s = launch_nlc_filter(g, ch.fq, 1, c->stream, c->num_sms);
+  if (s) return s;
+  if (vmask0)
+    SMG_CUDA(cudaMemcpyAsync(vmask0, ch.vmask[0], static_cast<size_t>(g.n) * 4, cudaMemcpyDeviceToHost, c->stream));
+  s = launch_walks(g, ch.fq, *c->fdev, c->stream, c->num_sms);
+  if (s) return s;
+  s = launch_collect(g, ch.fq, 1, c->stream, c->num_sms);
+  if (s) return s;
+  if (encodings)
+    SMG_CUDA(cudaMemcpyAsync(encodings, ch.enc[0], static_cast<size_t>(g.n) * pl->num_words * 4,
+                             cudaMemcpyDeviceToHost, c->stream));
+  if (candmask)
+    SMG_CUDA(cudaMemcpyAsync(candmask, ch.vmask[0], static_cast<size_t>(g.n) * 4, cudaMemcpyDeviceToHost, c->stream));
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
+  return SMG_OK;
+}
+
+}  // extern "C"

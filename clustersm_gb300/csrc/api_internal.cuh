@@ -1,0 +1,87 @@
+// api_internal.cuh — context, resident-graph and run structures behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "device.cuh"
+#include "filter.cuh"
+#include "join.cuh"
+
+namespace smg {
+
+constexpr size_t kPinnedBytes = 32u << 20;
+
+// Grow-only device buffer; each run carves its scratch out of it.
+struct Arena {
+  char *base = nullptr;
+  size_t cap = 0;
+  smg_status reserve(size_t bytes);
+  Arena() = default;
+  Arena(const Arena &) = delete;
+  Arena &operator=(const Arena &) = delete;
+  ~Arena();
+};
+
+// Per-query counters (zeroed before each run).
+struct QCounters {
+  uint32_t cand_cnt[kMaxK];    // initial candidates appended per query vertex
+  uint32_t num_roots;          // root candidates after the bitmap filter
+  uint32_t pad[3];
+  unsigned long long stat[4];  // [0] sum |C(u)| final, [1] walk list entries
+  unsigned long long count;    // embeddings
+  unsigned long long emb_count;
+  unsigned long long pad2[8];
+};
+static_assert(sizeof(QCounters) % 16 == 0, "QCounters must keep 16-byte alignment");
+
+uint64_t time_limit_ns();
+
+// Options of one run (plain path: one query; batched: many).
+struct RunOpts {
+  bool profile = false;
+  uint32_t root_chunk = 0;
+  uint32_t max_seed_tasks = 0;   // 0: derived from the device size
+  uint32_t *emb_host = nullptr;  // plain path only
+  uint64_t emb_cap = 0;
+  bool use_graph = false;        // capture the launches in a CUDA graph
+};
+
+struct QueryOut {
+  uint64_t count = 0, emb_written = 0, cands = 0, walk_entries = 0;
+  uint32_t num_roots = 0, overflow = 0;
+  uint64_t initial_cands = 0;
+};
+
+struct RunStats {
+  float filter_ms = 0, join_ms = 0;
+  uint64_t tasks = 0, donations = 0, scanned = 0, descents = 0, probes = 0;
+  uint64_t filter_bytes = 0, join_bytes = 0;
+  uint32_t chunks = 0;
+};
+
+}  // namespace smg
+
+struct smg_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  void *pinned = nullptr;  // kPinnedBytes of page-locked staging
+  smg::Arena arena;
+  std::unique_ptr<smg::FilterDev> fdev;
+};
+
+struct smg_graph {
+  int device = 0;
+  smg::DevGraph g;
+};
+
+namespace smg {
+// Filter + join for `nq` plans against a resident graph; splits into chunks
+// that fit the device memory.  out[i] receives plan i's results.
+smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, uint32_t nq, const RunOpts &o,
+                       QueryOut *out, RunStats *st);
+}  // namespace smg

@@ -1,0 +1,121 @@
+// device.cuh — device-side data layout shared by the filter, the join and the
+// C-ABI implementation.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "host.h"
+
+namespace smg {
+
+constexpr uint32_t kMaxK = SMG_MAX_QUERY_VERTICES;  // query vertices (u-bitmask width)
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr int kWarp = 32;
+
+// CUDA status -> smg_status with a message naming the call site.
+smg_status cuda_fail(cudaError_t e, const char *what);
+#define SMG_CUDA(call)                                                  \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) return ::smg::cuda_fail(e_, #call);          \
+  } while (0)
+
+// ------------------------------------------------------------ resident graph
+// The data graph lives in HBM for as long as the smg_graph handle.  Neighbour
+// lists are sorted so that non-tree edges are checked by binary search.
+struct DevGraph {
+  uint32_t n = 0;
+  uint64_t m2 = 0;            // directed adjacency entries (2|E|)
+  uint32_t num_labels = 0;    // largest label + 1
+  uint32_t nlc_stride = 0;    // bytes per vertex in `nlc` (multiple of 16)
+  uint32_t max_degree = 0;
+  uint32_t *off = nullptr;    // [n+1]  (2|E| < 2^32 is required)
+  uint32_t *adj = nullptr;    // [2|E|] sorted per vertex
+  uint32_t *label = nullptr;  // [n]
+  uint8_t *nlc = nullptr;     // [n][nlc_stride] neighbour-label counts, saturated at 255
+  std::vector<uint64_t> label_count;  // vertices per label (host copy)
+  uint64_t bytes = 0;
+};
+
+// ------------------------------------------------------ per-query filter plan
+// One star / merge / combine step of the cluster bitmap, flattened for the
+// device.  Slot bits of a cluster are set per 32-bit word: for a word group,
+// `qmask` holds the query vertices whose slot lies in that word and `pos[u]`
+// the bit of u's slot inside it.
+struct WordGroup {
+  uint32_t word;   // word index within a vertex's num_words words
+  uint32_t qmask;  // query vertices with a slot in this word (neighbour slots)
+  uint8_t pos[kMaxK];
+};
+
+struct ClusterStep {
+  uint32_t kind;          // 0 star, 1 merge, 2 combine
+  uint32_t core;          // query vertex whose candidates are walked
+  uint32_t core_slot;     // slot of the core in this cluster
+  uint32_t left_pos, right_pos;  // merge: slots tested on the candidate
+  uint32_t type;          // combine: 0 new cluster, 1 in place
+  uint32_t num_groups;    // word groups of the neighbour slots (<= 2)
+  WordGroup groups[2];
+  // combine only, in the batch's aux array:
+  //   aux[others_off + o]  core slot of the o-th other cluster
+  //   from aux[targets_off], per neighbour slot of this cluster:
+  //     slot, nsrc, then the nsrc slots holding the same vertex in the others
+  uint32_t num_others, others_off;
+  uint32_t num_targets, targets_off;
+};
+
+// Kernels of one launch walk the candidates of a group of steps sharing a
+// core: merges with the same core in one layer must see each other's
+// removals in cluster order (filter.cu:718).
+struct StepGroup {
+  uint32_t query;        // index into the batch
+  uint32_t core;
+  uint32_t first, count; // steps [first, first+count) of the step array
+};
+
+// Per-query device state (filter scratch and join inputs).
+struct QueryDev {
+  uint32_t k = 0, words = 0, nvlq = 0;
+  uint32_t *vmask = nullptr;   // [n]: initial masks, overwritten by final masks
+  uint32_t *enc = nullptr;     // [n * words] cluster bitmap
+  uint32_t *cand = nullptr;    // candidate lists of the initial filter, [k] segments
+  uint32_t *cand_cnt = nullptr;// [k] (device), entries used per segment
+  std::vector<uint64_t> cand_off;  // [k+1] segment offsets (host)
+  uint32_t *roots = nullptr;   // root candidate list (after the bitmap filter)
+};
+
+// Query-side constants the filter kernels read (one per query in a batch).
+struct FilterQuery {
+  uint32_t k, words, nvlq;
+  uint32_t label[kMaxK];
+  uint32_t deg[kMaxK];
+  uint32_t nnlc[kMaxK];          // non-zero neighbour-label counts of u
+  uint16_t nlc_label[kMaxK][kMaxK];
+  uint8_t nlc_count[kMaxK][kMaxK];
+  uint32_t last_slot[kMaxK];
+  uint32_t root;
+  uint64_t cand_off[kMaxK + 1];
+  uint32_t *vmask, *enc, *cand, *cand_cnt, *roots, *num_roots;
+  unsigned long long *stat;       // [0] sum over u of final |C(u)|, [1] walk list entries
+};
+
+// Query-side constants the join reads.
+struct JoinQuery {
+  uint32_t k;
+  uint32_t order[kMaxK];      // query vertex matched at each level
+  uint32_t back_mask[kMaxK];  // earlier levels adjacent to the level's vertex
+  uint32_t same_label[kMaxK]; // earlier levels with the same label (injectivity)
+  const uint32_t *candmask;   // [n] final candidate masks
+  const uint32_t *roots;      // root candidates
+  const uint32_t *num_roots;  // device counter
+  unsigned long long *count;  // result
+  uint32_t *emb;              // optional embedding rows [emb_cap][k]
+  unsigned long long emb_cap;
+  unsigned long long *emb_count;
+};
+
+}  // namespace smg

@@ -1,0 +1,496 @@
+// filter.cu — the bitmap-encoded cluster candidate filter on sm_103a.
+//
+//   k_build_nlc     per-vertex neighbour-label counts, once per resident graph
+//   k_nlc_filter    label / degree / NLC test (filter.cu:404-539 of the reference)
+//   k_cluster_walk  star encode, merge and combine steps of one layer
+//                   (encodeKernel filter.cu:585-653, mergeKernel 656-746,
+//                   combineMultipleClustersKernel 749-873)
+//   k_collect       final per-vertex candidate masks and the root list
+//                   (collectCandidatesKernel filter.cu:1158-1232)
+//
+// All of it is integer, HBM-bound work: coalesced sweeps over the vertex
+// arrays, warp-per-candidate walks over neighbour lists, and warp-aggregated
+// atomics for appends.  Differences from the reference, all on purpose:
+//  * neighbour-label counts of data vertices are computed once per graph
+//    (saturated at 255 >= any query count) instead of once per query;
+//  * every kernel is sized to the device (the reference launches the encode
+//    kernels with a single block because the host count it sizes them by is
+//    still zero, filter.cu:982-983 vs main.cu:102-103);
+//  * the steps of one layer run in one launch per phase, and each combine runs
+//    at the end of its own layer with the intended AND semantics (the
+//    reference negates the combined bit and strides by the wrong width,
+//    filter.cu:858-863, and runs new-cluster combines one layer late);
+//  * labels of any value below 256 are supported (the reference overflows its
+//    shared NLC table for query labels >= 16, filter.cu:425-426).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+#include "device.cuh"
+#include "filter.cuh"
+
+namespace smg {
+
+namespace {
+
+__device__ __forceinline__ bool enc_bit(const uint32_t *enc, uint32_t W, uint32_t v, uint32_t s) {
+  return (enc[static_cast<size_t>(v) * W + (s >> 5)] >> (s & 31)) & 1u;
+}
+
+__device__ __forceinline__ void enc_set(uint32_t *enc, uint32_t W, uint32_t v, uint32_t word, uint32_t mask) {
+  uint32_t *p = enc + static_cast<size_t>(v) * W + word;
+  if ((*p & mask) != mask) atomicOr(p, mask);
+}
+
+__device__ __forceinline__ void enc_clear(uint32_t *enc, uint32_t W, uint32_t v, uint32_t s) {
+  uint32_t *p = enc + static_cast<size_t>(v) * W + (s >> 5);
+  const uint32_t b = 1u << (s & 31);
+  if (*p & b) atomicAnd(p, ~b);
+}
+
+// ---------------------------------------------------------------- NLC table
+// One warp per vertex: lanes stride the neighbour list and count labels in a
+// per-warp shared histogram, then write saturated bytes.
+__global__ void k_build_nlc(uint32_t n, const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                            const uint32_t *__restrict__ label, uint32_t ncols, uint32_t stride,
+                            uint8_t *__restrict__ nlc) {
+  extern __shared__ uint32_t hist[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint32_t *h = hist + wib * ncols;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t v = blockIdx.x * (blockDim.x >> 5) + wib; v < n; v += warps) {
+    for (uint32_t c = lane; c < ncols; c += 32) h[c] = 0;
+    __syncwarp();
+    for (uint32_t e = off[v] + lane; e < off[v + 1]; e += 32) {
+      const uint32_t l = label[adj[e]];
+      if (l < ncols) atomicAdd_block(&h[l], 1u);
+    }
+    __syncwarp();
+    uint8_t *row = nlc + static_cast<size_t>(v) * stride;
+    for (uint32_t c = lane; c < stride; c += 32) row[c] = c < ncols ? static_cast<uint8_t>(min(h[c], 255u)) : 0;
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------ initial filter
+// Thread per data vertex (coalesced over labels and masks).  Candidates are
+// appended to per-u lists with one atomic per warp and query vertex.
+__global__ void __launch_bounds__(256) k_nlc_filter(uint32_t n, const uint32_t *__restrict__ off,
+                                                    const uint32_t *__restrict__ label,
+                                                    const uint8_t *__restrict__ nlc, uint32_t stride,
+                                                    const FilterQuery *__restrict__ qs) {
+  __shared__ FilterQuery Q;
+  const FilterQuery *src = qs + blockIdx.y;
+  for (uint32_t i = threadIdx.x; i < sizeof(FilterQuery) / 4; i += blockDim.x)
+    reinterpret_cast<uint32_t *>(&Q)[i] = reinterpret_cast<const uint32_t *>(src)[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const uint32_t k = Q.k;
+  const uint32_t total = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += total) {
+    const uint32_t v = base + threadIdx.x;
+    uint32_t mask = 0;
+    if (v < n) {
+      const uint32_t lv = label[v];
+      uint32_t same = 0;
+      for (uint32_t u = 0; u < k; ++u) same |= (Q.label[u] == lv) ? (1u << u) : 0u;
+      if (same) {
+        const uint32_t dv = off[v + 1] - off[v];
+        const uint8_t *row = nlc + static_cast<size_t>(v) * stride;
+        for (uint32_t b = same; b; b &= b - 1) {
+          const uint32_t u = __ffs(b) - 1;
+          if (Q.deg[u] > dv) continue;
+          bool ok = true;
+          for (uint32_t i = 0; i < Q.nnlc[u] && ok; ++i) ok = row[Q.nlc_label[u][i]] >= Q.nlc_count[u][i];
+          if (ok) mask |= 1u << u;
+        }
+      }
+      Q.vmask[v] = mask;
+    }
+    // warp-aggregated appends, one atomic per query vertex present in the warp
+    uint32_t any = __reduce_or_sync(0xFFFFFFFFu, mask);
+    for (; any; any &= any - 1) {
+      const uint32_t u = __ffs(any) - 1;
+      const uint32_t bal = __ballot_sync(0xFFFFFFFFu, (mask >> u) & 1u);
+      uint32_t pos = 0;
+      if (lane == 0) pos = atomicAdd(Q.cand_cnt + u, __popc(bal));
+      pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+      if ((mask >> u) & 1u) Q.cand[Q.cand_off[u] + pos + __popc(bal & ((1u << lane) - 1))] = v;
+    }
+  }
+}
+
+// ----------------------------------------------------- cluster bitmap steps
+// Grid: x strides the candidates of the group's core, y indexes the group.
+// One warp per candidate v of the core:
+//   star    set the core slot on v, then the neighbour slots on N(v)
+//   merge   for each merge of the group in cluster order: v keeps going only
+//           while both connection slots are set; failing v become holes
+//   combine core slot = AND of the other clusters' core slots; neighbour
+//           slot = AND of the same vertex's slots in the other clusters
+__device__ __forceinline__ void spread_slots(const ClusterStep &st, uint32_t xm, uint32_t *enc, uint32_t W,
+                                             uint32_t w) {
+  for (uint32_t gi = 0; gi < st.num_groups; ++gi) {
+    const WordGroup &gr = st.groups[gi];
+    uint32_t y = xm & gr.qmask, mask = 0;
+    for (; y; y &= y - 1) mask |= 1u << gr.pos[__ffs(y) - 1];
+    if (mask) enc_set(enc, W, w, gr.word, mask);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict__ off,
+                                                      const uint32_t *__restrict__ adj,
+                                                      const StepGroup *__restrict__ groups,
+                                                      const ClusterStep *__restrict__ steps,
+                                                      const uint32_t *__restrict__ aux,
+                                                      const FilterQuery *__restrict__ qs) {
+  const StepGroup G = groups[blockIdx.y];
+  const FilterQuery &Q = qs[G.query];
+  const int lane = threadIdx.x & 31;
+  const uint32_t W = Q.words;
+  uint32_t *const enc = Q.enc;
+  const uint32_t *const vmask = Q.vmask;
+  uint32_t *const list = Q.cand + Q.cand_off[G.core];
+  const uint32_t cnt = *(volatile const uint32_t *)(Q.cand_cnt + G.core);
+  const uint32_t kind = steps[G.first].kind;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  unsigned long long scanned = 0;
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < cnt; i += warps) {
+    const uint32_t v = list[i];
+    if (v == kNone) continue;  // removed by an earlier merge
+    uint32_t pass = 0;         // steps of the group that v passed
+    if (kind == 0) {
+      const ClusterStep &st = steps[G.first];
+      if (lane == 0) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+      pass = 1;
+    } else if (kind == 1) {
+      bool alive = true;
+      for (uint32_t j = 0; j < G.count && alive; ++j) {
+        const ClusterStep &st = steps[G.first + j];
+        if (enc_bit(enc, W, v, st.left_pos) && enc_bit(enc, W, v, st.right_pos)) {
+          pass |= 1u << j;
+          if (lane == 0) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+        } else {
+          alive = false;
+        }
+      }
+      if (!alive && lane == 0) list[i] = kNone;
+    } else {
+      const ClusterStep &st = steps[G.first];
+      bool all = true;
+      for (uint32_t o = 0; o < st.num_others && all; ++o) all = enc_bit(enc, W, v, aux[st.others_off + o]);
+      if (lane == 0) {
+        if (st.type == 0) {
+          if (all) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+        } else if (!all) {
+          enc_clear(enc, W, v, st.core_slot);
+        }
+      }
+    }
+    if (kind != 2 && pass == 0) continue;
+    scanned += off[v + 1] - off[v];
+    for (uint32_t e = off[v] + lane; e < off[v + 1]; e += 32) {
+      const uint32_t w = adj[e];
+      if (kind != 2) {
+        const uint32_t xm = vmask[w];
+        if (!xm) continue;
+        for (uint32_t p = pass; p; p &= p - 1) spread_slots(steps[G.first + __ffs(p) - 1], xm, enc, W, w);
+      } else {
+        const ClusterStep &st = steps[G.first];
+        uint32_t t = st.targets_off;
+        for (uint32_t ti = 0; ti < st.num_targets; ++ti) {
+          const uint32_t slot = aux[t], nsrc = aux[t + 1];
+          bool fin = true;
+          for (uint32_t s = 0; s < nsrc && fin; ++s) fin = enc_bit(enc, W, w, aux[t + 2 + s]);
+          t += 2 + nsrc;
+          if (st.type == 0) {
+            if (fin) enc_set(enc, W, w, slot >> 5, 1u << (slot & 31));
+          } else if (!fin) {
+            enc_clear(enc, W, w, slot);
+          }
+        }
+      }
+    }
+  }
+  if (lane == 0 && scanned) atomicAdd(Q.stat + 1, scanned);
+}
+
+// --------------------------------------------------------------- collect
+// Thread per vertex: bit u of the final mask is the bit of u's last slot.
+// Vertices with no initial candidate bit are skipped (the bitmap can only
+// hold bits the initial filter allowed).  Root candidates are appended with
+// a warp-aggregated atomic.
+__global__ void __launch_bounds__(256) k_collect(uint32_t n, const FilterQuery *__restrict__ qs) {
+  __shared__ uint32_t last_slot[kMaxK];
+  const FilterQuery &Q = qs[blockIdx.y];
+  if (threadIdx.x < kMaxK) last_slot[threadIdx.x] = Q.last_slot[threadIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const uint32_t W = Q.words, root = Q.root;
+  uint32_t *const vmask = Q.vmask;
+  const uint32_t *const enc = Q.enc;
+  unsigned long long ncand = 0;
+  const uint32_t total = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += total) {
+    const uint32_t v = base + threadIdx.x;
+    uint32_t cm = 0;
+    if (v < n) {
+      const uint32_t m0 = vmask[v];
+      for (uint32_t b = m0; b; b &= b - 1) {
+        const uint32_t u = __ffs(b) - 1;
+        if (enc_bit(enc, W, v, last_slot[u])) cm |= 1u << u;
+      }
+      if (m0 != cm) vmask[v] = cm;
+      ncand += __popc(cm);
+    }
+    const bool is_root = (cm >> root) & 1u;
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, is_root);
+    if (bal) {
+      uint32_t pos = 0;
+      if (lane == 0) pos = atomicAdd(Q.num_roots, __popc(bal));
+      pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+      if (is_root) Q.roots[pos + __popc(bal & ((1u << lane) - 1))] = v;
+    }
+  }
+  for (int o = 16; o; o >>= 1) ncand += __shfl_down_sync(0xFFFFFFFFu, ncand, o);
+  if (lane == 0 && ncand) atomicAdd(Q.stat, ncand);
+}
+
+}  // namespace
+
+// ======================================================================
+// host side
+// ======================================================================
+
+smg_status launch_build_nlc(DevGraph &g, cudaStream_t s, int num_sms) {
+  const uint32_t ncols = std::min<uint32_t>(g.num_labels, kMaxLabels);
+  const int threads = 256;
+  const size_t smem = static_cast<size_t>(threads / 32) * ncols * sizeof(uint32_t);
+  const uint32_t blocks = std::max<uint32_t>(1, std::min<uint64_t>((g.n + 7) / 8, static_cast<uint64_t>(num_sms) * 16));
+  if (g.n) k_build_nlc<<<blocks, threads, smem, s>>>(g.n, g.off, g.adj, g.label, ncols, g.nlc_stride, g.nlc);
+  SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
+
+smg_status fill_filter_query(const Plan &P, const DevGraph &g, FilterQuery &fq) {
+  std::memset(&fq, 0, sizeof(fq));
+  const uint32_t ncols = std::min<uint32_t>(g.num_labels, kMaxLabels);
+  fq.k = P.k;
+  fq.words = P.num_words;
+  fq.nvlq = P.nvlq;
+  fq.root = P.root;
+  for (uint32_t u = 0; u < P.k; ++u) {
+    if (P.label[u] >= kMaxLabels) return fail(SMG_ERR_LIMIT, "query labels must be below 256");
+    fq.label[u] = P.label[u];
+    fq.deg[u] = P.deg[u];
+    fq.last_slot[u] = P.last_slot[u];
+    uint32_t c = 0;
+    for (uint32_t l = 0; l < P.nvlq; ++l) {
+      const uint32_t cnt = P.nlc[u * P.nvlq + l];
+      if (!cnt) continue;
+      if (l >= ncols) fq.deg[u] = kNone;  // no data vertex carries label l: u has no candidate
+      fq.nlc_label[u][c] = static_cast<uint16_t>(l < ncols ? l : 0);
+      fq.nlc_count[u][c] = static_cast<uint8_t>(cnt);
+      ++c;
+    }
+    fq.nnlc[u] = c;
+  }
+  return SMG_OK;
+}
+
+namespace {
+
+void word_groups(const Plan &P, uint32_t c, ClusterStep &st) {
+  st.num_groups = 0;
+  for (uint32_t s = P.cl_off[c] + 1; s < P.cl_off[c + 1]; ++s) {
+    const uint32_t word = s >> 5;
+    WordGroup *gr = nullptr;
+    for (uint32_t i = 0; i < st.num_groups; ++i)
+      if (st.groups[i].word == word) gr = &st.groups[i];
+    if (!gr) {
+      gr = &st.groups[st.num_groups++];
+      gr->word = word;
+      gr->qmask = 0;
+    }
+    const uint32_t u = P.slots[s];
+    gr->qmask |= 1u << u;
+    gr->pos[u] = static_cast<uint8_t>(s & 31);
+  }
+}
+
+}  // namespace
+
+smg_status append_filter_steps(const Plan &P, uint32_t qi, FilterBatch &fb) {
+  const uint32_t phases = 2 * P.num_layers - 1;
+  if (fb.phases.size() < phases) fb.phases.resize(phases);
+  std::vector<int64_t> merge_of(P.clusters.size(), -1);
+  for (size_t r = 0; r < P.mg_cluster.size(); ++r) merge_of[P.mg_cluster[r]] = static_cast<int64_t>(r);
+  auto base_step = [&](uint32_t c, uint32_t kind) {
+    ClusterStep st;
+    std::memset(&st, 0, sizeof(st));
+    st.kind = kind;
+    st.core_slot = P.cl_off[c];
+    st.core = P.slots[st.core_slot];
+    word_groups(P, c, st);
+    return st;
+  };
+  // phase 0: stars of layer 0, one group each
+  for (uint32_t c = P.layer_begin[0]; c < P.layer_begin[1]; ++c) {
+    ClusterStep st = base_step(c, 0);
+    fb.phases[0].push_back({qi, st.core, static_cast<uint32_t>(fb.steps.size()), 1});
+    fb.steps.push_back(st);
+  }
+  for (uint32_t layer = 1; layer < P.num_layers; ++layer) {
+    // merges of this layer grouped by core, clusters in index order
+    std::vector<uint32_t> cores;
+    std::map<uint32_t, std::vector<uint32_t>> by_core;
+    for (uint32_t c = P.layer_begin[layer]; c < P.layer_begin[layer + 1]; ++c) {
+      if (P.cl_kind[c] != 1) continue;
+      const uint32_t core = P.slots[P.cl_off[c]];
+      if (!by_core.count(core)) cores.push_back(core);
+      by_core[core].push_back(c);
+    }
+    for (uint32_t core : cores) {
+      StepGroup gr{qi, core, static_cast<uint32_t>(fb.steps.size()), 0};
+      for (uint32_t c : by_core[core]) {
+        const int64_t r = merge_of[c];
+        if (r < 0) return fail(SMG_ERR_INTERNAL, "merge cluster without a merge record");
+        ClusterStep st = base_step(c, 1);
+        st.left_pos = P.mg_left_pos[r];
+        st.right_pos = P.mg_right_pos[r];
+        fb.steps.push_back(st);
+        ++gr.count;
+      }
+      if (gr.count > 32) return fail(SMG_ERR_LIMIT, "more than 32 merges share a core in one layer");
+      fb.phases[2 * layer - 1].push_back(gr);
+    }
+    // combines of this layer
+    for (const CombineRec &rec : P.combines) {
+      if (rec.layer != layer) continue;
+      ClusterStep st = base_step(rec.out, 2);
+      st.type = rec.type;
+      st.num_others = static_cast<uint32_t>(rec.others.size());
+      st.others_off = static_cast<uint32_t>(fb.aux.size());
+      for (uint32_t o : rec.others) fb.aux.push_back(P.cl_off[o]);
+      st.targets_off = static_cast<uint32_t>(fb.aux.size());
+      st.num_targets = 0;
+      for (uint32_t s = P.cl_off[rec.out] + 1; s < P.cl_off[rec.out + 1]; ++s) {
+        const uint32_t u = P.slots[s];
+        fb.aux.push_back(s);
+        const size_t nsrc_at = fb.aux.size();
+        fb.aux.push_back(0);
+        for (uint32_t o : rec.others)
+          for (uint32_t t = P.cl_off[o]; t < P.cl_off[o + 1]; ++t)
+            if (P.slots[t] == u) {
+              fb.aux.push_back(t);
+              ++fb.aux[nsrc_at];
+              break;
+            }
+        ++st.num_targets;
+      }
+      fb.phases[2 * layer].push_back({qi, st.core, static_cast<uint32_t>(fb.steps.size()), 1});
+      fb.steps.push_back(st);
+    }
+  }
+  return SMG_OK;
+}
+
+smg_status FilterDev::upload(const FilterBatch &fb, cudaStream_t s) {
+  phase_first.clear();
+  phase_count.clear();
+  std::vector<StepGroup> flat;
+  for (const auto &ph : fb.phases) {
+    phase_first.push_back(static_cast<uint32_t>(flat.size()));
+    phase_count.push_back(static_cast<uint32_t>(ph.size()));
+    flat.insert(flat.end(), ph.begin(), ph.end());
+  }
+  const size_t bytes_steps = fb.steps.size() * sizeof(ClusterStep);
+  const size_t bytes_groups = flat.size() * sizeof(StepGroup);
+  const size_t bytes_aux = fb.aux.size() * sizeof(uint32_t);
+  auto al256 = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t need = al256(bytes_steps) + al256(bytes_groups) + al256(bytes_aux) + 256;
+  if (need > cap) {
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    cap = 0;
+    SMG_CUDA(cudaMalloc(&buf, need));
+    cap = need;
+  }
+  host.resize(need);
+  size_t o = 0;
+  auto put = [&](const void *src, size_t n) {
+    size_t at = o;
+    if (n) std::memcpy(host.data() + o, src, n);
+    o = (o + n + 255) & ~size_t(255);
+    return at;
+  };
+  const size_t os = put(fb.steps.data(), bytes_steps);
+  const size_t og = put(flat.data(), bytes_groups);
+  const size_t oa = put(fb.aux.data(), bytes_aux);
+  steps = reinterpret_cast<ClusterStep *>(static_cast<char *>(buf) + os);
+  groups = reinterpret_cast<StepGroup *>(static_cast<char *>(buf) + og);
+  aux = reinterpret_cast<uint32_t *>(static_cast<char *>(buf) + oa);
+  SMG_CUDA(cudaMemcpyAsync(buf, host.data(), o, cudaMemcpyHostToDevice, s));
+  // the staging buffer must outlive the copy
+  SMG_CUDA(cudaStreamSynchronize(s));
+  return SMG_OK;
+}
+
+FilterDev::~FilterDev() {
+  if (buf) cudaFree(buf);
+}
+
+static uint32_t vertex_blocks(const DevGraph &g, uint32_t nq, int num_sms) {
+  const uint32_t vblocks = static_cast<uint32_t>((static_cast<uint64_t>(g.n) + 255) / 256);
+  return std::max<uint32_t>(1, std::min<uint32_t>(vblocks, (num_sms * 16u + nq - 1) / nq));
+}
+
+smg_status launch_nlc_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, cudaStream_t s, int num_sms) {
+  if (!nq || !g.n) return SMG_OK;
+  for (uint32_t y0 = 0; y0 < nq; y0 += 65535) {
+    const uint32_t ny = std::min<uint32_t>(65535, nq - y0);
+    k_nlc_filter<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.n, g.off, g.label, g.nlc, g.nlc_stride,
+                                                                         d_qs + y0);
+    SMG_CUDA(cudaGetLastError());
+  }
+  return SMG_OK;
+}
+
+smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const FilterDev &fd, cudaStream_t s,
+                        int num_sms) {
+  for (size_t p = 0; p < fd.phase_count.size(); ++p) {
+    const uint32_t ng = fd.phase_count[p];
+    if (!ng) continue;
+    const uint32_t wx = std::max<uint32_t>(1, std::min<uint32_t>(2048, (num_sms * 16u + ng - 1) / ng));
+    for (uint32_t y0 = 0; y0 < ng; y0 += 65535) {
+      const uint32_t ny = std::min<uint32_t>(65535, ng - y0);
+      k_cluster_walk<<<dim3(wx, ny), 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p] + y0, fd.steps,
+                                                  fd.aux, d_qs);
+      SMG_CUDA(cudaGetLastError());
+    }
+  }
+  return SMG_OK;
+}
+
+smg_status launch_collect(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, cudaStream_t s, int num_sms) {
+  if (!nq || !g.n) return SMG_OK;
+  for (uint32_t y0 = 0; y0 < nq; y0 += 65535) {
+    const uint32_t ny = std::min<uint32_t>(65535, nq - y0);
+    k_collect<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.n, d_qs + y0);
+    SMG_CUDA(cudaGetLastError());
+  }
+  return SMG_OK;
+}
+
+smg_status launch_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, const FilterDev &fd,
+                         cudaStream_t s, int num_sms) {
+  smg_status st = launch_nlc_filter(g, d_qs, nq, s, num_sms);
+  if (st) return st;
+  st = launch_walks(g, d_qs, fd, s, num_sms);
+  if (st) return st;
+  return launch_collect(g, d_qs, nq, s, num_sms);
+}
+
+}  // namespace smg

@@ -1,0 +1,53 @@
+// filter.cuh — host interface of the candidate filter (filter.cu).
+#pragma once
+
+#include <vector>
+
+#include "device.cuh"
+
+namespace smg {
+
+// Neighbour-label counts are kept for labels below this bound.
+constexpr uint32_t kMaxLabels = 256;
+
+// Steps of the cluster bitmap for a batch of queries, grouped into phases:
+// phase 0 = stars of layer 0; phase 2l-1 = merges of layer l; phase 2l =
+// combines of layer l.  Queries of a batch share the phases, so a batch runs
+// 2 * max_layers - 1 walk launches whatever its size.
+struct FilterBatch {
+  std::vector<ClusterStep> steps;
+  std::vector<uint32_t> aux;
+  std::vector<std::vector<StepGroup>> phases;
+};
+
+// The steps of a batch in device memory.
+struct FilterDev {
+  void *buf = nullptr;
+  size_t cap = 0;
+  std::vector<char> host;
+  ClusterStep *steps = nullptr;
+  StepGroup *groups = nullptr;
+  uint32_t *aux = nullptr;
+  std::vector<uint32_t> phase_first, phase_count;
+  smg_status upload(const FilterBatch &fb, cudaStream_t s);
+  FilterDev() = default;
+  FilterDev(const FilterDev &) = delete;
+  FilterDev &operator=(const FilterDev &) = delete;
+  ~FilterDev();
+};
+
+smg_status launch_build_nlc(DevGraph &g, cudaStream_t s, int num_sms);
+// Query constants (not the device pointers) of one plan.
+smg_status fill_filter_query(const Plan &P, const DevGraph &g, FilterQuery &fq);
+smg_status append_filter_steps(const Plan &P, uint32_t query_index, FilterBatch &fb);
+// NLC filter, every walk phase, then collect, for `nq` queries whose
+// FilterQuery records are at d_qs (device).  Candidate counters, the bitmap
+// and the root counters must be zero on entry.
+smg_status launch_nlc_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, cudaStream_t s, int num_sms);
+smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const FilterDev &fd, cudaStream_t s,
+                        int num_sms);
+smg_status launch_collect(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, cudaStream_t s, int num_sms);
+smg_status launch_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, const FilterDev &fd,
+                         cudaStream_t s, int num_sms);
+
+}  // namespace smg

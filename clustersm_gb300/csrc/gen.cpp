@@ -130,19 +130,11 @@ void build_simple_csr(uint32_t n, const std::vector<uint32_t> &src, const std::v
               g.adj.begin() + static_cast<int64_t>(uniq[v]));
 }
 
-bool adjacent(const HostGraph &g, uint32_t a, uint32_t b) {
+bool adjacent(const smg_csr &g, uint32_t a, uint32_t b) {
   // lists of generated and uploaded graphs are sorted; file graphs may not be
-  uint64_t lo = g.off[a], hi = g.off[a + 1];
-  if (hi - lo <= 64) {
-    for (uint64_t e = lo; e < hi; ++e)
-      if (g.adj[e] == b) return true;
-    return false;
-  }
-  bool sorted = std::is_sorted(g.adj.begin() + static_cast<int64_t>(lo), g.adj.begin() + static_cast<int64_t>(hi));
-  if (sorted) return std::binary_search(g.adj.begin() + static_cast<int64_t>(lo), g.adj.begin() + static_cast<int64_t>(hi), b);
-  for (uint64_t e = lo; e < hi; ++e)
-    if (g.adj[e] == b) return true;
-  return false;
+  const uint32_t *lo = g.neighbors + g.offsets[a], *hi = g.neighbors + g.offsets[a + 1];
+  if (hi - lo > 64 && std::is_sorted(lo, hi)) return std::binary_search(lo, hi, b);
+  return std::find(lo, hi, b) != hi;
 }
 
 }  // namespace
@@ -235,20 +227,15 @@ smg_status smg_gen_query(const smg_csr *gc, uint32_t k, uint32_t shape, uint64_t
   if (!gc || !out || k < 2 || k > SMG_MAX_QUERY_VERTICES || shape > SMG_SHAPE_DENSE)
     return fail(SMG_ERR_INVALID, "bad query-generator arguments");
   *out = nullptr;
-  // wrap the caller's CSR without copying
-  HostGraph g;
-  g.n = gc->num_vertices;
-  g.m = gc->num_edges;
-  g.off.assign(gc->offsets, gc->offsets + g.n + 1);
-  g.adj.assign(gc->neighbors, gc->neighbors + 2 * g.m);
+  const smg_csr &g = *gc;
   Rng r(stream_seed(seed, 4, k * 3 + shape));
-  const int max_attempts = 200000;
+  const int max_attempts = 20000000;
   for (int attempt = 0; attempt < max_attempts; ++attempt) {
     uint32_t start = 0;
     bool found = false;
     for (int t = 0; t < 4096; ++t) {
-      start = static_cast<uint32_t>(r.below(g.n));
-      if (g.off[start + 1] > g.off[start]) {
+      start = static_cast<uint32_t>(r.below(g.num_vertices));
+      if (g.offsets[start + 1] > g.offsets[start]) {
         found = true;
         break;
       }
@@ -258,8 +245,8 @@ smg_status smg_gen_query(const smg_csr *gc, uint32_t k, uint32_t shape, uint64_t
     std::vector<uint32_t> tree;  // query-index pairs
     uint32_t cur = start, cur_idx = 0;
     for (uint32_t step = 0; step < 100 * k && vis.size() < k; ++step) {
-      uint64_t d = g.off[cur + 1] - g.off[cur];
-      uint32_t nxt = g.adj[g.off[cur] + r.below(d)];
+      uint64_t d = g.offsets[cur + 1] - g.offsets[cur];
+      uint32_t nxt = g.neighbors[g.offsets[cur] + r.below(d)];
       auto it = std::find(vis.begin(), vis.end(), nxt);
       uint32_t nxt_idx;
       if (it == vis.end()) {

@@ -30,7 +30,9 @@ def _load():
                                        u64p, u64p]
     lib.oracle_nlc_filter.argtypes = [C.POINTER(Csr), C.POINTER(PlanView), u32p]
     lib.oracle_encode.argtypes = [C.POINTER(Csr), C.POINTER(PlanView), u32p, u32p, u32p]
-    for f in ("oracle_count", "oracle_embeddings", "oracle_count_roots", "oracle_nlc_filter", "oracle_encode"):
+    lib.oracle_count_budget.argtypes = [C.POINTER(Csr), C.POINTER(QueryDesc), u32p, C.c_int, C.c_uint64, u64p,
+                                        u64p]
+    for f in ("oracle_count_budget", "oracle_count", "oracle_embeddings", "oracle_count_roots", "oracle_nlc_filter", "oracle_encode"):
         getattr(lib, f).restype = C.c_int
     return lib
 
@@ -49,6 +51,20 @@ def count(graph, query, candmask=None, threads: int = 0) -> int:
     if rc:
         raise ValueError("oracle_count rejected the input")
     return out.value
+
+
+def count_budget(graph, query, budget: int, candmask=None, threads: int = 0):
+    """(count, partial matches used) or (lower bound, None) when the budget ran out."""
+    out, used = C.c_uint64(), C.c_uint64()
+    cm = None
+    if candmask is not None:
+        candmask = np.ascontiguousarray(candmask, dtype=np.uint32)
+        cm = candmask.ctypes.data_as(u32p)
+    rc = _lib.oracle_count_budget(C.byref(graph.csr), C.byref(query.desc), cm, threads, budget, C.byref(out),
+                                  C.byref(used))
+    if rc:
+        raise ValueError("oracle_count_budget rejected the input")
+    return out.value, (None if used.value == (1 << 64) - 1 else used.value)
 
 
 def count_roots(graph, query, lo, hi, threads: int = 0):

@@ -79,6 +79,10 @@ struct Matcher {
   uint64_t count = 0;
   std::vector<uint32_t> *rows = nullptr;
   uint64_t max_rows = 0;
+  // optional work budget shared by all threads (partial matches created)
+  uint64_t *budget_used = nullptr;
+  uint64_t budget = 0, local = 0;
+  bool aborted = false;
 
   bool ok_vertex(uint32_t lvl, uint32_t v) const {
     uint32_t u = Q.order[lvl];
@@ -110,6 +114,11 @@ struct Matcher {
         good = has_edge(g, m[__builtin_ctz(b)], w);
       if (!good) continue;
       m[lvl] = w;
+      if (budget_used && ++local == 4096) {
+        if (__atomic_add_fetch(budget_used, local, __ATOMIC_RELAXED) > budget) aborted = true;
+        local = 0;
+      }
+      if (aborted) return;
       if (lvl + 1 == Q.k) {
         ++count;
         if (rows && rows->size() / Q.k < max_rows) {
@@ -163,6 +172,40 @@ int oracle_count(const smg_csr *g, const smg_query_desc *q, const uint32_t *cand
   return 0;
 }
 
+int oracle_count_budget(const smg_csr *g, const smg_query_desc *q, const uint32_t *candmask, int threads,
+                        uint64_t budget, uint64_t *count, uint64_t *used) {
+  QueryInfo Q;
+  if (!g || !count || !used || !make_query(q, Q) || Q.k < 2) return 1;
+  std::vector<uint32_t> roots;
+  root_candidates(g, Q, candmask, roots);
+  uint64_t total = 0, spent = 0;
+  bool aborted = false;
+  int nt = threads;
+#ifdef _OPENMP
+  if (nt <= 0) nt = omp_get_max_threads();
+#else
+  nt = 1;
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total) reduction(|| : aborted) num_threads(nt)
+  for (int64_t r = 0; r < static_cast<int64_t>(roots.size()); ++r) {
+    if (__atomic_load_n(&spent, __ATOMIC_RELAXED) > budget) {
+      aborted = true;
+      continue;
+    }
+    Matcher mt{g, Q, candmask};
+    mt.budget_used = &spent;
+    mt.budget = budget;
+    mt.m[0] = roots[r];
+    mt.extend(1);
+    __atomic_add_fetch(&spent, mt.local, __ATOMIC_RELAXED);
+    total += mt.count;
+    aborted = aborted || mt.aborted;
+  }
+  *count = total;
+  *used = aborted ? ~0ull : spent;
+  return 0;
+}
+
 int oracle_count_roots(const smg_csr *g, const smg_query_desc *q, int threads, uint64_t root_lo,
                        uint64_t root_hi, uint64_t *count, uint64_t *num_roots) {
   QueryInfo Q;
@@ -185,12 +228,12 @@ int oracle_embeddings(const smg_csr *g, const smg_query_desc *q, uint64_t max_ro
   std::vector<uint32_t> all;
   Matcher mt{g, Q, nullptr};
   mt.rows = &all;
-  mt.max_rows = ~0ull;
+  mt.max_rows = max_rows;
   for (uint32_t r : roots) {
     mt.m[0] = r;
     if (Q.k == 1) {
       ++mt.count;
-      all.push_back(r);
+      if (all.size() < max_rows) all.push_back(r);
     } else {
       mt.extend(1);
     }

@@ -28,11 +28,18 @@ extern "C" {
  * vertex v may only take query vertex u when bit u of candmask[v] is set.
  * threads <= 0 uses all cores.  max_rows/emb: if emb is non-NULL, up to
  * max_rows embeddings (k ids each, in query-vertex order, lexicographically
- * sorted) are written; *rows receives how many. */
+ * sorted) are written; *rows receives how many.  When the count exceeds
+ * max_rows the rows written are the first ones found, not the smallest. */
 int oracle_count(const smg_csr *g, const smg_query_desc *q, const uint32_t *candmask,
                  int threads, uint64_t *count);
 int oracle_embeddings(const smg_csr *g, const smg_query_desc *q, uint64_t max_rows,
                       uint32_t *emb, uint64_t *rows, uint64_t *count);
+
+/* As oracle_count, but gives up once more than `budget` partial matches have
+ * been created: then *used = UINT64_MAX and *count is a lower bound.
+ * Otherwise *used is the number of partial matches created. */
+int oracle_count_budget(const smg_csr *g, const smg_query_desc *q, const uint32_t *candmask,
+                        int threads, uint64_t budget, uint64_t *count, uint64_t *used);
 
 /* Backtracking count limited to root candidates [root_lo, root_hi) of the
  * oracle's own order (for timing a bounded sample).  *num_roots receives

@@ -1,0 +1,152 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Bit-exact: initial candidate masks, the cluster bitmap and final candidate
+masks against the oracle's restatement of filter.cu; uint64 counts and sorted
+embedding sets against the backtracking oracle.  Plain and batched paths must
+agree.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from clustersm_gb300 import native
+from clustersm_gb300.native import DeviceGraph, HostGraph, Plan, Query
+
+pytestmark = pytest.mark.gpu
+
+EXAMPLE_EMBEDDINGS = [(0, 1, 4, 2, 3), (4, 1, 0, 2, 3), (5, 8, 7, 9, 10), (7, 8, 5, 9, 10)]
+BUDGET = 3_000_000  # oracle partial matches per query (keeps the CPU side short)
+
+
+@pytest.fixture(scope="module")
+def er(ctx):
+    g = HostGraph.er(1000, 4000, 4, seed=1)
+    return g, DeviceGraph(ctx, g)
+
+
+@pytest.fixture(scope="module")
+def rmat(ctx):
+    g = HostGraph.rmat(12, 16, 8, seed=7)
+    return g, DeviceGraph(ctx, g)
+
+
+def small_queries(g, shapes=("tree", "sparse", "dense"), ks=(4, 5, 6, 7, 8), seeds=range(4)):
+    out = []
+    for shape in shapes:
+        for k in ks:
+            for s in seeds:
+                out.append(Query.generate(g, k, shape, seed=1000 * k + s))
+    return out
+
+
+def test_example(ctx, example):
+    g, q = example
+    dg = DeviceGraph(ctx, g)
+    plan = Plan(q)
+    res, emb = native.match(ctx, dg, plan, emit=16)
+    assert res.count == 4
+    assert res.embeddings_written == 4 and res.overflow == 0
+    rows = sorted(tuple(r) for r in emb.tolist())
+    assert rows == EXAMPLE_EMBEDDINGS
+
+
+def check_filter(ctx, host, dev, q):
+    plan = Plan(q)
+    vm, enc, cm = native.filter_inspect(ctx, dev, plan)
+    ovm = oracle.nlc_filter(host, plan)
+    oenc, ocm = oracle.encode(host, plan, ovm)
+    assert np.array_equal(vm, ovm), "initial candidate masks differ"
+    assert np.array_equal(enc, oenc), "cluster bitmaps differ"
+    assert np.array_equal(cm, ocm), "final candidate masks differ"
+    return plan, ocm
+
+
+@pytest.mark.parametrize("shape", ["tree", "sparse", "dense"])
+def test_filter_bit_exact_er(ctx, er, shape):
+    host, dev = er
+    for q in small_queries(host, shapes=(shape,), ks=(4,), seeds=range(12)):
+        check_filter(ctx, host, dev, q)
+
+
+@pytest.mark.parametrize("shape", ["tree", "sparse", "dense"])
+def test_filter_bit_exact_rmat(ctx, rmat, shape):
+    host, dev = rmat
+    for q in small_queries(host, shapes=(shape,), ks=(4, 6, 8, 10, 12, 16), seeds=range(3)):
+        check_filter(ctx, host, dev, q)
+
+
+def budgeted(host, q):
+    c, used = oracle.count_budget(host, q, BUDGET)
+    return None if used is None else c
+
+
+@pytest.mark.parametrize("which", ["er", "rmat"])
+def test_counts_match_oracle(ctx, er, rmat, which):
+    host, dev = er if which == "er" else rmat
+    checked = 0
+    for q in small_queries(host, ks=(4, 5, 6) if which == "rmat" else (4, 5, 6, 8), seeds=range(3)):
+        want = budgeted(host, q)
+        if want is None:
+            continue
+        res, _ = native.match(ctx, dev, Plan(q))
+        assert res.count == want, (q.to_dict(), res.count, want)
+        checked += 1
+    assert checked >= 10
+
+
+def test_batch_equals_plain(ctx, er):
+    host, dev = er
+    qs = small_queries(host, ks=(4, 6, 8), seeds=range(3))
+    plans = [Plan(q) for q in qs]
+    counts, st = native.match_batch(ctx, dev, plans)
+    for p, c in zip(plans, counts):
+        res, _ = native.match(ctx, dev, p)
+        assert res.count == int(c)
+    assert st.total_embeddings == int(counts.sum())
+
+
+def test_embeddings_equal_oracle(ctx, er):
+    host, dev = er
+    for q in small_queries(host, ks=(4, 5), seeds=range(2)):
+        want = budgeted(host, q)
+        if want is None or want > 200000:
+            continue
+        cnt, rows = oracle.embeddings(host, q, max_rows=want + 1)
+        res, emb = native.match(ctx, dev, Plan(q), emit=want + 1)
+        assert res.count == cnt and res.embeddings_written == cnt and not res.overflow
+        got = emb[np.lexsort(emb.T[::-1])]
+        assert np.array_equal(got, rows)
+
+
+def test_emit_overflow_keeps_exact_count(ctx, er):
+    host, dev = er
+    q = Query.generate(host, 4, "tree", seed=3)
+    full, _ = native.match(ctx, dev, Plan(q))
+    assert full.count > 8
+    res, emb = native.match(ctx, dev, Plan(q), emit=8)
+    assert res.count == full.count and res.overflow == 1 and res.embeddings_written == 8
+
+
+def test_edge_cases(ctx, er):
+    host, dev = er
+    # a label absent from the data graph: no candidate, count 0
+    res, _ = native.match(ctx, dev, Plan(Query([0, 7], [0, 1])))
+    assert res.count == 0
+    # a single edge: ordered pairs of adjacent vertices with those labels
+    lab = host.labels()
+    off, adj = host.offsets().astype(np.int64), host.neighbors()
+    want = sum(1 for v in range(host.n) for w in adj[off[v]:off[v + 1]] if lab[v] == 0 and lab[w] == 1)
+    res, _ = native.match(ctx, dev, Plan(Query([0, 1], [0, 1])))
+    assert res.count == want
+    # triangle of one label
+    q = Query([2, 2, 2], [0, 1, 1, 2, 2, 0])
+    res, _ = native.match(ctx, dev, Plan(q))
+    assert res.count == oracle.count(host, q)
+
+
+def test_graph_with_isolated_vertices(ctx):
+    g = HostGraph.from_arrays([0, 1, 2, 2, 2], [1, 0], [0, 0, 0, 0])
+    dev = DeviceGraph(ctx, g)
+    res, emb = native.match(ctx, dev, Plan(Query([0, 0], [0, 1])), emit=4)
+    assert res.count == 2
+    assert sorted(tuple(r) for r in emb.tolist()) == [(0, 1), (1, 0)]
