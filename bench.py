@@ -1,0 +1,285 @@
+"""Benchmark of the subgraph-matching hot path (filter + join) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload rmat22] [--impl reference]
+
+One step = one batched pass (smg_match_batch: one filter pass and one
+persistent join launch per memory chunk) over the workload's queries against
+the device-resident data graph.  Prints one JSON line (rank 0).
+
+  value      queries/s of the batched path, device-timed with CUDA events on
+             the library's stream, data graph resident, L2 flushed between
+             steps (a 256 MB write)
+  e2e        queries/s through the C ABI from host query descriptions: plan
+             creation, host->device staging, matching, counts read back
+  plain      queries/s of the one-query-per-call path on a sample of queries
+  roofline   the join kernel's algorithmic bytes / its event-timed duration
+             against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (backtracking, all host cores) on a bounded
+             sample of the same queries
+
+--impl reference times the reference's algorithm on the host cores instead:
+the reference has no CPU implementation of its path and its GPU binary cannot
+be rebuilt on the GPU host (its sources are not there), so the arm runs the
+oracle port, the CPU restatement of the same semantics.
+
+For N > 1 (torchrun) the queries are dealt round-robin to ranks: each rank
+matches its own share against its own replica of the graph (no collective on
+the data path); value = all ranks' queries / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="rmat22")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.out.flush()
+        rows = []
+        for line in Path(self.out.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(host, queries, seconds):
+    """The oracle (backtracking, all cores) on the first queries until `seconds` pass."""
+    import oracle
+    t0 = time.perf_counter()
+    done, emb = 0, 0
+    for q in queries:
+        emb += oracle.count(host, q)
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"first {done} of {len(queries)} queries of the workload, oracle_count with "
+                      f"{os.cpu_count()} OpenMP threads, {dt:.1f} s", "embeddings_per_s": emb / dt}
+
+
+def run_reference(args, wl, host, queries, rank):
+    if rank != 0:
+        return
+    import oracle
+    # calibrate a bounded per-step sample (about 5 s of CPU work)
+    t0 = time.perf_counter()
+    sample = 0
+    for q in queries:
+        oracle.count(host, q)
+        sample += 1
+        if time.perf_counter() - t0 > 5.0:
+            break
+    sub = queries[:sample]
+    for _ in range(args.warmup):
+        for q in sub[: max(1, sample // 4)]:
+            oracle.count(host, q)
+    times, embs = [], 0
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        for q in sub:
+            embs += oracle.count(host, q)
+        times.append(time.perf_counter() - t)
+    tot = sum(times)
+    value = args.steps * sample / tot
+    line = {"metric": "queries/s (batched subgraph matching, exact uint64 counts)", "value": value,
+            "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": wl.name, "description": wl.description, "queries_per_step": sample},
+            "embeddings_per_s": embs / tot,
+            "cpu_baseline": {"value": value, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"first {sample} queries of the workload per step"},
+            "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    from clustersm_gb300.workloads import load
+    wl = load(args.workload)
+    queries_all, expected, meta = wl.queries()
+    mine = list(range(rank, len(queries_all), world))
+    queries = [queries_all[i] for i in mine]
+    host = wl.graph()
+    if args.impl == "reference":
+        return run_reference(args, wl, host, queries_all, rank)
+
+    import torch
+    from clustersm_gb300 import native
+    from clustersm_gb300.native import Context, DeviceGraph, Plan
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    ctx = Context(local)
+    dev = DeviceGraph(ctx, host)
+    plans = [Plan(q) for q in queries]
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # correctness against the committed counts before timing
+    counts, _ = native.match_batch(ctx, dev, plans)
+    want = [expected[i] for i in mine]
+    mismatches = sum(1 for c, w in zip(counts.tolist(), want) if w is not None and int(c) != int(w))
+    for _ in range(args.warmup):
+        native.match_batch(ctx, dev, plans)
+
+    step_ms, join_ms, filt_ms, jbytes, fbytes, launches = [], 0.0, 0.0, 0, 0, 0
+    h2d = d2h = 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            counts, st = native.match_batch(ctx, dev, plans, profile=True)
+            e1.record(stream)
+            barrier()
+            step_ms.append(e0.elapsed_time(e1))
+            join_ms += st.join_ms
+            filt_ms += st.filter_ms
+            jbytes += st.join_bytes
+            fbytes += st.filter_bytes
+            launches += st.kernel_launches
+            h2d, d2h = st.h2d_bytes, st.d2h_bytes
+    clocks = clk.summary()
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    nq_all = len(queries_all)
+    value = nq_all * args.steps / (total_ms / 1e3)
+    embeddings = int(counts.sum())
+
+    # end to end through the C ABI from host query descriptions
+    e2e_t = []
+    for _ in range(max(1, min(3, args.steps))):
+        barrier()
+        t = time.perf_counter()
+        ps = [Plan(q) for q in queries]
+        c2, st2 = native.match_batch(ctx, dev, ps)
+        e2e_t.append(time.perf_counter() - t)
+    e2e_value = nq_all / (max(e2e_t) if world > 1 else statistics.median(e2e_t))
+
+    # plain path (one query per call) on a sample
+    ns = min(args.plain_sample, len(plans))
+    barrier()
+    t = time.perf_counter()
+    for p in plans[:ns]:
+        native.match(ctx, dev, p)
+    plain_qps = ns / (time.perf_counter() - t)
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = jbytes / (join_ms / 1e3) / 1e9 if join_ms > 0 else 0.0
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(wl.name, {}).get("join_dram_bytes_per_step")
+    if rank == 0:
+        line = {
+            "metric": "queries/s (batched subgraph matching, exact uint64 counts)",
+            "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": wl.name, "description": wl.description, "queries": nq_all,
+                       "graph_vertices": host.n, "graph_edges": host.m, "l2": "flushed (256 MB write) between steps",
+                       "parallelism": f"replicas{world}" if world > 1 else "single"},
+            "embeddings_per_s": embeddings * world * args.steps / (total_ms / 1e3),
+            "embeddings_per_step": embeddings,
+            "counts_checked": len(want), "count_mismatches": mismatches,
+            "plain_queries_per_s": plain_qps, "batched_over_plain": value / plain_qps if plain_qps else None,
+            "filter_ms_per_step": filt_ms / args.steps, "join_ms_per_step": join_ms / args.steps,
+            "gpu_launches": launches,
+            "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": "k_join", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                         "traffic": traffic,
+                         "algorithmic_bytes_per_step": jbytes / args.steps},
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(host, queries_all, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

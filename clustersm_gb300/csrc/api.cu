@@ -57,6 +57,18 @@ Arena::~Arena() {
   if (base) cudaFree(base);
 }
 
+// Vertices of at least this degree get a neighbour bitmap (one-load
+// membership tests in the join), up to hub_max_bytes of bitmaps per graph.
+uint32_t hub_min_degree() {
+  const char *s = std::getenv("SMG_HUB_MIN_DEGREE");
+  return s ? static_cast<uint32_t>(std::atol(s)) : 128u;
+}
+
+size_t hub_max_bytes() {
+  const char *s = std::getenv("SMG_HUB_BYTES");
+  return s ? static_cast<size_t>(std::atoll(s)) : (2ull << 30);
+}
+
 uint64_t time_limit_ns() {
   const char *s = std::getenv("SMG_TIME_LIMIT_S");
   double v = s ? std::atof(s) : 120.0;
@@ -94,6 +106,8 @@ smg_status smg_open(int device, smg_ctx **out) {
   *out = c.release();
   return SMG_OK;
 }
+
+void *smg_ctx_stream(smg_ctx *c) { return c ? static_cast<void *>(c->stream) : nullptr; }
 
 void smg_close(smg_ctx *c) {
   if (!c) return;
@@ -182,6 +196,14 @@ smg_status smg_graph_upload(smg_ctx *c, const smg_csr *in, smg_graph **out) {
   if (n) SMG_CUDA(cudaMemcpyAsync(g.label, in->labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
   smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
   if (st) return st;
+  {
+    std::vector<uint32_t> deg(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t v = 0; v < static_cast<int64_t>(n); ++v)
+      deg[v] = static_cast<uint32_t>(in->offsets[v + 1] - in->offsets[v]);
+    st = build_hub_bitmaps(g, hub_min_degree(), hub_max_bytes(), c->stream, deg);
+    if (st) return st;
+  }
   SMG_CUDA(cudaStreamSynchronize(c->stream));
   G->device = c->device;
   *out = G.release();
@@ -196,6 +218,8 @@ void smg_graph_free(smg_graph *G) {
   if (g.adj) cudaFree(g.adj);
   if (g.label) cudaFree(g.label);
   if (g.nlc) cudaFree(g.nlc);
+  if (g.hub_of) cudaFree(g.hub_of);
+  if (g.hub_bits) cudaFree(g.hub_bits);
   delete G;
 }
 
@@ -375,6 +399,9 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   std::memset(&jl, 0, sizeof(jl));
   jl.off = g.off;
   jl.adj = g.adj;
+  jl.hub_of = g.hub_of;
+  jl.hub_bits = g.hub_bits;
+  jl.hub_words = g.hub_words;
   jl.queries = ch.jq;
   jl.nq = nq;
   jl.kmax = ch.kmax;
@@ -387,6 +414,11 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   jl.donate_min = 33;
   jl.time_limit_ns = time_limit_ns();
   jl.emit = ch.emb != nullptr;
+  st->h2d += c->fdev->host.size() + nq * (sizeof(FilterQuery) + sizeof(JoinQuery));
+  st->d2h += nq * sizeof(QCounters) + sizeof(QueueState);
+  uint64_t walk_launches = 0;
+  for (uint32_t ng : c->fdev->phase_count) walk_launches += (ng + 65534) / 65535;
+  st->launches += 2 * ((nq + 65534) / 65535) + walk_launches + 2;
   if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[0], c->stream));
   s = launch_filter(g, ch.fq, nq, *c->fdev, c->stream, c->num_sms);
   if (s) return s;
@@ -405,7 +437,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
                                                             : "a queued task was never published";
     return fail(SMG_ERR_TIMEOUT, why);
   }
-  if (hq->pending != 0) return fail(SMG_ERR_INTERNAL, "join ended with pending tasks");
+  if (hq->pending.v != 0) return fail(SMG_ERR_INTERNAL, "join ended with pending tasks");
   for (uint32_t i = 0; i < nq; ++i) {
     QueryOut &q = out[ch.a + i];
     q.count = hc[i].count;
@@ -444,6 +476,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   if (ch.emb) {
     const uint64_t rows = out[ch.a].emb_written;
     if (rows) SMG_CUDA(cudaMemcpy(o.emb_host, ch.emb, rows * plans[ch.a]->k * 4, cudaMemcpyDeviceToHost));
+    st->d2h += rows * plans[ch.a]->k * 4;
   }
   ++st->chunks;
   return SMG_OK;
@@ -545,10 +578,17 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
     tot += q[i].count;
   }
   if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
     stats->filter_ms = st.filter_ms;
     stats->join_ms = st.join_ms;
     stats->tasks = st.tasks;
     stats->total_embeddings = tot;
+    stats->kernel_launches = st.launches;
+    stats->h2d_bytes = st.h2d;
+    stats->d2h_bytes = st.d2h;
+    stats->filter_bytes = st.filter_bytes;
+    stats->join_bytes = st.join_bytes;
+    stats->chunks = st.chunks;
   }
   return SMG_OK;
 }

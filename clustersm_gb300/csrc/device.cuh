@@ -37,6 +37,10 @@ struct DevGraph {
   uint32_t *adj = nullptr;    // [2|E|] sorted per vertex
   uint32_t *label = nullptr;  // [n]
   uint8_t *nlc = nullptr;     // [n][nlc_stride] neighbour-label counts, saturated at 255
+  uint32_t *hub_of = nullptr; // [n] index of the vertex's neighbour bitmap, or kNone
+  uint32_t *hub_bits = nullptr;  // [num_hubs][hub_words]
+  uint32_t num_hubs = 0;
+  uint64_t hub_words = 0;
   std::vector<uint64_t> label_count;  // vertices per label (host copy)
   uint64_t bytes = 0;
 };

@@ -224,7 +224,7 @@ smg_status smg_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels
 
 smg_status smg_gen_query(const smg_csr *gc, uint32_t k, uint32_t shape, uint64_t seed,
                          smg_host_query **out, uint32_t *out_data_vertices) {
-  if (!gc || !out || k < 2 || k > SMG_MAX_QUERY_VERTICES || shape > SMG_SHAPE_DENSE)
+  if (!gc || !out || k < 2 || k > SMG_MAX_QUERY_VERTICES || shape > SMG_SHAPE_INDUCED)
     return fail(SMG_ERR_INVALID, "bad query-generator arguments");
   *out = nullptr;
   const smg_csr &g = *gc;
@@ -283,6 +283,8 @@ smg_status smg_gen_query(const smg_csr *gc, uint32_t k, uint32_t shape, uint64_t
     } else if (shape == SMG_SHAPE_DENSE) {
       edges.insert(edges.end(), extra.begin(), extra.end());
       if (edges.size() < 3ull * k) continue;  // average degree 2|E|/k >= 3
+    } else if (shape == SMG_SHAPE_INDUCED) {
+      edges.insert(edges.end(), extra.begin(), extra.end());
     }
     std::unique_ptr<smg_host_query> h(new smg_host_query);
     h->q.n = k;

@@ -16,17 +16,22 @@
 //    memory stays bounded instead of growing with the level sizes;
 //  * candidates of a level come from the neighbour list of the matched
 //    neighbour with the fewest neighbours; 32 list entries are tested per
-//    step (candidate bit, injectivity, binary search in the other matched
-//    neighbours' sorted lists) and compacted with a warp ballot;
-//  * the last level is counted with popcounts of ballots, not materialised;
-//  * a warp whose remaining list is long donates half of it to the queue
-//    while the queue runs low (work splitting for hub-heavy graphs);
+//    step (candidate bit, injectivity, membership in the other matched
+//    neighbours' lists) and compacted with a warp ballot;
+//  * membership in the list of a high-degree vertex is one bit of a
+//    per-graph neighbour bitmap; other lists are binary-searched;
+//  * the last level is counted, not materialised: one warp walks the
+//    concatenated last-level lists of a whole batch of up to 32 candidates of
+//    the level before it (a segmented scan), so short lists fill the warp;
+//  * a warp with a long remaining list donates half of it to the queue while
+//    more warps wait than tasks are queued (work splitting for hubs);
 //  * every wait is bounded: a claimed-but-unpublished task, an idle grid and
 //    the whole run have time limits after which the kernel records an error
 //    and returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <numeric>
 
 #include "join.cuh"
 
@@ -37,28 +42,14 @@ constexpr int kWarpsPerBlock = 8;
 constexpr uint64_t kReadyWaitNs = 2000000000ull;   // 2 s for a producer to publish
 constexpr uint64_t kIdleLimitNs = 30000000000ull;  // 30 s without any progress
 
-__host__ __device__ inline uint32_t warp_words(uint32_t K) {
-  const uint32_t p = (11 * K + 1) & ~1u;
-  return p + 2 * K + 32 * K;
-}
-
 __device__ __forceinline__ uint64_t now_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
 
-__device__ __forceinline__ bool sorted_contains(const uint32_t *a, uint32_t n, uint32_t x, uint32_t &probes) {
-  uint32_t lo = 0, hi = n;
-  while (lo < hi) {
-    ++probes;
-    const uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(a + mid) < x)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  return lo < n && __ldg(a + lo) == x;
+__device__ __forceinline__ unsigned long long vload(const QLine &l) {
+  return *reinterpret_cast<const volatile unsigned long long *>(&l.v);
 }
 
 __device__ __forceinline__ void set_error(QueueState *qs, int code) {
@@ -68,13 +59,12 @@ __device__ __forceinline__ void set_error(QueueState *qs, int code) {
 
 // Claims the next published task index, or -1 if the queue is empty.
 __device__ long long pop_task(const JoinLaunch &p) {
-  volatile QueueState *s = p.qs;
-  for (int tries = 0; tries < 32; ++tries) {
-    const unsigned long long h = s->head;
-    unsigned long long t = s->tail;
+  for (int tries = 0; tries < 8; ++tries) {
+    const unsigned long long h = vload(p.qs->head);
+    unsigned long long t = vload(p.qs->tail);
     if (t > p.cap) t = p.cap;
     if (h >= t) return -1;
-    if (atomicCAS(&p.qs->head, h, h + 1) == h) return static_cast<long long>(h);
+    if (atomicCAS(&p.qs->head.v, h, h + 1) == h) return static_cast<long long>(h);
   }
   return -1;
 }
@@ -105,8 +95,8 @@ __global__ void k_seed(JoinLaunch p) {
     uint32_t chunk = p.root_chunk ? p.root_chunk : 1;
     chunk = max(chunk, (nr + p.max_seed_tasks - 1) / p.max_seed_tasks);
     const uint32_t nt = (nr + chunk - 1) / chunk;
-    atomicAdd(&p.qs->pending, static_cast<unsigned long long>(nt));
-    const unsigned long long first = atomicAdd(&p.qs->tail, static_cast<unsigned long long>(nt));
+    atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
+    const unsigned long long first = atomicAdd(&p.qs->tail.v, static_cast<unsigned long long>(nt));
     const uint32_t tw = 4 + p.kmax;
     for (uint32_t i = 0; i < nt; ++i) {
       uint32_t *t = p.tasks + (first + i) * tw;
@@ -120,33 +110,78 @@ __global__ void k_seed(JoinLaunch p) {
   }
 }
 
+// Block per hub: set one bit per neighbour.
+__global__ void k_hub_bits(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                           const uint32_t *__restrict__ hubs, uint64_t words, uint32_t *__restrict__ bits) {
+  const uint32_t v = hubs[blockIdx.x];
+  uint32_t *row = bits + blockIdx.x * words;
+  for (uint32_t e = off[v] + threadIdx.x; e < off[v + 1]; e += blockDim.x) {
+    const uint32_t w = adj[e];
+    atomicOr(row + (w >> 5), 1u << (w & 31));
+  }
+}
+
+// Is w in the neighbour list (beg, deg) of a matched vertex?  `hub` selects
+// its bitmap when it has one.
+__device__ __forceinline__ bool is_neighbor(const JoinLaunch &p, uint32_t beg, uint32_t deg, uint32_t hub,
+                                            uint32_t w, uint32_t &probes) {
+  if (hub != kNone) {
+    ++probes;
+    return (__ldg(p.hub_bits + hub * p.hub_words + (w >> 5)) >> (w & 31)) & 1u;
+  }
+  const uint32_t *a = p.adj + beg;
+  uint32_t lo = 0, hi = deg;
+  while (lo < hi) {
+    ++probes;
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(a + mid) < w)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo < deg && __ldg(a + lo) == w;
+}
+
 // Per-warp shared state, K = largest query of the launch:
-//   m, beg, deg   matched data vertex per level, its list offset and degree
-//   cur, end      cursor and end of the level's candidate source list
+//   m, beg, deg, hub  matched data vertex per level, its list and bitmap
+//   cur, end      cursor and end of the level's source list
 //   bcnt, bidx    batch of up to 32 tested candidates of the level
 //   piv           level whose matched vertex's list feeds this level
 //   ord, bmask, slab  the task's query: vertex, backward-edge mask and
 //                 same-label mask per level
 //   lbase         base pointer of the level's source list
 //   batch         [K][32] tested candidates
+//   seg*          per-candidate segments of the segmented last level
+__host__ __device__ inline uint32_t scalar_words(uint32_t K) { return (12 * K + 1) & ~1u; }
+__host__ __device__ inline uint32_t warp_words(uint32_t K) { return scalar_words(K) + 2 * K + 32 * K + 7 * 32; }
+
 struct WarpView {
-  uint32_t *m, *beg, *deg, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *batch;
+  uint32_t *m, *beg, *deg, *hub, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *batch;
+  uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv;
   const uint32_t **lbase;
   __device__ WarpView(uint32_t *W, uint32_t K) {
     m = W;
     beg = W + K;
     deg = W + 2 * K;
-    cur = W + 3 * K;
-    end = W + 4 * K;
-    bcnt = W + 5 * K;
-    bidx = W + 6 * K;
-    piv = W + 7 * K;
-    ord = W + 8 * K;
-    bmask = W + 9 * K;
-    slab = W + 10 * K;
-    const uint32_t p = (11 * K + 1) & ~1u;
-    lbase = reinterpret_cast<const uint32_t **>(W + p);
-    batch = W + p + 2 * K;
+    hub = W + 3 * K;
+    cur = W + 4 * K;
+    end = W + 5 * K;
+    bcnt = W + 6 * K;
+    bidx = W + 7 * K;
+    piv = W + 8 * K;
+    ord = W + 9 * K;
+    bmask = W + 10 * K;
+    slab = W + 11 * K;
+    const uint32_t s = scalar_words(K);
+    lbase = reinterpret_cast<const uint32_t **>(W + s);
+    batch = W + s + 2 * K;
+    sv = batch + 32 * K;
+    sbeg = sv + 32;
+    sdeg = sbeg + 32;
+    shub = sdeg + 32;
+    sbase = shub + 32;
+    spre = sbase + 32;
+    spiv = spre + 32;
   }
 };
 
@@ -162,18 +197,108 @@ __device__ __forceinline__ uint32_t choose_pivot(const WarpView &S, uint32_t lev
   return best;
 }
 
-// Candidate test for list entry w at `level` (>= 1).
-__device__ __forceinline__ bool accept(const WarpView &S, const uint32_t *__restrict__ adj,
-                                       const uint32_t *__restrict__ candmask, uint32_t level, uint32_t w,
-                                       uint32_t &probes) {
+// Candidate test for list entry w at `level` (>= 1, not the last level).
+__device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const uint32_t *__restrict__ candmask,
+                                       uint32_t level, uint32_t w, uint32_t &probes) {
   if (!((__ldg(candmask + w) >> S.ord[level]) & 1u)) return false;
   for (uint32_t b = S.slab[level]; b; b &= b - 1)
     if (S.m[__ffs(b) - 1] == w) return false;
   for (uint32_t b = S.bmask[level] & ~(1u << S.piv[level]); b; b &= b - 1) {
     const uint32_t j = __ffs(b) - 1;
-    if (!sorted_contains(adj + S.beg[j], S.deg[j], w, probes)) return false;
+    if (!is_neighbor(p, S.beg[j], S.deg[j], S.hub[j], w, probes)) return false;
   }
   return true;
+}
+
+// Counts (and optionally emits) the last level for every candidate of the
+// batch of level P = k-2: the candidates' last-level lists are concatenated
+// and walked 32 entries at a time, each lane finding its candidate by binary
+// search over the segment starts.  Returns the count (same in every lane).
+__device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const JoinQuery &Q,
+                                         const uint32_t *__restrict__ candmask, uint32_t P, uint32_t bc,
+                                         uint32_t lane, unsigned long long &scanned, uint32_t &probes) {
+  const uint32_t L = P + 1;
+  const uint32_t lt = (1u << lane) - 1;
+  uint32_t len = 0;
+  if (lane < bc) {
+    const uint32_t v = S.batch[P * 32 + lane];
+    const uint32_t vb = __ldg(p.off + v), vd = __ldg(p.off + v + 1) - vb;
+    uint32_t piv = 0, bd = 0xFFFFFFFFu;
+    for (uint32_t b = S.bmask[L]; b; b &= b - 1) {
+      const uint32_t j = __ffs(b) - 1;
+      const uint32_t d = j == P ? vd : S.deg[j];
+      if (d < bd) {
+        bd = d;
+        piv = j;
+      }
+    }
+    len = bd;
+    S.sv[lane] = v;
+    S.sbeg[lane] = vb;
+    S.sdeg[lane] = vd;
+    S.shub[lane] = __ldg(p.hub_of + v);
+    S.sbase[lane] = piv == P ? vb : S.beg[piv];
+    S.spiv[lane] = piv;
+  }
+  uint32_t incl = len;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= static_cast<uint32_t>(o)) incl += t;
+  }
+  const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  S.spre[lane] = incl - len;
+  __syncwarp();
+  scanned += total;
+  unsigned long long cnt = 0;
+  const uint32_t u = S.ord[L];
+  const uint32_t back = S.bmask[L], same = S.slab[L];
+  for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+    const uint32_t t = t0 + lane;
+    bool good = false;
+    uint32_t w = 0, i = 0;
+    if (t < total) {
+      uint32_t lo = 0, hi = bc;  // last segment starting at or before t
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (S.spre[mid] <= t)
+          lo = mid;
+        else
+          hi = mid;
+      }
+      i = lo;
+      const uint32_t vi = S.sv[i];
+      w = __ldg(p.adj + S.sbase[i] + (t - S.spre[i]));
+      good = (__ldg(candmask + w) >> u) & 1u;
+      for (uint32_t b = same; b && good; b &= b - 1) {
+        const uint32_t j = __ffs(b) - 1;
+        good = (j == P ? vi : S.m[j]) != w;
+      }
+      // back edges other than the pivot's (whose list w comes from)
+      for (uint32_t b = back & ~(1u << S.spiv[i]); b && good; b &= b - 1) {
+        const uint32_t j = __ffs(b) - 1;
+        if (j == P)
+          good = is_neighbor(p, S.sbeg[i], S.sdeg[i], S.shub[i], w, probes);
+        else
+          good = is_neighbor(p, S.beg[j], S.deg[j], S.hub[j], w, probes);
+      }
+    }
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
+    cnt += __popc(bal);
+    if (p.emit && bal) {
+      unsigned long long pos = 0;
+      if (lane == 0) pos = atomicAdd(Q.emb_count, static_cast<unsigned long long>(__popc(bal)));
+      pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+      const unsigned long long r = pos + __popc(bal & lt);
+      if (good && r < Q.emb_cap) {
+        uint32_t *row = Q.emb + r * Q.k;
+        for (uint32_t j = 0; j < P; ++j) row[S.ord[j]] = S.m[j];
+        row[S.ord[P]] = S.sv[i];
+        row[S.ord[L]] = w;
+      }
+    }
+  }
+  __syncwarp();
+  return cnt;
 }
 
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
@@ -182,9 +307,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
   const uint32_t K = p.kmax, tw = 4 + K;
   WarpView S(smem + wib * warp_words(K), K);
   const uint32_t lt = (1u << lane) - 1;
-  volatile QueueState *vqs = p.qs;
+  QueueState *qs = p.qs;
+  volatile int *vabort = &qs->abort;
+  const unsigned long long total_warps = static_cast<unsigned long long>(gridDim.x) * kWarpsPerBlock;
   uint64_t idle_mark = 0, idle_t0 = 0;
-  uint32_t idle_ns = 64;
+  uint32_t idle_ns = 256;
+  bool is_idle = false;
+  unsigned long long scanned = 0, descents = 0;
+  uint32_t probes = 0;
 
   while (true) {
     long long slot = -1;
@@ -193,40 +323,50 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     if (slot < 0) {
       int stop = 0;
       if (lane == 0) {
-        if (vqs->pending == 0 || vqs->abort) {
+        if (!is_idle) {
+          atomicAdd(&qs->idle.v, 1ull);
+          is_idle = true;
+        }
+        if (vload(qs->pending) == 0 || *vabort) {
           stop = 1;
         } else {
-          const uint64_t pr = vqs->progress, t = now_ns();
+          const uint64_t pr = vload(qs->progress), t = now_ns();
           if (pr != idle_mark || idle_t0 == 0) {
             idle_mark = pr;
             idle_t0 = t;
           } else if (t - idle_t0 > kIdleLimitNs) {
-            set_error(p.qs, JOIN_ERR_IDLE_TIMEOUT);
+            set_error(qs, JOIN_ERR_IDLE_TIMEOUT);
             stop = 1;
           }
-          if (t - vqs->start_ns > p.time_limit_ns) {
-            set_error(p.qs, JOIN_ERR_DEADLINE);
+          if (t - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.time_limit_ns) {
+            set_error(qs, JOIN_ERR_DEADLINE);
             stop = 1;
           }
           __nanosleep(idle_ns);
-          idle_ns = min(idle_ns * 2, 4096u);
+          idle_ns = min(idle_ns * 2, 8192u);
         }
       }
       if (__shfl_sync(0xFFFFFFFFu, stop, 0)) break;
       continue;
     }
-    idle_ns = 64;
+    idle_ns = 256;
     int ok = 1;
-    if (lane == 0 && !wait_ready(p, static_cast<uint64_t>(slot))) {
-      set_error(p.qs, JOIN_ERR_READY_TIMEOUT);
-      ok = 0;
+    if (lane == 0) {
+      if (is_idle) {
+        atomicAdd(&qs->idle.v, ~0ull);  // -1
+        is_idle = false;
+      }
+      if (!wait_ready(p, static_cast<uint64_t>(slot))) {
+        set_error(qs, JOIN_ERR_READY_TIMEOUT);
+        ok = 0;
+      }
     }
     if (!__shfl_sync(0xFFFFFFFFu, ok, 0)) break;
 
     const uint32_t *T = p.tasks + static_cast<uint64_t>(slot) * tw;
     const uint32_t q = T[0], L0 = T[1], lo = T[2], hi = T[3];
     const JoinQuery &Q = p.queries[q];
-    const uint32_t k = Q.k;
+    const uint32_t k = Q.k, P = k - 2;
     if (lane < k) {
       S.ord[lane] = Q.order[lane];
       S.bmask[lane] = Q.back_mask[lane];
@@ -238,6 +378,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
       const uint32_t b = __ldg(p.off + v);
       S.beg[lane] = b;
       S.deg[lane] = __ldg(p.off + v + 1) - b;
+      S.hub[lane] = __ldg(p.hub_of + v);
     }
     __syncwarp();
     if (lane == 0) {
@@ -255,19 +396,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     }
     __syncwarp();
 
-    unsigned long long cnt = 0, scanned = 0, descents = 0;
-    uint32_t probes = 0;
-    uint32_t level = L0, iter = 0;
+    unsigned long long cnt = 0;
+    uint32_t level = L0, iter = 0, tick = 0;
     const uint32_t *const candmask = Q.candmask;
     bool aborted = false;
     while (true) {
-      if ((++iter & 1023) == 0) {
+      if ((++iter & 255) == 0) {
         int stop = 0;
         if (lane == 0) {
-          atomicAdd(&p.qs->progress, 1ull);
-          if (vqs->abort) stop = 1;
-          else if (now_ns() - vqs->start_ns > p.time_limit_ns) {
-            set_error(p.qs, JOIN_ERR_DEADLINE);
+          atomicAdd(&qs->progress.v, 1ull);
+          if (*vabort) {
+            stop = 1;
+          } else if (now_ns() - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.time_limit_ns) {
+            set_error(qs, JOIN_ERR_DEADLINE);
             stop = 1;
           }
         }
@@ -276,83 +417,65 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
           break;
         }
       }
-      if (level == k - 1) {
-        // last level: count (and optionally emit) without materialising
-        const uint32_t *base = S.lbase[level];
-        const uint32_t e = S.end[level];
-        if (e > S.cur[level]) scanned += e - S.cur[level];
-        for (uint32_t c = S.cur[level]; c < e; c += 32) {
-          const uint32_t idx = c + lane;
-          bool good = false;
-          uint32_t w = 0;
-          if (idx < e) {
-            w = __ldg(base + idx);
-            good = level == 0 || accept(S, p.adj, candmask, level, w, probes);
+      if (level == P) {
+        const uint32_t bc = S.bcnt[level];
+        if (bc) {
+          cnt += last_level(S, p, Q, candmask, P, bc, lane, scanned, probes);
+          descents += bc;
+          if (lane == 0) S.bcnt[level] = 0;
+          __syncwarp();
+          continue;
+        }
+      } else {
+        const uint32_t bi = S.bidx[level], bc = S.bcnt[level];
+        if (bi < bc) {
+          // descend into the next tested candidate
+          const uint32_t v = S.batch[level * 32 + bi];
+          __syncwarp();
+          if (lane == 0) {
+            S.bidx[level] = bi + 1;
+            S.m[level] = v;
+            const uint32_t b = __ldg(p.off + v);
+            S.beg[level] = b;
+            S.deg[level] = __ldg(p.off + v + 1) - b;
+            S.hub[level] = __ldg(p.hub_of + v);
           }
-          const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
-          cnt += __popc(bal);
-          if (p.emit && bal) {
-            unsigned long long pos = 0;
-            if (lane == 0) pos = atomicAdd(Q.emb_count, static_cast<unsigned long long>(__popc(bal)));
-            pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
-            const unsigned long long r = pos + __popc(bal & lt);
-            if (good && r < Q.emb_cap) {
-              uint32_t *row = Q.emb + r * k;
-              for (uint32_t j = 0; j < level; ++j) row[S.ord[j]] = S.m[j];
-              row[S.ord[level]] = w;
-            }
+          __syncwarp();
+          const uint32_t nl = level + 1;
+          if (lane == 0) {
+            const uint32_t pv = choose_pivot(S, nl);
+            S.piv[nl] = pv;
+            S.lbase[nl] = p.adj + S.beg[pv];
+            S.cur[nl] = 0;
+            S.end[nl] = S.deg[pv];
+            S.bcnt[nl] = 0;
+            S.bidx[nl] = 0;
           }
+          __syncwarp();
+          ++descents;
+          level = nl;
+          continue;
         }
-        if (level == L0) break;
-        --level;
-        continue;
-      }
-      const uint32_t bi = S.bidx[level], bc = S.bcnt[level];
-      if (bi < bc) {
-        // descend into the next tested candidate
-        const uint32_t v = S.batch[level * 32 + bi];
-        __syncwarp();
-        if (lane == 0) {
-          S.bidx[level] = bi + 1;
-          S.m[level] = v;
-          const uint32_t b = __ldg(p.off + v);
-          S.beg[level] = b;
-          S.deg[level] = __ldg(p.off + v + 1) - b;
-        }
-        __syncwarp();
-        ++descents;
-        const uint32_t nl = level + 1;
-        if (lane == 0) {
-          const uint32_t pv = choose_pivot(S, nl);
-          S.piv[nl] = pv;
-          S.lbase[nl] = p.adj + S.beg[pv];
-          S.cur[nl] = 0;
-          S.end[nl] = S.deg[pv];
-          S.bcnt[nl] = 0;
-          S.bidx[nl] = 0;
-        }
-        __syncwarp();
-        level = nl;
-        continue;
       }
       const uint32_t c = S.cur[level];
       uint32_t e = S.end[level];
       if (c < e) {
-        // donate the back half of a long list while the queue runs low
-        if (e - c >= p.donate_min) {
+        // donate the back half of a long list while warps wait for work
+        if (e - c >= p.donate_min && ((++tick & 7) == 0 || level == 0)) {
           long long ds = -1;
           uint32_t mid = 0;
           if (lane == 0) {
-            const unsigned long long h = vqs->head, t = vqs->tail;
+            const unsigned long long idle = vload(qs->idle);
+            const unsigned long long h = vload(qs->head), t = vload(qs->tail);
             const unsigned long long queued = t > h ? t - h : 0;
-            if (queued < gridDim.x * kWarpsPerBlock && t < p.cap) {
-              const unsigned long long s = atomicAdd(&p.qs->tail, 1ull);
+            if (idle > queued && t < p.cap && idle <= total_warps) {
+              const unsigned long long s = atomicAdd(&qs->tail.v, 1ull);
               if (s < p.cap) {
-                atomicAdd(&p.qs->pending, 1ull);
+                atomicAdd(&qs->pending.v, 1ull);
                 ds = static_cast<long long>(s);
                 mid = c + ((e - c) >> 1);
               } else {
-                p.qs->full = 1;
+                qs->full = 1;
               }
             }
           }
@@ -371,7 +494,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
             __syncwarp();
             if (lane == 0) {
               atomicExch(p.ready + ds, 1u);
-              atomicAdd(&p.qs->donations, 1ull);
+              atomicAdd(&qs->donations, 1ull);
               S.end[level] = mid;
             }
             e = mid;
@@ -379,14 +502,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
           }
         }
         // refill the batch with the next 32 tested entries
-        scanned += min(32u, e - c);
+        const uint32_t n = min(32u, e - c);
+        scanned += n;
         const uint32_t *base = S.lbase[level];
-        const uint32_t idx = c + lane;
         bool good = false;
         uint32_t w = 0;
-        if (idx < e) {
-          w = __ldg(base + idx);
-          good = level == 0 || accept(S, p.adj, candmask, level, w, probes);
+        if (lane < n) {
+          w = __ldg(base + c + lane);
+          good = level == 0 || accept(S, p, candmask, level, w, probes);
         }
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
         if (good) S.batch[level * 32 + __popc(bal & lt)] = w;
@@ -394,7 +517,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
         if (lane == 0) {
           S.bcnt[level] = __popc(bal);
           S.bidx[level] = 0;
-          S.cur[level] = c + 32;
+          S.cur[level] = c + n;
         }
         __syncwarp();
         continue;
@@ -403,18 +526,21 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
       --level;
     }
     unsigned long long pr = probes;
+    probes = 0;
     for (int o = 16; o; o >>= 1) pr += __shfl_down_sync(0xFFFFFFFFu, pr, o);
     if (lane == 0) {
       if (cnt) atomicAdd(Q.count, cnt);
-      atomicAdd(&p.qs->scanned, scanned);
-      atomicAdd(&p.qs->descents, descents);
-      if (pr) atomicAdd(&p.qs->probes, pr);
+      atomicAdd(&qs->scanned, scanned);
+      atomicAdd(&qs->descents, descents);
+      if (pr) atomicAdd(&qs->probes, pr);
       if (!aborted) {
-        atomicAdd(&p.qs->tasks_done, 1ull);
-        atomicAdd(&p.qs->progress, 1ull);
-        atomicAdd(&p.qs->pending, ~0ull);  // -1
+        atomicAdd(&qs->tasks_done, 1ull);
+        atomicAdd(&qs->progress.v, 1ull);
+        atomicAdd(&qs->pending.v, ~0ull);  // -1
       }
     }
+    scanned = 0;
+    descents = 0;
     if (aborted) break;
   }
 }
@@ -428,8 +554,8 @@ size_t join_queue_bytes(uint32_t cap, uint32_t kmax) {
 smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   if (jl.nq == 0) return SMG_OK;
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
-  if (smem > 48 * 1024) SMG_CUDA(cudaFuncSetAttribute(k_join, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      static_cast<int>(smem)));
+  if (smem > 48 * 1024)
+    SMG_CUDA(cudaFuncSetAttribute(k_join, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   SMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join, kWarpsPerBlock * 32, smem));
   per_sm = std::max(1, per_sm);
@@ -438,6 +564,37 @@ smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   SMG_CUDA(cudaGetLastError());
   k_join<<<num_sms * per_sm, kWarpsPerBlock * 32, smem, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
+
+smg_status build_hub_bitmaps(DevGraph &g, uint32_t min_degree, size_t max_bytes, cudaStream_t s,
+                             const std::vector<uint32_t> &deg) {
+  g.hub_words = (static_cast<uint64_t>(g.n) + 31) / 32;
+  std::vector<uint32_t> cand;
+  for (uint32_t v = 0; v < g.n; ++v)
+    if (deg[v] >= min_degree) cand.push_back(v);
+  std::stable_sort(cand.begin(), cand.end(), [&](uint32_t a, uint32_t b) { return deg[a] > deg[b]; });
+  const uint64_t per = g.hub_words * 4;
+  const uint64_t fit = per ? max_bytes / per : 0;
+  if (cand.size() > fit) cand.resize(fit);
+  g.num_hubs = static_cast<uint32_t>(cand.size());
+  std::vector<uint32_t> hub_of(std::max<uint32_t>(g.n, 1), kNone);
+  for (uint32_t i = 0; i < g.num_hubs; ++i) hub_of[cand[i]] = i;
+  SMG_CUDA(cudaMalloc(&g.hub_of, hub_of.size() * 4));
+  SMG_CUDA(cudaMemcpyAsync(g.hub_of, hub_of.data(), hub_of.size() * 4, cudaMemcpyHostToDevice, s));
+  g.bytes += hub_of.size() * 4;
+  if (g.num_hubs) {
+    uint32_t *d_hubs = nullptr;
+    SMG_CUDA(cudaMalloc(&g.hub_bits, per * g.num_hubs));
+    SMG_CUDA(cudaMalloc(&d_hubs, g.num_hubs * 4));
+    SMG_CUDA(cudaMemsetAsync(g.hub_bits, 0, per * g.num_hubs, s));
+    SMG_CUDA(cudaMemcpyAsync(d_hubs, cand.data(), g.num_hubs * 4, cudaMemcpyHostToDevice, s));
+    k_hub_bits<<<g.num_hubs, 256, 0, s>>>(g.off, g.adj, d_hubs, g.hub_words, g.hub_bits);
+    SMG_CUDA(cudaGetLastError());
+    SMG_CUDA(cudaStreamSynchronize(s));
+    cudaFree(d_hubs);
+    g.bytes += per * g.num_hubs;
+  }
   return SMG_OK;
 }
 

@@ -5,15 +5,23 @@
 
 namespace smg {
 
+// One hot counter per 128-byte line, so that spinning readers of one do not
+// slow the atomics on another.
+struct alignas(128) QLine {
+  unsigned long long v;
+  unsigned long long pad[15];
+};
+
 // Work-queue state in device memory.  `pending` counts tasks pushed and not
-// yet finished; the persistent kernel ends when it reaches zero.
+// yet finished; the persistent kernel ends when it reaches zero.  `idle`
+// counts warps waiting for work; busy warps split their lists only while it
+// exceeds the number of queued tasks.
 struct QueueState {
-  unsigned long long head, tail, pending, progress;
-  unsigned long long tasks_done, donations, start_ns, reserved;
-  unsigned long long scanned, descents, probes, pad2;  // work counters
-  int error;   // JOIN_ERR_* below, first one wins
-  int abort;   // set on error or deadline: every warp leaves
-  int full;    // a donation found the queue full (load balance only)
+  QLine head, tail, pending, idle, progress;
+  unsigned long long tasks_done, donations, start_ns, scanned, descents, probes;
+  int error;  // JOIN_ERR_* below, first one wins
+  int abort;  // set on error or deadline: every warp leaves
+  int full;   // a donation found the queue full (load balance only)
   int pad;
 };
 constexpr int JOIN_ERR_READY_TIMEOUT = 1;  // a claimed task was never published
@@ -22,6 +30,9 @@ constexpr int JOIN_ERR_IDLE_TIMEOUT = 3;   // no warp made progress for too long
 
 struct JoinLaunch {
   const uint32_t *off, *adj;
+  const uint32_t *hub_of;    // [n] hub index or kNone
+  const uint32_t *hub_bits;  // [hubs][hub_words] neighbour bitmaps of hubs
+  uint64_t hub_words;
   const JoinQuery *queries;  // device array
   uint32_t nq, kmax;
   QueueState *qs;            // device
@@ -42,5 +53,9 @@ size_t join_queue_bytes(uint32_t cap, uint32_t kmax);
 // no host round trip sits between the filter and the join) and runs the
 // persistent kernel.  QueueState must be zeroed on entry.
 smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms);
+// Neighbour bitmaps of the highest-degree vertices (degree >= min_degree,
+// at most max_bytes of bitmaps), built once per resident graph.
+smg_status build_hub_bitmaps(DevGraph &g, uint32_t min_degree, size_t max_bytes, cudaStream_t s,
+                             const std::vector<uint32_t> &degrees_host);
 
 }  // namespace smg

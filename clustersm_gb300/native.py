@@ -23,7 +23,7 @@ STATUS = {0: "SMG_OK", 1: "SMG_ERR_INVALID", 2: "SMG_ERR_IO", 3: "SMG_ERR_FORMAT
           5: "SMG_ERR_LIMIT", 6: "SMG_ERR_CUDA", 7: "SMG_ERR_OOM", 8: "SMG_ERR_TIMEOUT",
           9: "SMG_ERR_NO_DEVICE", 10: "SMG_ERR_BUDGET", 11: "SMG_ERR_CANCELLED", 12: "SMG_ERR_NOT_READY",
           13: "SMG_ERR_INTERNAL"}
-SHAPES = {"tree": 0, "sparse": 1, "dense": 2}
+SHAPES = {"tree": 0, "sparse": 1, "dense": 2, "induced": 3}
 LABELS_UNIFORM, LABELS_ZIPF1 = 0, 1
 FLAG_EMIT, FLAG_PROFILE = 1, 2
 
@@ -74,7 +74,9 @@ class MatchResult(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("filter_ms", C.c_float), ("join_ms", C.c_float), ("tasks", C.c_uint64),
-                ("total_embeddings", C.c_uint64)]
+                ("total_embeddings", C.c_uint64), ("kernel_launches", C.c_uint64), ("h2d_bytes", C.c_uint64),
+                ("d2h_bytes", C.c_uint64), ("filter_bytes", C.c_uint64), ("join_bytes", C.c_uint64),
+                ("chunks", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class GraphStats(C.Structure):
@@ -121,6 +123,7 @@ def _load():
     dev = {
         "smg_open": (st, [C.c_int, C.POINTER(vp)]),
         "smg_close": (None, [vp]),
+        "smg_ctx_stream": (vp, [vp]),
         "smg_graph_upload": (st, [vp, C.POINTER(Csr), C.POINTER(vp)]),
         "smg_graph_free": (None, [vp]),
         "smg_graph_get_stats": (st, [vp, C.POINTER(GraphStats)]),
@@ -339,6 +342,11 @@ class Context:
     @property
     def handle(self):
         return self._h
+
+    @property
+    def stream_ptr(self) -> int:
+        """The library's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        return lib.smg_ctx_stream(self._h) or 0
 
     def close(self):
         if getattr(self, "_h", None):

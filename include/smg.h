@@ -113,7 +113,7 @@ void smg_host_query_free(smg_host_query *q);
 /* Erdos-Renyi G(n, m): m distinct unordered pairs, no self-loops. */
 smg_status smg_gen_er(uint32_t n, uint64_t m, uint32_t num_labels,
                       uint32_t label_dist, uint64_t seed, smg_host_graph **out);
-/* R-MAT (a,b,c,d)=(0.57,0.19,0.19,0.05), 2^scale vertices, scale*... :
+/* R-MAT (a,b,c,d)=(0.57,0.19,0.19,0.05) on n = 2^scale vertices:
  * n*avg_degree/2 edge draws, symmetrised, self-loops and duplicates dropped,
  * neighbour lists sorted.  threads<=0 uses all host cores. */
 smg_status smg_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels,
@@ -124,6 +124,7 @@ smg_status smg_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels
 #define SMG_SHAPE_TREE 0   /* first-visit edges only                       */
 #define SMG_SHAPE_SPARSE 1 /* tree + 2 random induced non-tree edges       */
 #define SMG_SHAPE_DENSE 2  /* all induced edges, average query degree >= 3 */
+#define SMG_SHAPE_INDUCED 3 /* all induced edges, no density requirement    */
 smg_status smg_gen_query(const smg_csr *g, uint32_t k, uint32_t shape,
                          uint64_t seed, smg_host_query **out,
                          uint32_t *out_data_vertices /* [k] or NULL */);
@@ -193,6 +194,9 @@ typedef struct smg_graph smg_graph;
 /* Bind a context to CUDA device `device` (main.cu:36-43) on its own stream. */
 smg_status smg_open(int device, smg_ctx **out);
 void smg_close(smg_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * their own work against the library's launches. */
+void *smg_ctx_stream(smg_ctx *ctx);
 
 /* Upload a data graph: CSR with sorted neighbour lists, labels and the
  * per-vertex neighbour-label counts become device-resident until freed. */
@@ -243,10 +247,17 @@ smg_status smg_match(smg_ctx *ctx, const smg_graph *g, const smg_plan *p,
 /* Batched path: all queries in one persistent launch fed by a device work
  * queue; counts[i] receives the exact count of plans[i]. */
 typedef struct smg_batch_stats {
-  float filter_ms;
-  float join_ms;
-  uint64_t tasks;
-  uint64_t total_embeddings;
+  float filter_ms;           /* device time of the filters (PROFILE)       */
+  float join_ms;             /* device time of the joins (PROFILE)         */
+  uint64_t tasks;            /* depth-first tasks processed                */
+  uint64_t total_embeddings; /* sum of the counts                          */
+  uint64_t kernel_launches;  /* kernels this call launched                 */
+  uint64_t h2d_bytes;        /* host-to-device bytes this call copied      */
+  uint64_t d2h_bytes;        /* device-to-host bytes this call copied      */
+  uint64_t filter_bytes;     /* algorithmic bytes of the filters           */
+  uint64_t join_bytes;       /* algorithmic bytes of the joins             */
+  uint32_t chunks;           /* memory-bounded sub-batches                 */
+  uint32_t reserved;
 } smg_batch_stats;
 smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
                            const smg_plan *const *plans, uint32_t n,
