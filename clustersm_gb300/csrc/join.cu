@@ -301,6 +301,71 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   return cnt;
 }
 
+// While more warps wait for work than tasks are queued, split off the
+// shallowest unexplored work of this warp's stack: the back half of a level's
+// unscanned list, or else one untried candidate of a level's batch (which
+// becomes a task one level deeper).  Returns true when something was pushed.
+__device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, uint32_t L0, uint32_t level, uint32_t P,
+                           uint32_t lane) {
+  int pushed = 0;
+  if (lane == 0) {
+    QueueState *qs = p.qs;
+    const unsigned long long idle = vload(qs->idle);
+    if (idle) {
+      const unsigned long long h = vload(qs->head), t = vload(qs->tail);
+      const unsigned long long queued = t > h ? t - h : 0;
+      if (idle > queued && t < p.cap) {
+        uint32_t tl = kNone, lo = 0, hi = 0, item = 0;
+        for (uint32_t l = L0; l <= level && tl == kNone; ++l) {
+          const uint32_t c = S.cur[l], e = S.end[l];
+          const uint32_t rem = e > c ? e - c : 0;
+          if (rem >= 2 || (rem == 1 && l < level)) {
+            tl = l;
+            lo = c + rem / 2;
+            hi = e;
+          } else if (l < P) {
+            const uint32_t left = S.bcnt[l] - S.bidx[l];
+            if (left >= 2 || (left == 1 && l < level)) {
+              tl = l + 1;
+              item = S.batch[l * 32 + S.bcnt[l] - 1];
+              lo = 0;
+              hi = kNone;
+            }
+          }
+        }
+        if (tl != kNone) {
+          const unsigned long long slot = atomicAdd(&qs->tail.v, 1ull);
+          if (slot < p.cap) {
+            atomicAdd(&qs->pending.v, 1ull);
+            uint32_t *T = p.tasks + slot * (4 + p.kmax);
+            T[0] = q;
+            T[1] = tl;
+            T[2] = lo;
+            T[3] = hi;
+            if (hi == kNone) {  // a batch candidate: prefix m[0..tl-2] plus the candidate
+              for (uint32_t j = 0; j + 1 < tl; ++j) T[4 + j] = S.m[j];
+              T[4 + tl - 1] = item;
+              --S.bcnt[tl - 1];
+            } else {
+              for (uint32_t j = 0; j < tl; ++j) T[4 + j] = S.m[j];
+              S.end[tl] = lo;
+            }
+            __threadfence();
+            atomicExch(p.ready + slot, 1u);
+            atomicAdd(&qs->donations, 1ull);
+            pushed = 1;
+          } else {
+            qs->full = 1;
+          }
+        }
+      }
+    }
+  }
+  pushed = __shfl_sync(0xFFFFFFFFu, pushed, 0);
+  __syncwarp();
+  return pushed != 0;
+}
+
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -390,14 +455,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
         S.lbase[L0] = p.adj + S.beg[pv];
       }
       S.cur[L0] = lo;
-      S.end[L0] = hi;
+      S.end[L0] = (hi == kNone && L0 > 0) ? S.deg[S.piv[L0]] : hi;
       S.bcnt[L0] = 0;
       S.bidx[L0] = 0;
     }
     __syncwarp();
 
     unsigned long long cnt = 0;
-    uint32_t level = L0, iter = 0, tick = 0;
+    uint32_t level = L0, iter = 0, tick = 0;  // tick paces donation checks
     const uint32_t *const candmask = Q.candmask;
     bool aborted = false;
     while (true) {
@@ -416,6 +481,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
           aborted = true;
           break;
         }
+      }
+      // give the shallowest unexplored work of this stack to a waiting warp
+      if ((++tick & 3) == 0) {
+        if (try_donate(S, p, q, L0, level, P, lane)) continue;
       }
       if (level == P) {
         const uint32_t bc = S.bcnt[level];
@@ -460,47 +529,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
       const uint32_t c = S.cur[level];
       uint32_t e = S.end[level];
       if (c < e) {
-        // donate the back half of a long list while warps wait for work
-        if (e - c >= p.donate_min && ((++tick & 7) == 0 || level == 0)) {
-          long long ds = -1;
-          uint32_t mid = 0;
-          if (lane == 0) {
-            const unsigned long long idle = vload(qs->idle);
-            const unsigned long long h = vload(qs->head), t = vload(qs->tail);
-            const unsigned long long queued = t > h ? t - h : 0;
-            if (idle > queued && t < p.cap && idle <= total_warps) {
-              const unsigned long long s = atomicAdd(&qs->tail.v, 1ull);
-              if (s < p.cap) {
-                atomicAdd(&qs->pending.v, 1ull);
-                ds = static_cast<long long>(s);
-                mid = c + ((e - c) >> 1);
-              } else {
-                qs->full = 1;
-              }
-            }
-          }
-          ds = __shfl_sync(0xFFFFFFFFu, ds, 0);
-          if (ds >= 0) {
-            mid = __shfl_sync(0xFFFFFFFFu, mid, 0);
-            uint32_t *t = p.tasks + static_cast<uint64_t>(ds) * tw;
-            if (lane < level) t[4 + lane] = S.m[lane];
-            if (lane == 0) {
-              t[0] = q;
-              t[1] = level;
-              t[2] = mid;
-              t[3] = e;
-            }
-            __threadfence();
-            __syncwarp();
-            if (lane == 0) {
-              atomicExch(p.ready + ds, 1u);
-              atomicAdd(&qs->donations, 1ull);
-              S.end[level] = mid;
-            }
-            e = mid;
-            __syncwarp();
-          }
-        }
         // refill the batch with the next 32 tested entries
         const uint32_t n = min(32u, e - c);
         scanned += n;
