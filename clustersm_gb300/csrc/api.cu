@@ -378,6 +378,8 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     j.emb = ch.emb;
     j.emb_cap = ch.emb ? o.emb_cap : 0;
     j.emb_count = &ch.counters[i].emb_count;
+    j.count_limit = o.count_limit;
+    j.over = &ch.counters[i].over;
   }
   if (!c->fdev) c->fdev.reset(new FilterDev);
   smg_status st = c->fdev->upload(fb, c->stream);
@@ -441,6 +443,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   for (uint32_t i = 0; i < nq; ++i) {
     QueryOut &q = out[ch.a + i];
     q.count = hc[i].count;
+    q.limit_hit = hc[i].over;
     q.num_roots = hc[i].num_roots;
     q.cands = hc[i].stat[0];
     q.walk_entries = hc[i].stat[1];
@@ -529,6 +532,7 @@ smg_status smg_match(smg_ctx *c, const smg_graph *G, const smg_plan *p, const sm
   if (opts) {
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
+    o.count_limit = opts->max_count;
     if (opts->flags & SMG_FLAG_EMIT) {
       if (!opts->embeddings && opts->max_embeddings) return fail(SMG_ERR_INVALID, "null embeddings buffer");
       o.emb_host = opts->embeddings;
@@ -550,6 +554,7 @@ smg_status smg_match(smg_ctx *c, const smg_graph *G, const smg_plan *p, const sm
   out->tasks = st.tasks;
   out->filter_bytes = st.filter_bytes;
   out->join_bytes = st.join_bytes;
+  out->limit_hit = q.limit_hit;
   return SMG_OK;
 }
 
@@ -567,6 +572,7 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
   if (opts) {
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
+    o.count_limit = opts->max_count;
   }
   std::vector<QueryOut> q(n);
   RunStats st;
@@ -574,8 +580,8 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
   if (s) return s;
   uint64_t tot = 0;
   for (uint32_t i = 0; i < n; ++i) {
-    counts[i] = q[i].count;
-    tot += q[i].count;
+    counts[i] = q[i].limit_hit ? ~0ull : q[i].count;
+    if (!q[i].limit_hit) tot += q[i].count;
   }
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));

@@ -29,7 +29,8 @@ struct Arena {
 struct QCounters {
   uint32_t cand_cnt[kMaxK];    // initial candidates appended per query vertex
   uint32_t num_roots;          // root candidates after the bitmap filter
-  uint32_t pad[3];
+  uint32_t over;               // count exceeded the run's count limit
+  uint32_t pad[2];
   unsigned long long stat[4];  // [0] sum |C(u)| final, [1] walk list entries
   unsigned long long count;    // embeddings
   unsigned long long emb_count;
@@ -47,11 +48,12 @@ struct RunOpts {
   uint32_t *emb_host = nullptr;  // plain path only
   uint64_t emb_cap = 0;
   bool use_graph = false;        // capture the launches in a CUDA graph
+  uint64_t count_limit = 0;      // 0: none
 };
 
 struct QueryOut {
   uint64_t count = 0, emb_written = 0, cands = 0, walk_entries = 0;
-  uint32_t num_roots = 0, overflow = 0;
+  uint32_t num_roots = 0, overflow = 0, limit_hit = 0;
   uint64_t initial_cands = 0;
 };
 

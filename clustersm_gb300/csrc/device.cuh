@@ -120,6 +120,8 @@ struct JoinQuery {
   uint32_t *emb;              // optional embedding rows [emb_cap][k]
   unsigned long long emb_cap;
   unsigned long long *emb_count;
+  unsigned long long count_limit;  // 0: none; else stop once the count exceeds it
+  uint32_t *over;             // set to 1 when the count exceeded count_limit
 };
 
 }  // namespace smg

@@ -57,34 +57,39 @@ __device__ __forceinline__ void set_error(QueueState *qs, int code) {
   atomicExch(&qs->abort, 1);
 }
 
-// Claims the next published task index, or -1 if the queue is empty.
-__device__ long long pop_task(const JoinLaunch &p) {
-  for (int tries = 0; tries < 8; ++tries) {
-    const unsigned long long h = vload(p.qs->head);
-    unsigned long long t = vload(p.qs->tail);
-    if (t > p.cap) t = p.cap;
-    if (h >= t) return -1;
-    if (atomicCAS(&p.qs->head.v, h, h + 1) == h) return static_cast<long long>(h);
-  }
-  return -1;
-}
-
-// Bounded wait until the producer of `slot` has written it.
-__device__ bool wait_ready(const JoinLaunch &p, uint64_t slot) {
-  volatile uint32_t *r = p.ready + slot;
-  if (*r) {
-    __threadfence();
-    return true;
-  }
-  const uint64_t t0 = now_ns();
-  uint32_t ns = 32;
-  while (!*r) {
-    if (now_ns() - t0 > kReadyWaitNs) return false;
+// Waits for the task of `ticket` to be published.  Returns 1 when it is,
+// 0 when the run is over (no task pending anywhere, so none can come) or
+// aborted, -1 on a deadline / idle timeout (recorded in the queue state).
+// Each waiter polls its own ready flag; the shared counters are read only
+// every 16 polls.
+__device__ int wait_ticket(const JoinLaunch &p, unsigned long long ticket, uint64_t &idle_mark, uint64_t &idle_t0) {
+  QueueState *qs = p.qs;
+  volatile uint32_t *r = ticket < p.cap ? p.ready + ticket : nullptr;
+  uint32_t ns = 128, polls = 0;
+  while (true) {
+    if (r && *r) {
+      __threadfence();
+      return 1;
+    }
+    if ((polls++ & 15) == 0) {
+      if (vload(qs->pending) == 0) return 0;
+      if (*reinterpret_cast<volatile int *>(&qs->abort)) return 0;
+      const uint64_t pr = vload(qs->progress), t = now_ns();
+      if (pr != idle_mark || idle_t0 == 0) {
+        idle_mark = pr;
+        idle_t0 = t;
+      } else if (t - idle_t0 > kIdleLimitNs) {
+        set_error(qs, JOIN_ERR_IDLE_TIMEOUT);
+        return -1;
+      }
+      if (t - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.time_limit_ns) {
+        set_error(qs, JOIN_ERR_DEADLINE);
+        return -1;
+      }
+    }
     __nanosleep(ns);
-    ns = min(ns * 2, 1024u);
+    ns = min(ns * 2, 2048u);
   }
-  __threadfence();
-  return true;
 }
 
 __global__ void k_seed(JoinLaunch p) {
@@ -301,7 +306,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   return cnt;
 }
 
-// While more warps wait for work than tasks are queued, split off the
+// While warps wait for work (tickets beyond the tail), split off the
 // shallowest unexplored work of this warp's stack: the back half of a level's
 // unscanned list, or else one untried candidate of a level's batch (which
 // becomes a task one level deeper).  Returns true when something was pushed.
@@ -310,11 +315,10 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, uint32_
   int pushed = 0;
   if (lane == 0) {
     QueueState *qs = p.qs;
-    const unsigned long long idle = vload(qs->idle);
-    if (idle) {
-      const unsigned long long h = vload(qs->head), t = vload(qs->tail);
-      const unsigned long long queued = t > h ? t - h : 0;
-      if (idle > queued && t < p.cap) {
+    const unsigned long long h = vload(qs->head), t = vload(qs->tail);
+    {
+      // tickets beyond the tail are warps waiting for work
+      if (h > t && t < p.cap) {
         uint32_t tl = kNone, lo = 0, hi = 0, item = 0;
         for (uint32_t l = L0; l <= level && tl == kNone; ++l) {
           const uint32_t c = S.cur[l], e = S.end[l];
@@ -374,64 +378,33 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
   const uint32_t lt = (1u << lane) - 1;
   QueueState *qs = p.qs;
   volatile int *vabort = &qs->abort;
-  const unsigned long long total_warps = static_cast<unsigned long long>(gridDim.x) * kWarpsPerBlock;
   uint64_t idle_mark = 0, idle_t0 = 0;
-  uint32_t idle_ns = 256;
-  bool is_idle = false;
   unsigned long long scanned = 0, descents = 0;
   uint32_t probes = 0;
 
   while (true) {
-    long long slot = -1;
-    if (lane == 0) slot = pop_task(p);
-    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-    if (slot < 0) {
-      int stop = 0;
-      if (lane == 0) {
-        if (!is_idle) {
-          atomicAdd(&qs->idle.v, 1ull);
-          is_idle = true;
-        }
-        if (vload(qs->pending) == 0 || *vabort) {
-          stop = 1;
-        } else {
-          const uint64_t pr = vload(qs->progress), t = now_ns();
-          if (pr != idle_mark || idle_t0 == 0) {
-            idle_mark = pr;
-            idle_t0 = t;
-          } else if (t - idle_t0 > kIdleLimitNs) {
-            set_error(qs, JOIN_ERR_IDLE_TIMEOUT);
-            stop = 1;
-          }
-          if (t - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.time_limit_ns) {
-            set_error(qs, JOIN_ERR_DEADLINE);
-            stop = 1;
-          }
-          __nanosleep(idle_ns);
-          idle_ns = min(idle_ns * 2, 8192u);
-        }
-      }
-      if (__shfl_sync(0xFFFFFFFFu, stop, 0)) break;
-      continue;
-    }
-    idle_ns = 256;
-    int ok = 1;
+    int got = 0;
+    unsigned long long slot = 0;
     if (lane == 0) {
-      if (is_idle) {
-        atomicAdd(&qs->idle.v, ~0ull);  // -1
-        is_idle = false;
-      }
-      if (!wait_ready(p, static_cast<uint64_t>(slot))) {
-        set_error(qs, JOIN_ERR_READY_TIMEOUT);
-        ok = 0;
-      }
+      slot = atomicAdd(&qs->head.v, 1ull);
+      got = wait_ticket(p, slot, idle_mark, idle_t0);
     }
-    if (!__shfl_sync(0xFFFFFFFFu, ok, 0)) break;
+    got = __shfl_sync(0xFFFFFFFFu, got, 0);
+    if (got != 1) break;
+    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
 
     const uint32_t *T = p.tasks + static_cast<uint64_t>(slot) * tw;
     const uint32_t q = T[0], L0 = T[1], lo = T[2], hi = T[3];
     const JoinQuery &Q = p.queries[q];
     const uint32_t k = Q.k, P = k - 2;
+    if (Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over)) {
+      if (lane == 0) {
+        atomicAdd(&qs->tasks_done, 1ull);
+        atomicAdd(&qs->progress.v, 1ull);
+        atomicAdd(&qs->pending.v, ~0ull);
+      }
+      continue;
+    }
     if (lane < k) {
       S.ord[lane] = Q.order[lane];
       S.bmask[lane] = Q.back_mask[lane];
@@ -470,14 +443,23 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
         int stop = 0;
         if (lane == 0) {
           atomicAdd(&qs->progress.v, 1ull);
-          if (*vabort) {
+          if (Q.count_limit && (*reinterpret_cast<volatile uint32_t *>(Q.over) ||
+                                *reinterpret_cast<volatile unsigned long long *>(Q.count) + cnt > Q.count_limit)) {
+            *Q.over = 1;
+            stop = 2;  // this query is over its limit: drop the task, keep running
+          } else if (*vabort) {
             stop = 1;
           } else if (now_ns() - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.time_limit_ns) {
             set_error(qs, JOIN_ERR_DEADLINE);
             stop = 1;
           }
         }
-        if (__shfl_sync(0xFFFFFFFFu, stop, 0)) {
+        stop = __shfl_sync(0xFFFFFFFFu, stop, 0);
+        if (stop == 2) {
+          cnt = 0;
+          break;
+        }
+        if (stop) {
           aborted = true;
           break;
         }
@@ -557,7 +539,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     probes = 0;
     for (int o = 16; o; o >>= 1) pr += __shfl_down_sync(0xFFFFFFFFu, pr, o);
     if (lane == 0) {
-      if (cnt) atomicAdd(Q.count, cnt);
+      if (cnt) {
+        const unsigned long long before = atomicAdd(Q.count, cnt);
+        if (Q.count_limit && before + cnt > Q.count_limit) *Q.over = 1;
+      }
       atomicAdd(&qs->scanned, scanned);
       atomicAdd(&qs->descents, descents);
       if (pr) atomicAdd(&qs->probes, pr);

@@ -12,12 +12,13 @@ struct alignas(128) QLine {
   unsigned long long pad[15];
 };
 
-// Work-queue state in device memory.  `pending` counts tasks pushed and not
-// yet finished; the persistent kernel ends when it reaches zero.  `idle`
-// counts warps waiting for work; busy warps split their lists only while it
-// exceeds the number of queued tasks.
+// Work-queue state in device memory.  A warp wanting work takes a ticket
+// (head++) and waits for slot `ticket` to be published; producers append at
+// tail++.  head > tail therefore means warps are waiting, which is when busy
+// warps split their work.  `pending` counts tasks pushed and not yet
+// finished; the persistent kernel ends when it reaches zero.
 struct QueueState {
-  QLine head, tail, pending, idle, progress;
+  QLine head, tail, pending, progress;
   unsigned long long tasks_done, donations, start_ns, scanned, descents, probes;
   int error;  // JOIN_ERR_* below, first one wins
   int abort;  // set on error or deadline: every warp leaves

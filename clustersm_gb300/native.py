@@ -62,14 +62,16 @@ class PlanView(C.Structure):
 
 class MatchOpts(C.Structure):
     _fields_ = [("flags", C.c_uint32), ("bfs_depth", C.c_uint32), ("root_chunk", C.c_uint32),
-                ("reserved", C.c_uint32), ("max_embeddings", C.c_uint64), ("embeddings", u32p)]
+                ("reserved", C.c_uint32), ("max_embeddings", C.c_uint64), ("embeddings", u32p),
+                ("max_count", C.c_uint64)]
 
 
 class MatchResult(C.Structure):
     _fields_ = [("count", C.c_uint64), ("embeddings_written", C.c_uint64), ("overflow", C.c_uint32),
                 ("num_candidates_root", C.c_uint32), ("candidates_total", C.c_uint64),
                 ("filter_ms", C.c_float), ("join_ms", C.c_float), ("tasks", C.c_uint64),
-                ("filter_bytes", C.c_uint64), ("join_bytes", C.c_uint64)]
+                ("filter_bytes", C.c_uint64), ("join_bytes", C.c_uint64), ("limit_hit", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class BatchStats(C.Structure):
@@ -385,9 +387,10 @@ class DeviceGraph:
 
 
 def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=False, bfs_depth=0,
-          root_chunk=0):
+          root_chunk=0, max_count=0):
     """Plain path.  Returns (MatchResult, embeddings array or None)."""
     opts = MatchOpts()
+    opts.max_count = max_count
     opts.flags = (FLAG_EMIT if emit else 0) | (FLAG_PROFILE if profile else 0)
     opts.bfs_depth = bfs_depth
     opts.root_chunk = root_chunk
@@ -403,7 +406,9 @@ def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=F
     return res, buf
 
 
-def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk=0, profile=False):
+def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk=0, profile=False, max_count=0):
+    """Batched path.  Returns (counts, BatchStats); with max_count, queries over
+    the limit report 2**64-1."""
     n = len(plans)
     arr = (C.c_void_p * n)(*[p.handle.value for p in plans])
     counts = np.zeros(n, dtype=np.uint64)
@@ -411,6 +416,7 @@ def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk
     opts.flags = FLAG_PROFILE if profile else 0
     opts.bfs_depth = bfs_depth
     opts.root_chunk = root_chunk
+    opts.max_count = max_count
     st = BatchStats()
     check(lib.smg_match_batch(ctx.handle, graph.handle, arr, n, C.byref(opts), counts.ctypes.data_as(u64p),
                               C.byref(st)), "smg_match_batch")

@@ -225,6 +225,9 @@ typedef struct smg_match_opts {
   uint64_t max_embeddings; /* rows of k ids the embeddings buffer can hold */
   uint32_t *embeddings;    /* host buffer [max_embeddings * k], row r holds
                               the data vertex of query vertex 0..k-1       */
+  uint64_t max_count;      /* 0 = none; otherwise a query stops as soon as
+                              its count is known to exceed max_count, and
+                              reports UINT64_MAX (batch) / limit_hit = 1   */
 } smg_match_opts;
 
 typedef struct smg_match_result {
@@ -238,6 +241,8 @@ typedef struct smg_match_result {
   uint64_t tasks;               /* depth-first tasks processed            */
   uint64_t filter_bytes;        /* algorithmic bytes of the filter        */
   uint64_t join_bytes;          /* algorithmic bytes of the join          */
+  uint32_t limit_hit;           /* 1: count exceeded opts->max_count      */
+  uint32_t reserved;
 } smg_match_result;
 
 /* Plain path: one query, filter then join, synchronous. */
