@@ -275,7 +275,7 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   ch.kmax = 0;
   for (uint32_t i = ch.a; i < ch.b; ++i) ch.kmax = std::max(ch.kmax, plans[i]->k);
   const uint32_t seeds = seed_tasks(c, o, nq);
-  const uint64_t cap64 = static_cast<uint64_t>(nq) * seeds + (2u << 20);
+  const uint64_t cap64 = static_cast<uint64_t>(nq) * seeds + (4u << 20);
   ch.cap = static_cast<uint32_t>(std::min<uint64_t>(cap64, 0x7FFFFFFFu));
   ch.cand_total.resize(nq);
   // zero region
