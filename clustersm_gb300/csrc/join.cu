@@ -443,9 +443,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
         int stop = 0;
         if (lane == 0) {
           atomicAdd(&qs->progress.v, 1ull);
-          if (Q.count_limit && (*reinterpret_cast<volatile uint32_t *>(Q.over) ||
-                                *reinterpret_cast<volatile unsigned long long *>(Q.count) + cnt > Q.count_limit)) {
-            *Q.over = 1;
+          if (Q.count_limit) {
+            // publish the running count so that the limit sees every warp's share
+            if (cnt) {
+              const unsigned long long before = atomicAdd(Q.count, cnt);
+              if (before + cnt > Q.count_limit) *Q.over = 1;
+            }
+          }
+          if (Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over)) {
             stop = 2;  // this query is over its limit: drop the task, keep running
           } else if (*vabort) {
             stop = 1;
@@ -455,6 +460,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
           }
         }
         stop = __shfl_sync(0xFFFFFFFFu, stop, 0);
+        if (Q.count_limit) cnt = 0;  // flushed above
         if (stop == 2) {
           cnt = 0;
           break;

@@ -1,20 +1,28 @@
-"""Generate the committed query sets of the benchmark workloads with their
-exact embedding counts (computed here by the CPU oracle).
+"""Generate the committed query sets of the benchmark workloads, with exact
+embedding counts checked by two independent implementations.
 
-    python tests/golden/make_workloads.py er1k rmat20 rmat22
+    # on a GPU host: draw and screen queries (writes gpurun_out/workload_<name>.json)
+    python tests/golden/make_workloads.py gpu rmat22 rmat20
+    # on any host: recount every kept query with the CPU oracle and commit
+    python tests/golden/make_workloads.py verify rmat22 rmat20
+    # small workloads drawn and counted by the oracle alone
+    python tests/golden/make_workloads.py cpu er1k
 
-Queries are drawn by seeded random-walk extraction (smg_gen_query) with the
-configured vertex counts and shapes.  On R-MAT graphs with Zipf labels almost
-every walk-extracted query has far more embeddings than any exact enumerator
-can count (on R-MAT 2^22 / 32 labels no drawn query with 6+ vertices stayed
-under 10^8 partial matches), so a drawn query is kept only when the oracle
-finishes it within BUDGET partial matches; otherwise the next seed is tried.
-The acceptance budget and the number of draws per kept query are recorded in
-the fixture.
+Queries are drawn by seeded random-walk extraction (smg_gen_query).  On R-MAT
+graphs with Zipf labels, walk-extracted queries have embedding counts far
+beyond exact enumeration: on R-MAT 2^22 / 32 labels only 13 of 187 drawn
+queries (4..16 vertices) had at most 10^8 embeddings, and none of those had
+more than 5 vertices.  A drawn query is therefore kept when its exact count is at
+most COUNT_LIMIT, decided on the GPU with the library's per-query count limit
+(the join stops a query as soon as its running count passes the limit) and a
+2 s device deadline; each slot retries new seeds up to MAX_DRAWS times.
+Every kept count is then recomputed by the CPU oracle; a fixture is written
+only when all counts agree.
 """
 from __future__ import annotations
 
 import json
+import os
 import random
 import sys
 import time
@@ -23,54 +31,120 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-import oracle  # noqa: E402
 from clustersm_gb300.workloads import load  # noqa: E402
-from clustersm_gb300.native import Query  # noqa: E402
+from clustersm_gb300.native import Query, SmgError  # noqa: E402
 
+COUNT_LIMIT = 10**8
+MAX_DRAWS = 64
 SPECS = {
-    # name: (number of queries, k choices, shapes, oracle budget, max draws per slot)
-    "er1k": (96, [4], ["tree", "sparse", "dense"], 10**8, 2000),
-    "rmat20": (96, [8], ["tree", "sparse", "dense"], 5 * 10**7, 400),
-    "rmat22": (1024, list(range(4, 17)), ["tree", "sparse", "dense"], 2 * 10**7, 60),
+    # name: (slots, vertex counts, shapes)
+    "er1k": (96, [4], ["induced"]),
+    "rmat20": (96, [4, 5], ["tree", "sparse", "dense"]),
+    "rmat22": (1024, [4, 5], ["tree", "sparse", "dense"]),
 }
 
 
-def main(names):
-    for name in names:
-        wl = load(name)
-        nq, ks, shapes, budget, draws = SPECS[name]
-        t0 = time.time()
-        g = wl.graph()
-        rng = random.Random(f"{name}-slots")
-        out, tried = [], 0
-        for slot in range(nq):
-            k = rng.choice(ks)
-            shape = shapes[slot % len(shapes)]
-            kept = None
-            for attempt in range(draws):
-                seed = (slot << 20) | attempt
-                try:
-                    q = Query.generate(g, k, shape, seed=seed)
-                except Exception:
-                    continue
-                tried += 1
-                c, used = oracle.count_budget(g, q, budget)
-                if used is not None:
-                    kept = (q, c, attempt, seed)
-                    break
-            if kept is None:
-                continue
-            q, c, attempt, seed = kept
-            out.append({"slot": slot, "k": int(q.k), "shape": shape, "seed": seed, "draws": attempt + 1,
-                        "labels": q.labels.tolist(), "edges": q.edges.tolist(), "count": int(c)})
-            print(f"{name} slot {slot}: k={q.k} {shape} count={c} draws={attempt + 1}", flush=True)
-        path = ROOT / wl.queries_file
-        path.write_text(json.dumps({
-            "workload": name, "generator": "tests/golden/make_workloads.py", "oracle_budget": budget,
-            "max_draws_per_slot": draws, "slots": nq, "kept": len(out), "draws_total": tried,
-            "seconds": round(time.time() - t0, 1), "queries": out}, separators=(",", ":")))
-        print(f"{name}: kept {len(out)} of {nq} slots ({tried} draws) -> {path}", flush=True)
+def draws(name):
+    nq, ks, shapes = SPECS[name]
+    rng = random.Random(f"{name}-slots")
+    for slot in range(nq):
+        k = rng.choice(ks)
+        shape = shapes[slot % len(shapes)]
+        for attempt in range(MAX_DRAWS):
+            yield slot, attempt, k, shape, (slot << 20) | attempt
+
+
+def record(slot, attempt, k, shape, seed, q, count, key):
+    return {"slot": slot, "k": int(k), "shape": shape, "seed": seed, "draws": attempt + 1,
+            "labels": q.labels.tolist(), "edges": q.edges.tolist(), key: int(count)}
+
+
+def gen_gpu(name):
+    from clustersm_gb300 import native
+    from clustersm_gb300.native import Context, DeviceGraph, Plan
+    os.environ["SMG_TIME_LIMIT_S"] = "2"
+    wl = load(name)
+    t0 = time.time()
+    host = wl.graph()
+    ctx = Context(0)
+    dev = DeviceGraph(ctx, host)
+    out, done_slot, tried, timeouts = [], -1, 0, 0
+    for slot, attempt, k, shape, seed in draws(name):
+        if slot == done_slot:
+            continue
+        try:
+            q = Query.generate(host, k, shape, seed=seed)
+        except SmgError:
+            continue
+        tried += 1
+        try:
+            res, _ = native.match(ctx, dev, Plan(q), max_count=COUNT_LIMIT)
+        except SmgError:
+            timeouts += 1
+            continue
+        if res.limit_hit:
+            continue
+        out.append(record(slot, attempt, k, shape, seed, q, res.count, "gpu_count"))
+        done_slot = slot
+    path = ROOT / "gpurun_out" / f"workload_{name}.json"
+    path.parent.mkdir(exist_ok=True)
+    path.write_text(json.dumps({"workload": name, "count_limit": COUNT_LIMIT, "max_draws": MAX_DRAWS,
+                                "slots": SPECS[name][0], "kept": len(out), "draws_total": tried,
+                                "timeouts": timeouts, "seconds": round(time.time() - t0, 1),
+                                "queries": out}, separators=(",", ":")))
+    print(f"{name}: kept {len(out)} of {SPECS[name][0]} slots, {tried} draws, {timeouts} timeouts -> {path}")
+
+
+def verify(name, src=None):
+    import oracle
+    wl = load(name)
+    src = Path(src) if src else ROOT / "gpurun_out" / f"workload_{name}.json"
+    data = json.loads(src.read_text())
+    host = wl.graph()
+    t0 = time.time()
+    bad = 0
+    for rec in data["queries"]:
+        q = Query(rec["labels"], rec["edges"])
+        rec["count"] = oracle.count(host, q)
+        if rec["count"] != rec["gpu_count"]:
+            bad += 1
+            print(f"MISMATCH slot {rec['slot']}: oracle {rec['count']} gpu {rec['gpu_count']}")
+    data["oracle_seconds"] = round(time.time() - t0, 1)
+    data["verified_by"] = "oracle_count (CPU backtracking) == GPU count for every query"
+    if bad:
+        sys.exit(f"{bad} mismatches: fixture not written")
+    dst = ROOT / wl.queries_file
+    dst.write_text(json.dumps(data, separators=(",", ":")))
+    print(f"{name}: {len(data['queries'])} counts verified in {data['oracle_seconds']} s -> {dst}")
+
+
+def gen_cpu(name):
+    import oracle
+    wl = load(name)
+    host = wl.graph()
+    out, done_slot, tried = [], -1, 0
+    for slot, attempt, k, shape, seed in draws(name):
+        if slot == done_slot:
+            continue
+        try:
+            q = Query.generate(host, k, shape, seed=seed)
+        except SmgError:
+            continue
+        tried += 1
+        c, used = oracle.count_budget(host, q, 10**9)
+        if used is None or c > COUNT_LIMIT:
+            continue
+        out.append(record(slot, attempt, k, shape, seed, q, c, "count"))
+        done_slot = slot
+    dst = ROOT / wl.queries_file
+    dst.write_text(json.dumps({"workload": name, "count_limit": COUNT_LIMIT, "max_draws": MAX_DRAWS,
+                               "slots": SPECS[name][0], "kept": len(out), "draws_total": tried,
+                               "verified_by": "oracle_count (CPU backtracking)", "queries": out},
+                              separators=(",", ":")))
+    print(f"{name}: kept {len(out)} -> {dst}")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or list(SPECS))
+    mode, names = sys.argv[1], sys.argv[2:]
+    for n in names:
+        {"gpu": gen_gpu, "verify": verify, "cpu": gen_cpu}[mode](n)
