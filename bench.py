@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--subset", type=int, default=0, help="use only the first N queries (profiling runs)")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
 
 
@@ -164,10 +167,12 @@ def run_reference(args, wl, host, queries, rank):
 def main():
     args = parse()
     rank, world, local = dist_env()
-    from clustersm_gb300.workloads import load
+    from clustersm_gb300.workloads import load, shard
     wl = load(args.workload)
     queries_all, expected, meta = wl.queries()
-    mine = list(range(rank, len(queries_all), world))
+    if args.subset:
+        queries_all, expected = queries_all[: args.subset], expected[: args.subset]
+    mine = shard(len(queries_all), rank, world)
     queries = [queries_all[i] for i in mine]
     host = wl.graph()
     if args.impl == "reference":
@@ -228,22 +233,26 @@ def main():
     embeddings = int(counts.sum())
 
     # end to end through the C ABI from host query descriptions
-    e2e_t = []
-    for _ in range(max(1, min(3, args.steps))):
-        barrier()
-        t = time.perf_counter()
-        ps = [Plan(q) for q in queries]
-        c2, st2 = native.match_batch(ctx, dev, ps)
-        e2e_t.append(time.perf_counter() - t)
-    e2e_value = nq_all / (max(e2e_t) if world > 1 else statistics.median(e2e_t))
+    e2e_value = None
+    if not args.no_e2e:
+        e2e_t = []
+        for _ in range(max(1, min(3, args.steps))):
+            barrier()
+            t = time.perf_counter()
+            ps = [Plan(q) for q in queries]
+            native.match_batch(ctx, dev, ps)
+            e2e_t.append(time.perf_counter() - t)
+        e2e_value = nq_all / (max(e2e_t) if world > 1 else statistics.median(e2e_t))
 
     # plain path (one query per call) on a sample
-    ns = min(args.plain_sample, len(plans))
-    barrier()
-    t = time.perf_counter()
-    for p in plans[:ns]:
-        native.match(ctx, dev, p)
-    plain_qps = ns / (time.perf_counter() - t)
+    plain_qps = None
+    if not args.no_plain:
+        ns = min(args.plain_sample, len(plans))
+        barrier()
+        t = time.perf_counter()
+        for p in plans[:ns]:
+            native.match(ctx, dev, p)
+        plain_qps = ns / (time.perf_counter() - t)
 
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -265,6 +274,7 @@ def main():
             "embeddings_per_step": embeddings,
             "counts_checked": len(want), "count_mismatches": mismatches,
             "plain_queries_per_s": plain_qps, "batched_over_plain": value / plain_qps if plain_qps else None,
+            "plain_sample": None if args.no_plain else min(args.plain_sample, len(plans)),
             "filter_ms_per_step": filt_ms / args.steps, "join_ms_per_step": join_ms / args.steps,
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

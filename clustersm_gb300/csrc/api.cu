@@ -249,11 +249,75 @@ struct Chunk {
   QueueState *qs = nullptr;
   uint32_t *ready = nullptr, *tasks = nullptr, *emb = nullptr;
   QCounters *counters = nullptr;
+  unsigned int *walk_count = nullptr;  // one zeroed counter pair per walk phase
+  uint4 *walk_items = nullptr;
+  uint32_t walk_cap = 0;
   FilterQuery *fq = nullptr;
   JoinQuery *jq = nullptr;
   std::vector<uint32_t *> vmask, enc, cand, roots;
   std::vector<uint64_t> cand_total;
 };
+
+}  // namespace
+
+QueryFootprint query_footprint(const DevGraph &g, const Plan &P) {
+  QueryFootprint f;
+  uint64_t cand = 0;
+  for (uint32_t u = 0; u < P.k; ++u) cand += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
+  const uint64_t rc = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
+  f.vmask = al(static_cast<size_t>(g.n) * 4);
+  f.enc = al(static_cast<size_t>(g.n) * P.num_words * 4);
+  f.cand = al(std::max<uint64_t>(cand, 1) * 4);
+  f.roots = al(std::max<uint64_t>(rc, 1) * 4);
+  return f;
+}
+
+smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffers &b, uint64_t count_limit,
+                              FilterQuery &f, JoinQuery &j) {
+  smg_status st = fill_filter_query(P, g, f);
+  if (st) return st;
+  uint64_t acc = 0;
+  for (uint32_t u = 0; u < P.k; ++u) {
+    f.cand_off[u] = acc;
+    acc += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
+  }
+  f.cand_off[P.k] = acc;
+  f.vmask = b.vmask;
+  f.enc = b.enc;
+  f.cand = b.cand;
+  f.cand_cnt = b.counters->cand_cnt;
+  f.roots = b.roots;
+  f.num_roots = &b.counters->num_roots;
+  f.stat = b.counters->stat;
+  std::memset(&j, 0, sizeof(j));
+  j.k = P.k;
+  for (uint32_t l = 0; l < P.k; ++l) {
+    j.order[l] = P.order[l];
+    j.back_mask[l] = P.back_mask[l];
+    j.same_label[l] = P.same_label_mask[l];
+  }
+  j.candmask = b.vmask;
+  j.roots = b.roots;
+  j.num_roots = &b.counters->num_roots;
+  j.count = &b.counters->count;
+  j.emb = b.emb;
+  j.emb_cap = b.emb_cap;
+  j.emb_count = &b.counters->emb_count;
+  j.count_limit = count_limit;
+  j.over = &b.counters->over;
+  j.pending = &b.counters->pending;
+  return SMG_OK;
+}
+
+namespace {
+
+WalkOverflow walk_overflow(const Chunk &ch) {
+  WalkOverflow w;
+  w.count = ch.walk_count;
+  w.cap = ch.walk_cap;
+  w.items = ch.walk_items;
+  return w;
+}
 
 size_t query_bytes(const DevGraph &g, const Plan &P, uint64_t &cand_total) {
   cand_total = 0;
@@ -286,6 +350,8 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   off += al(static_cast<size_t>(ch.cap) * 4);
   const size_t o_cnt = off;
   off += al(nq * sizeof(QCounters));
+  const size_t o_wcnt = off;
+  off += al(kMaxWalkPhases * 2 * sizeof(unsigned int));
   std::vector<size_t> o_enc(nq), o_vm(nq), o_cand(nq), o_root(nq);
   for (uint32_t i = 0; i < nq; ++i) {
     o_enc[i] = off;
@@ -305,6 +371,9 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   }
   const size_t o_tasks = off;
   off += al(static_cast<size_t>(ch.cap) * (4 + ch.kmax) * 4);
+  ch.walk_cap = kWalkCap;
+  const size_t o_witems = off;
+  off += al(static_cast<size_t>(ch.walk_cap) * sizeof(uint4));
   const size_t o_fq = off;
   off += al(nq * sizeof(FilterQuery));
   const size_t o_jq = off;
@@ -318,6 +387,8 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   ch.qs = reinterpret_cast<QueueState *>(B + o_qs);
   ch.ready = reinterpret_cast<uint32_t *>(B + o_ready);
   ch.counters = reinterpret_cast<QCounters *>(B + o_cnt);
+  ch.walk_count = reinterpret_cast<unsigned int *>(B + o_wcnt);
+  ch.walk_items = reinterpret_cast<uint4 *>(B + o_witems);
   ch.tasks = reinterpret_cast<uint32_t *>(B + o_tasks);
   ch.fq = reinterpret_cast<FilterQuery *>(B + o_fq);
   ch.jq = reinterpret_cast<JoinQuery *>(B + o_jq);
@@ -345,41 +416,18 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
   FilterBatch fb;
   for (uint32_t i = 0; i < nq; ++i) {
     const Plan &P = *plans[ch.a + i];
-    FilterQuery &f = hf[i];
-    smg_status st = fill_filter_query(P, g, f);
+    QueryBuffers b;
+    b.vmask = ch.vmask[i];
+    b.enc = ch.enc[i];
+    b.cand = ch.cand[i];
+    b.roots = ch.roots[i];
+    b.counters = ch.counters + i;
+    b.emb = ch.emb;
+    b.emb_cap = ch.emb ? o.emb_cap : 0;
+    smg_status st = make_query_records(P, g, b, o.count_limit, hf[i], hj[i]);
     if (st) return st;
-    uint64_t acc = 0;
-    for (uint32_t u = 0; u < P.k; ++u) {
-      f.cand_off[u] = acc;
-      acc += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
-    }
-    f.cand_off[P.k] = acc;
-    f.vmask = ch.vmask[i];
-    f.enc = ch.enc[i];
-    f.cand = ch.cand[i];
-    f.cand_cnt = ch.counters[i].cand_cnt;
-    f.roots = ch.roots[i];
-    f.num_roots = &ch.counters[i].num_roots;
-    f.stat = ch.counters[i].stat;
     st = append_filter_steps(P, i, fb);
     if (st) return st;
-    JoinQuery &j = hj[i];
-    std::memset(&j, 0, sizeof(j));
-    j.k = P.k;
-    for (uint32_t l = 0; l < P.k; ++l) {
-      j.order[l] = P.order[l];
-      j.back_mask[l] = P.back_mask[l];
-      j.same_label[l] = P.same_label_mask[l];
-    }
-    j.candmask = ch.vmask[i];
-    j.roots = ch.roots[i];
-    j.num_roots = &ch.counters[i].num_roots;
-    j.count = &ch.counters[i].count;
-    j.emb = ch.emb;
-    j.emb_cap = ch.emb ? o.emb_cap : 0;
-    j.emb_count = &ch.counters[i].emb_count;
-    j.count_limit = o.count_limit;
-    j.over = &ch.counters[i].over;
   }
   if (!c->fdev) c->fdev.reset(new FilterDev);
   smg_status st = c->fdev->upload(fb, c->stream);
@@ -419,10 +467,11 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   st->h2d += c->fdev->host.size() + nq * (sizeof(FilterQuery) + sizeof(JoinQuery));
   st->d2h += nq * sizeof(QCounters) + sizeof(QueueState);
   uint64_t walk_launches = 0;
-  for (uint32_t ng : c->fdev->phase_count) walk_launches += (ng + 65534) / 65535;
+  for (uint32_t ng : c->fdev->phase_count)
+    if (ng) walk_launches += (ng + 65534) / 65535 + 1;  // walk + chunk pass
   st->launches += 2 * ((nq + 65534) / 65535) + walk_launches + 2;
   if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[0], c->stream));
-  s = launch_filter(g, ch.fq, nq, *c->fdev, c->stream, c->num_sms);
+  s = launch_filter(g, ch.fq, nq, *c->fdev, walk_overflow(ch), c->stream, c->num_sms);
   if (s) return s;
   if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[1], c->stream));
   s = launch_join(jl, c->stream, c->num_sms);
@@ -617,7 +666,7 @@ smg_status smg_filter_inspect(smg_ctx *c, const smg_graph *G, const smg_plan *p,
   if (s) return s;
   if (vmask0)
     SMG_CUDA(cudaMemcpyAsync(vmask0, ch.vmask[0], static_cast<size_t>(g.n) * 4, cudaMemcpyDeviceToHost, c->stream));
-  s = launch_walks(g, ch.fq, *c->fdev, c->stream, c->num_sms);
+  s = launch_walks(g, ch.fq, *c->fdev, walk_overflow(ch), c->stream, c->num_sms);
   if (s) return s;
   s = launch_collect(g, ch.fq, 1, c->stream, c->num_sms);
   if (s) return s;

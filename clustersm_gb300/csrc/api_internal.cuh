@@ -34,7 +34,8 @@ struct QCounters {
   unsigned long long stat[4];  // [0] sum |C(u)| final, [1] walk list entries
   unsigned long long count;    // embeddings
   unsigned long long emb_count;
-  unsigned long long pad2[8];
+  unsigned long long pending;  // tasks of this query not yet finished
+  unsigned long long pad2[7];
 };
 static_assert(sizeof(QCounters) % 16 == 0, "QCounters must keep 16-byte alignment");
 
@@ -83,6 +84,25 @@ struct smg_graph {
 };
 
 namespace smg {
+// Device buffers holding one query's filter state and results.
+struct QueryBuffers {
+  uint32_t *vmask = nullptr, *enc = nullptr, *cand = nullptr, *roots = nullptr;
+  QCounters *counters = nullptr;
+  uint32_t *emb = nullptr;
+  uint64_t emb_cap = 0;
+};
+// Sizes of those buffers for one plan (bytes, each rounded to 256).
+struct QueryFootprint {
+  size_t vmask, enc, cand, roots;
+  size_t total() const { return vmask + enc + cand + roots; }
+};
+QueryFootprint query_footprint(const DevGraph &g, const Plan &P);
+// Fills the filter and join records of one query whose state lives in `b`.
+smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffers &b, uint64_t count_limit,
+                              FilterQuery &f, JoinQuery &j);
+constexpr uint32_t kMaxWalkPhases = 2 * 100;  // 2 * MAX_LAYERS - 1 phases at most
+constexpr uint32_t kWalkCap = 1u << 20;        // chunk-pass items per filter launch
+
 // Filter + join for `nq` plans against a resident graph; splits into chunks
 // that fit the device memory.  out[i] receives plan i's results.
 smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, uint32_t nq, const RunOpts &o,

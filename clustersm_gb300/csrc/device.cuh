@@ -122,6 +122,7 @@ struct JoinQuery {
   unsigned long long *emb_count;
   unsigned long long count_limit;  // 0: none; else stop once the count exceeds it
   uint32_t *over;             // set to 1 when the count exceeded count_limit
+  unsigned long long *pending;  // tasks of this query queued or running
 };
 
 }  // namespace smg

@@ -140,18 +140,53 @@ __device__ __forceinline__ void spread_slots(const ClusterStep &st, uint32_t xm,
   }
 }
 
-__global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict__ off,
-                                                      const uint32_t *__restrict__ adj,
-                                                      const StepGroup *__restrict__ groups,
-                                                      const ClusterStep *__restrict__ steps,
-                                                      const uint32_t *__restrict__ aux,
-                                                      const FilterQuery *__restrict__ qs) {
-  const StepGroup G = groups[blockIdx.y];
-  const FilterQuery &Q = qs[G.query];
-  const int lane = threadIdx.x & 31;
+// Neighbour part of a step group for candidate v over adj[e0, e1): set the
+// neighbour slots of every step v passed (star / merge), or apply the
+// combine rule (AND of the other clusters' slots) to each neighbour.
+__device__ __forceinline__ void walk_neighbors(const uint32_t *__restrict__ adj, const StepGroup &G,
+                                               const ClusterStep *__restrict__ steps,
+                                               const uint32_t *__restrict__ aux, const FilterQuery &Q,
+                                               uint32_t kind, uint32_t pass, uint32_t e0, uint32_t e1,
+                                               uint32_t lane) {
   const uint32_t W = Q.words;
   uint32_t *const enc = Q.enc;
   const uint32_t *const vmask = Q.vmask;
+  for (uint32_t e = e0 + lane; e < e1; e += 32) {
+    const uint32_t w = adj[e];
+    if (kind != 2) {
+      const uint32_t xm = vmask[w];
+      if (!xm) continue;
+      for (uint32_t p = pass; p; p &= p - 1) spread_slots(steps[G.first + __ffs(p) - 1], xm, enc, W, w);
+    } else {
+      const ClusterStep &st = steps[G.first];
+      uint32_t t = st.targets_off;
+      for (uint32_t ti = 0; ti < st.num_targets; ++ti) {
+        const uint32_t slot = aux[t], nsrc = aux[t + 1];
+        bool fin = true;
+        for (uint32_t s = 0; s < nsrc && fin; ++s) fin = enc_bit(enc, W, w, aux[t + 2 + s]);
+        t += 2 + nsrc;
+        if (st.type == 0) {
+          if (fin) enc_set(enc, W, w, slot >> 5, 1u << (slot & 31));
+        } else if (!fin) {
+          enc_clear(enc, W, w, slot);
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict__ off,
+                                                      const uint32_t *__restrict__ adj,
+                                                      const StepGroup *__restrict__ groups, uint32_t group_base,
+                                                      const ClusterStep *__restrict__ steps,
+                                                      const uint32_t *__restrict__ aux,
+                                                      const FilterQuery *__restrict__ qs, WalkOverflow ov) {
+  const uint32_t gi = group_base + blockIdx.y;
+  const StepGroup G = groups[gi];
+  const FilterQuery &Q = qs[G.query];
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t W = Q.words;
+  uint32_t *const enc = Q.enc;
   uint32_t *const list = Q.cand + Q.cand_off[G.core];
   const uint32_t cnt = *(volatile const uint32_t *)(Q.cand_cnt + G.core);
   const uint32_t kind = steps[G.first].kind;
@@ -190,31 +225,54 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
       }
     }
     if (kind != 2 && pass == 0) continue;
-    scanned += off[v + 1] - off[v];
-    for (uint32_t e = off[v] + lane; e < off[v + 1]; e += 32) {
-      const uint32_t w = adj[e];
-      if (kind != 2) {
-        const uint32_t xm = vmask[w];
-        if (!xm) continue;
-        for (uint32_t p = pass; p; p &= p - 1) spread_slots(steps[G.first + __ffs(p) - 1], xm, enc, W, w);
-      } else {
-        const ClusterStep &st = steps[G.first];
-        uint32_t t = st.targets_off;
-        for (uint32_t ti = 0; ti < st.num_targets; ++ti) {
-          const uint32_t slot = aux[t], nsrc = aux[t + 1];
-          bool fin = true;
-          for (uint32_t s = 0; s < nsrc && fin; ++s) fin = enc_bit(enc, W, w, aux[t + 2 + s]);
-          t += 2 + nsrc;
-          if (st.type == 0) {
-            if (fin) enc_set(enc, W, w, slot >> 5, 1u << (slot & 31));
-          } else if (!fin) {
-            enc_clear(enc, W, w, slot);
+    const uint32_t e0 = off[v], e1 = off[v + 1];
+    scanned += e1 - e0;
+    uint32_t mine = e1;
+    if (e1 - e0 > kWalkChunk) {
+      // hand the tail of a long list to the chunk pass, one warp per chunk
+      const uint32_t extra = (e1 - e0 - 1) / kWalkChunk;
+      uint32_t base = kNone;
+      if (lane == 0) {
+        unsigned int old = *(volatile unsigned int *)ov.count;
+        while (old + extra <= ov.cap) {
+          const unsigned int seen = atomicCAS(ov.count, old, old + extra);
+          if (seen == old) {
+            base = old;
+            break;
           }
+          old = seen;
         }
       }
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base != kNone) {
+        for (uint32_t c = lane; c < extra; c += 32)
+          ov.items[base + c] = make_uint4(gi, v, pass, e0 + (c + 1) * kWalkChunk);
+        mine = e0 + kWalkChunk;
+      }
     }
+    walk_neighbors(adj, G, steps, aux, Q, kind, pass, e0, mine, lane);
   }
   if (lane == 0 && scanned) atomicAdd(Q.stat + 1, scanned);
+}
+
+// Chunks of long neighbour lists queued by k_cluster_walk: one warp each.
+__global__ void __launch_bounds__(256) k_walk_chunks(const uint32_t *__restrict__ off,
+                                                     const uint32_t *__restrict__ adj,
+                                                     const StepGroup *__restrict__ groups,
+                                                     const ClusterStep *__restrict__ steps,
+                                                     const uint32_t *__restrict__ aux,
+                                                     const FilterQuery *__restrict__ qs, WalkOverflow ov) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t n = min(*ov.count, ov.cap);
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    const uint4 it = ov.items[i];
+    const StepGroup G = groups[it.x];
+    const FilterQuery &Q = qs[G.query];
+    const uint32_t kind = steps[G.first].kind;
+    const uint32_t e1 = min(it.w + kWalkChunk, off[it.y + 1]);
+    walk_neighbors(adj, G, steps, aux, Q, kind, it.z, it.w, e1, lane);
+  }
 }
 
 // --------------------------------------------------------------- collect
@@ -458,18 +516,23 @@ smg_status launch_nlc_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_
   return SMG_OK;
 }
 
-smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const FilterDev &fd, cudaStream_t s,
-                        int num_sms) {
+smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const FilterDev &fd, WalkOverflow ov,
+                        cudaStream_t s, int num_sms) {
   for (size_t p = 0; p < fd.phase_count.size(); ++p) {
     const uint32_t ng = fd.phase_count[p];
     if (!ng) continue;
+    WalkOverflow po = ov;
+    po.count = ov.count + 2 * p;  // one zeroed counter per phase
     const uint32_t wx = std::max<uint32_t>(1, std::min<uint32_t>(2048, (num_sms * 16u + ng - 1) / ng));
     for (uint32_t y0 = 0; y0 < ng; y0 += 65535) {
       const uint32_t ny = std::min<uint32_t>(65535, ng - y0);
-      k_cluster_walk<<<dim3(wx, ny), 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p] + y0, fd.steps,
-                                                  fd.aux, d_qs);
+      k_cluster_walk<<<dim3(wx, ny), 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p], y0, fd.steps,
+                                                  fd.aux, d_qs, po);
       SMG_CUDA(cudaGetLastError());
     }
+    k_walk_chunks<<<num_sms * 8, 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p], fd.steps, fd.aux,
+                                                d_qs, po);
+    SMG_CUDA(cudaGetLastError());
   }
   return SMG_OK;
 }
@@ -485,10 +548,10 @@ smg_status launch_collect(const DevGraph &g, const FilterQuery *d_qs, uint32_t n
 }
 
 smg_status launch_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, const FilterDev &fd,
-                         cudaStream_t s, int num_sms) {
+                         WalkOverflow ov, cudaStream_t s, int num_sms) {
   smg_status st = launch_nlc_filter(g, d_qs, nq, s, num_sms);
   if (st) return st;
-  st = launch_walks(g, d_qs, fd, s, num_sms);
+  st = launch_walks(g, d_qs, fd, ov, s, num_sms);
   if (st) return st;
   return launch_collect(g, d_qs, nq, s, num_sms);
 }

@@ -9,6 +9,18 @@ namespace smg {
 
 // Neighbour-label counts are kept for labels below this bound.
 constexpr uint32_t kMaxLabels = 256;
+// Neighbour lists longer than this are walked by several warps, one chunk each.
+constexpr uint32_t kWalkChunk = 2048;
+
+// Chunks of long neighbour lists queued by one walk phase for the chunk pass.
+// `count` points at this phase's counter (zeroed before the run; the walk
+// launcher gives each phase its own); items are (group, vertex, passed-step
+// mask, first adjacency index).
+struct WalkOverflow {
+  unsigned int *count;
+  uint32_t cap;
+  uint4 *items;
+};
 
 // Steps of the cluster bitmap for a batch of queries, grouped into phases:
 // phase 0 = stars of layer 0; phase 2l-1 = merges of layer l; phase 2l =
@@ -44,10 +56,10 @@ smg_status append_filter_steps(const Plan &P, uint32_t query_index, FilterBatch 
 // FilterQuery records are at d_qs (device).  Candidate counters, the bitmap
 // and the root counters must be zero on entry.
 smg_status launch_nlc_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, cudaStream_t s, int num_sms);
-smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const FilterDev &fd, cudaStream_t s,
-                        int num_sms);
+smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const FilterDev &fd, WalkOverflow ov,
+                        cudaStream_t s, int num_sms);
 smg_status launch_collect(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, cudaStream_t s, int num_sms);
 smg_status launch_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_t nq, const FilterDev &fd,
-                         cudaStream_t s, int num_sms);
+                         WalkOverflow ov, cudaStream_t s, int num_sms);
 
 }  // namespace smg

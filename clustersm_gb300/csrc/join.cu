@@ -74,6 +74,7 @@ __device__ int wait_ticket(const JoinLaunch &p, unsigned long long ticket, uint6
     if ((polls++ & 15) == 0) {
       if (vload(qs->pending) == 0) return 0;
       if (*reinterpret_cast<volatile int *>(&qs->abort)) return 0;
+      if (*reinterpret_cast<volatile int *>(&qs->closing)) return 0;
       const uint64_t pr = vload(qs->progress), t = now_ns();
       if (pr != idle_mark || idle_t0 == 0) {
         idle_mark = pr;
@@ -94,13 +95,16 @@ __device__ int wait_ticket(const JoinLaunch &p, unsigned long long ticket, uint6
 
 __global__ void k_seed(JoinLaunch p) {
   if (blockIdx.x == 0 && threadIdx.x == 0) p.qs->start_ns = now_ns();
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < p.nq; q += gridDim.x * blockDim.x) {
+  const uint32_t nseed = p.seed_list ? p.seed_n : p.nq;
+  for (uint32_t si = blockIdx.x * blockDim.x + threadIdx.x; si < nseed; si += gridDim.x * blockDim.x) {
+    const uint32_t q = p.seed_list ? p.seed_list[si] : si;
     const uint32_t nr = *p.queries[q].num_roots;
     if (nr == 0) continue;
     uint32_t chunk = p.root_chunk ? p.root_chunk : 1;
     chunk = max(chunk, (nr + p.max_seed_tasks - 1) / p.max_seed_tasks);
     const uint32_t nt = (nr + chunk - 1) / chunk;
     atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
+    atomicAdd(p.queries[q].pending, static_cast<unsigned long long>(nt));
     const unsigned long long first = atomicAdd(&p.qs->tail.v, static_cast<unsigned long long>(nt));
     const uint32_t tw = 4 + p.kmax;
     for (uint32_t i = 0; i < nt; ++i) {
@@ -310,8 +314,8 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
 // shallowest unexplored work of this warp's stack: the back half of a level's
 // unscanned list, or else one untried candidate of a level's batch (which
 // becomes a task one level deeper).  Returns true when something was pushed.
-__device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, uint32_t L0, uint32_t level, uint32_t P,
-                           uint32_t lane) {
+__device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned long long *qpending, uint32_t L0,
+                           uint32_t level, uint32_t P, uint32_t lane) {
   int pushed = 0;
   if (lane == 0) {
     QueueState *qs = p.qs;
@@ -341,6 +345,7 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, uint32_
           const unsigned long long slot = atomicAdd(&qs->tail.v, 1ull);
           if (slot < p.cap) {
             atomicAdd(&qs->pending.v, 1ull);
+            atomicAdd(qpending, 1ull);
             uint32_t *T = p.tasks + slot * (4 + p.kmax);
             T[0] = q;
             T[1] = tl;
@@ -370,6 +375,65 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, uint32_
   return pushed != 0;
 }
 
+// End of a time slice: every part of this warp's stack that is not done
+// becomes a carry-over task: the unscanned rest of each level's list, and each
+// untried batch candidate (as a task one level deeper).  Returns false (and
+// the warp keeps working) if the carry buffer cannot take them all.
+__device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned long long *qpending, uint32_t L0,
+                        uint32_t level, uint32_t P, uint32_t lane) {
+  int ok = 0;
+  if (lane == 0) {
+    uint32_t n = 0;
+    for (uint32_t l = L0; l <= level; ++l) {
+      if (S.cur[l] < S.end[l]) ++n;
+      if (l < P) n += S.bcnt[l] - S.bidx[l];
+    }
+    if (n == 0) {
+      ok = 1;
+    } else {
+      unsigned int old = *reinterpret_cast<volatile unsigned int *>(p.carry_count);
+      unsigned int base = kNone;
+      while (old + n <= p.carry_cap) {
+        const unsigned int seen = atomicCAS(p.carry_count, old, old + n);
+        if (seen == old) {
+          base = old;
+          break;
+        }
+        old = seen;
+      }
+      if (base != kNone) {
+        const uint32_t tw = 4 + p.kmax;
+        uint32_t idx = base;
+        for (uint32_t l = L0; l <= level; ++l) {
+          if (S.cur[l] < S.end[l]) {
+            uint32_t *T = p.carry + static_cast<uint64_t>(idx++) * tw;
+            T[0] = q;
+            T[1] = l;
+            T[2] = S.cur[l];
+            T[3] = S.end[l];
+            for (uint32_t j = 0; j < l; ++j) T[4 + j] = S.m[j];
+          }
+          if (l < P)
+            for (uint32_t b = S.bidx[l]; b < S.bcnt[l]; ++b) {
+              uint32_t *T = p.carry + static_cast<uint64_t>(idx++) * tw;
+              T[0] = q;
+              T[1] = l + 1;
+              T[2] = 0;
+              T[3] = kNone;
+              for (uint32_t j = 0; j < l; ++j) T[4 + j] = S.m[j];
+              T[4 + l] = S.batch[l * 32 + b];
+            }
+        }
+        atomicAdd(qpending, static_cast<unsigned long long>(n));
+        ok = 1;
+      }
+    }
+  }
+  ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -386,8 +450,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     int got = 0;
     unsigned long long slot = 0;
     if (lane == 0) {
-      slot = atomicAdd(&qs->head.v, 1ull);
-      got = wait_ticket(p, slot, idle_mark, idle_t0);
+      if (!*reinterpret_cast<volatile int *>(&qs->closing)) {
+        slot = atomicAdd(&qs->head.v, 1ull);
+        got = wait_ticket(p, slot, idle_mark, idle_t0);
+        if (got == 1) p.ready[slot] = 2;  // taken (a time-sliced run carries untaken ones over)
+      }
     }
     got = __shfl_sync(0xFFFFFFFFu, got, 0);
     if (got != 1) break;
@@ -401,6 +468,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
       if (lane == 0) {
         atomicAdd(&qs->tasks_done, 1ull);
         atomicAdd(&qs->progress.v, 1ull);
+        atomicAdd(Q.pending, ~0ull);
         atomicAdd(&qs->pending.v, ~0ull);
       }
       continue;
@@ -437,7 +505,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     unsigned long long cnt = 0;
     uint32_t level = L0, iter = 0, tick = 0;  // tick paces donation checks
     const uint32_t *const candmask = Q.candmask;
-    bool aborted = false;
+    bool aborted = false, preempted = false;
     while (true) {
       if ((++iter & 255) == 0) {
         int stop = 0;
@@ -470,9 +538,26 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
           break;
         }
       }
+      // time slice over (serving): hand the rest of this stack back and leave
+      if (p.slice_ns && (iter & 31) == 0) {
+        int close = 0;
+        if (lane == 0) {
+          if (*reinterpret_cast<volatile int *>(&qs->closing)) {
+            close = 1;
+          } else if (now_ns() - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.slice_ns) {
+            atomicExch(&qs->closing, 1);
+            close = 1;
+          }
+        }
+        close = __shfl_sync(0xFFFFFFFFu, close, 0);
+        if (close && !(level == P && S.bcnt[P] != 0) && preempt(S, p, q, Q.pending, L0, level, P, lane)) {
+          preempted = true;
+          break;
+        }
+      }
       // give the shallowest unexplored work of this stack to a waiting warp
       if ((++tick & 3) == 0) {
-        if (try_donate(S, p, q, L0, level, P, lane)) continue;
+        if (try_donate(S, p, q, Q.pending, L0, level, P, lane)) continue;
       }
       if (level == P) {
         const uint32_t bc = S.bcnt[level];
@@ -555,16 +640,85 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
       if (!aborted) {
         atomicAdd(&qs->tasks_done, 1ull);
         atomicAdd(&qs->progress.v, 1ull);
+        atomicAdd(Q.pending, ~0ull);       // -1
         atomicAdd(&qs->pending.v, ~0ull);  // -1
       }
     }
     scanned = 0;
     descents = 0;
-    if (aborted) break;
+    if (aborted || preempted) break;
+  }
+}
+
+__global__ void k_slice_begin(QueueState *qs) {
+  qs->start_ns = now_ns();
+  qs->closing = 0;
+}
+
+// Single block: keep the published-but-untaken tasks of the old queue
+// (ready == 1) in order, then append the carry-over tasks.
+__global__ void __launch_bounds__(1024) k_compact(const uint32_t *__restrict__ tasks_old,
+                                                  const uint32_t *__restrict__ ready_old, uint32_t n_old,
+                                                  const uint32_t *__restrict__ carry,
+                                                  const unsigned int *__restrict__ carry_count, uint32_t carry_cap,
+                                                  uint32_t tw, uint32_t *__restrict__ tasks_new,
+                                                  uint32_t *__restrict__ ready_new, QueueState *qs) {
+  __shared__ uint32_t warp_sum[32];
+  __shared__ uint32_t running;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid == 0) running = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < n_old; base += blockDim.x) {
+    const uint32_t i = base + tid;
+    const bool keep = i < n_old && ready_old[i] == 1;
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
+    if (lane == 0) warp_sum[wid] = __popc(bal);
+    __syncthreads();
+    uint32_t before = running;
+    for (uint32_t w = 0; w < wid; ++w) before += warp_sum[w];
+    if (keep) {
+      const uint32_t dst = before + __popc(bal & ((1u << lane) - 1));
+      for (uint32_t j = 0; j < tw; ++j) tasks_new[static_cast<uint64_t>(dst) * tw + j] = tasks_old[static_cast<uint64_t>(i) * tw + j];
+      ready_new[dst] = 1;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t tot = 0;
+      for (uint32_t w = 0; w < blockDim.x / 32; ++w) tot += warp_sum[w];
+      running += tot;
+    }
+    __syncthreads();
+  }
+  const uint32_t kept = running;
+  const uint32_t nc = min(*carry_count, carry_cap);
+  for (uint32_t i = tid; i < nc; i += blockDim.x) {
+    for (uint32_t j = 0; j < tw; ++j) tasks_new[static_cast<uint64_t>(kept + i) * tw + j] = carry[static_cast<uint64_t>(i) * tw + j];
+    ready_new[kept + i] = 1;
+  }
+  if (tid == 0) {
+    qs->head.v = 0;
+    qs->tail.v = kept + nc;
+    qs->pending.v = kept + nc;
+    qs->closing = 0;
   }
 }
 
 }  // namespace
+
+smg_status launch_slice_begin(QueueState *qs, cudaStream_t s) {
+  k_slice_begin<<<1, 1, 0, s>>>(qs);
+  SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
+
+smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, uint32_t n_old,
+                          const uint32_t *carry, const unsigned int *carry_count, uint32_t carry_cap, uint32_t tw,
+                          uint32_t *tasks_new, uint32_t *ready_new, QueueState *qs, cudaStream_t s) {
+  k_compact<<<1, 1024, 0, s>>>(tasks_old, ready_old, n_old, carry, carry_count, carry_cap, tw, tasks_new, ready_new,
+                               qs);
+  SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
 
 size_t join_queue_bytes(uint32_t cap, uint32_t kmax) {
   return static_cast<size_t>(cap) * (4 + kmax) * sizeof(uint32_t) + static_cast<size_t>(cap) * sizeof(uint32_t);
@@ -579,9 +733,30 @@ smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   SMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join, kWarpsPerBlock * 32, smem));
   per_sm = std::max(1, per_sm);
   const uint32_t seed_threads = 128;
-  k_seed<<<(jl.nq + seed_threads - 1) / seed_threads, seed_threads, 0, s>>>(jl);
+  const uint32_t nseed = jl.seed_list ? jl.seed_n : jl.nq;
+  k_seed<<<(nseed + seed_threads - 1) / seed_threads, seed_threads, 0, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
   k_join<<<num_sms * per_sm, kWarpsPerBlock * 32, smem, s>>>(jl);
+  SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
+
+smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
+  const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
+  if (smem > 48 * 1024)
+    SMG_CUDA(cudaFuncSetAttribute(k_join, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  int per_sm = 0;
+  SMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join, kWarpsPerBlock * 32, smem));
+  per_sm = std::max(1, per_sm);
+  k_join<<<num_sms * per_sm, kWarpsPerBlock * 32, smem, s>>>(jl);
+  SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
+
+smg_status launch_seed(const JoinLaunch &jl, cudaStream_t s) {
+  const uint32_t n = jl.seed_list ? jl.seed_n : jl.nq;
+  if (!n) return SMG_OK;
+  k_seed<<<(n + 127) / 128, 128, 0, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }

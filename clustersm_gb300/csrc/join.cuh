@@ -23,7 +23,7 @@ struct QueueState {
   int error;  // JOIN_ERR_* below, first one wins
   int abort;  // set on error or deadline: every warp leaves
   int full;   // a donation found the queue full (load balance only)
-  int pad;
+  int closing;  // the time slice is over: warps hand their work back and leave
 };
 constexpr int JOIN_ERR_READY_TIMEOUT = 1;  // a claimed task was never published
 constexpr int JOIN_ERR_DEADLINE = 2;       // the run exceeded its time limit
@@ -45,6 +45,14 @@ struct JoinLaunch {
   uint32_t donate_min;       // shortest remaining list worth donating
   uint64_t time_limit_ns;    // device-side deadline for the whole run
   int emit;
+  // time-sliced runs (serving): after slice_ns every warp pushes what is left
+  // of its stack to `carry` and leaves; 0 = run to completion
+  uint64_t slice_ns;
+  uint32_t *carry;           // [carry_cap][4 + kmax]
+  uint32_t carry_cap;
+  unsigned int *carry_count;
+  const uint32_t *seed_list; // seed only these query indices (null: 0 .. nq-1)
+  uint32_t seed_n;
 };
 
 // Bytes of queue storage for `cap` tasks of a batch whose largest query has
@@ -54,6 +62,18 @@ size_t join_queue_bytes(uint32_t cap, uint32_t kmax);
 // no host round trip sits between the filter and the join) and runs the
 // persistent kernel.  QueueState must be zeroed on entry.
 smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms);
+// Starts a time slice (clock and closing flag) without seeding.
+smg_status launch_slice_begin(QueueState *qs, cudaStream_t s);
+// Seeds the root tasks of jl.queries[0 .. jl.nq) (appending to the queue).
+smg_status launch_seed(const JoinLaunch &jl, cudaStream_t s);
+// Persistent join without seeding (tasks already queued).
+smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms);
+// Rebuilds the queue after a slice: published-but-untaken tasks of the old
+// queue, then the carry-over tasks, into `tasks_new` (ready_new zeroed on
+// entry); resets head/tail/pending.  Single block.
+smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, uint32_t n_old,
+                          const uint32_t *carry, const unsigned int *carry_count, uint32_t carry_cap, uint32_t tw,
+                          uint32_t *tasks_new, uint32_t *ready_new, QueueState *qs, cudaStream_t s);
 // Neighbour bitmaps of the highest-degree vertices (degree >= min_degree,
 // at most max_bytes of bitmaps), built once per resident graph.
 smg_status build_hub_bitmaps(DevGraph &g, uint32_t min_degree, size_t max_bytes, cudaStream_t s,

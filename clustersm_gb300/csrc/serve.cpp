@@ -1,11 +1,26 @@
-// serve.cpp — request loop over a resident data graph.
+// serve.cpp — continuous-batching request loop over a resident data graph.
 //
 // The reference has no serving mode: runClusterSM.sh starts one process per
 // query and re-reads the data graph each time (runClusterSM.sh:9-13).  Here
-// requests are queued, admitted against a device-memory budget estimated from
-// each query's filter footprint, and run together as one batch (one filter
-// pass and one persistent join launch for the admitted set).
+// the data graph stays resident and requests flow through one shared,
+// persistent work queue:
+//
+//   * a request is admitted into a slot when a slot is free and its device
+//     state (candidate masks, cluster bitmap, candidate lists) fits the memory
+//     budget; admission order is arrival order;
+//   * newly admitted queries are filtered together and their root tasks are
+//     appended to the live queue;
+//   * the join runs in time slices (SMG_SLICE_MS, default 2 ms): at the end of
+//     a slice every warp hands the unfinished part of its depth-first stack
+//     back as tasks, so requests that arrived meanwhile start in the next
+//     slice alongside the ones still running;
+//   * a query is finished when its count of queued and running tasks is zero;
+//     its slot and memory are released and its count is final.
+//
+// smg_server_step never blocks while a slice is on the device.
 #include <chrono>
+#include <cstdlib>
+#include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
@@ -18,11 +33,62 @@ double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+constexpr uint32_t kServerK = smg::kMaxK;  // task width covers any query
+
 struct Request {
   uint64_t ticket;
   const smg::Plan *plan;
   double submit_s;
   uint64_t bytes;
+};
+
+struct Slot {
+  bool used = false;
+  uint64_t ticket = 0;
+  const smg::Plan *plan = nullptr;
+  size_t off = 0, size = 0;  // pool range
+  double submit_s = 0, start_s = 0;
+};
+
+// First-fit allocator over one device buffer, with coalescing frees.
+struct Pool {
+  char *base = nullptr;
+  size_t size = 0;
+  std::map<size_t, size_t> free_;  // offset -> length
+  void init(char *b, size_t s) {
+    base = b;
+    size = s;
+    free_.clear();
+    free_[0] = s;
+  }
+  bool alloc(size_t n, size_t &off) {
+    n = (n + 255) & ~size_t(255);
+    for (auto it = free_.begin(); it != free_.end(); ++it)
+      if (it->second >= n) {
+        off = it->first;
+        const size_t rest = it->second - n;
+        free_.erase(it);
+        if (rest) free_[off + n] = rest;
+        return true;
+      }
+    return false;
+  }
+  void release(size_t off, size_t n) {
+    n = (n + 255) & ~size_t(255);
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
 };
 
 }  // namespace
@@ -32,48 +98,242 @@ struct smg_server {
   const smg_graph *graph = nullptr;
   smg_server_config cfg{};
   uint64_t next_ticket = 1;
-  std::deque<Request> queue;
+  std::deque<Request> waiting;
+  std::vector<Slot> slots;
   std::map<uint64_t, smg_request_result> done;
+  Pool pool;
+  // device allocations
+  char *pool_mem = nullptr;
+  smg::FilterQuery *d_fq_new = nullptr;  // contiguous records of the newly admitted
+  smg::JoinQuery *d_jq = nullptr;        // [max_inflight], indexed by slot
+  smg::QCounters *d_cnt = nullptr;       // [max_inflight]
+  uint32_t *d_seed = nullptr;            // slots to seed
+  uint32_t *tasks[2] = {nullptr, nullptr};
+  uint32_t *ready[2] = {nullptr, nullptr};
+  uint32_t *carry = nullptr;
+  unsigned int *carry_count = nullptr;
+  smg::QueueState *qs = nullptr;
+  unsigned int *walk_count = nullptr;
+  uint4 *walk_items = nullptr;
+  uint32_t cap = 0, carry_cap = 0, cur = 0;
+  uint64_t slice_ns = 0;
+  cudaEvent_t ev = nullptr;
+  bool inflight = false;
+  uint64_t slices = 0;
+  smg::FilterDev fdev;
+  std::vector<smg::QCounters> h_cnt;
+
+  ~smg_server() {
+    if (ctx) cudaStreamSynchronize(ctx->stream);
+    for (void *p : {static_cast<void *>(pool_mem), static_cast<void *>(d_fq_new), static_cast<void *>(d_jq),
+                    static_cast<void *>(d_cnt), static_cast<void *>(d_seed), static_cast<void *>(tasks[0]),
+                    static_cast<void *>(tasks[1]), static_cast<void *>(ready[0]), static_cast<void *>(ready[1]),
+                    static_cast<void *>(carry), static_cast<void *>(carry_count), static_cast<void *>(qs),
+                    static_cast<void *>(walk_count), static_cast<void *>(walk_items)})
+      if (p) cudaFree(p);
+    if (ev) cudaEventDestroy(ev);
+  }
 };
 
 namespace {
 
-uint64_t footprint(const smg::DevGraph &g, const smg::Plan &P) {
-  uint64_t cand = 0;
-  for (uint32_t u = 0; u < P.k; ++u) cand += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
-  return static_cast<uint64_t>(g.n) * 4 * (1 + P.num_words) + cand * 8 + 4096;
+using smg::fail;
+
+uint32_t task_words() { return 4 + kServerK; }
+
+smg::WalkOverflow walk_overflow(smg_server *s) {
+  smg::WalkOverflow w;
+  w.count = s->walk_count;
+  w.cap = smg::kWalkCap;
+  w.items = s->walk_items;
+  return w;
 }
 
-smg_status run_admitted(smg_server *s) {
-  if (s->queue.empty()) return SMG_OK;
-  std::vector<Request> batch;
-  uint64_t used = 0;
-  while (!s->queue.empty() && batch.size() < s->cfg.max_inflight) {
-    const Request &r = s->queue.front();
-    if (!batch.empty() && used + r.bytes > s->cfg.memory_budget_bytes) break;
-    used += r.bytes;
-    batch.push_back(r);
-    s->queue.pop_front();
+smg::JoinLaunch join_launch(smg_server *s) {
+  const smg::DevGraph &g = s->graph->g;
+  smg::JoinLaunch jl;
+  std::memset(&jl, 0, sizeof(jl));
+  jl.off = g.off;
+  jl.adj = g.adj;
+  jl.hub_of = g.hub_of;
+  jl.hub_bits = g.hub_bits;
+  jl.hub_words = g.hub_words;
+  jl.queries = s->d_jq;
+  jl.nq = s->cfg.max_inflight;
+  jl.kmax = kServerK;
+  jl.qs = s->qs;
+  jl.tasks = s->tasks[s->cur];
+  jl.ready = s->ready[s->cur];
+  jl.cap = s->cap;
+  jl.max_seed_tasks = 256;
+  jl.donate_min = 33;
+  jl.time_limit_ns = smg::time_limit_ns();
+  jl.slice_ns = s->slice_ns;
+  jl.carry = s->carry;
+  jl.carry_cap = s->carry_cap;
+  jl.carry_count = s->carry_count;
+  return jl;
+}
+
+bool any_active(const smg_server *s) {
+  for (const Slot &sl : s->slots)
+    if (sl.used) return true;
+  return false;
+}
+
+// Empty queue: head = tail = pending = 0, every ready flag clear.
+smg_status reset_queue(smg_server *s) {
+  cudaStream_t st = s->ctx->stream;
+  SMG_CUDA(cudaMemsetAsync(s->qs, 0, sizeof(smg::QueueState), st));
+  SMG_CUDA(cudaMemsetAsync(s->ready[0], 0, static_cast<size_t>(s->cap) * 4, st));
+  SMG_CUDA(cudaMemsetAsync(s->ready[1], 0, static_cast<size_t>(s->cap) * 4, st));
+  SMG_CUDA(cudaMemsetAsync(s->carry_count, 0, sizeof(unsigned int), st));
+  s->cur = 0;
+  return SMG_OK;
+}
+
+void retire(smg_server *s, Slot &sl, smg_status status, uint64_t count) {
+  smg_request_result r{};
+  r.status = status;
+  r.count = status ? 0 : count;
+  r.submit_s = sl.submit_s;
+  r.start_s = sl.start_s;
+  r.finish_s = now_s();
+  s->done[sl.ticket] = r;
+  s->pool.release(sl.off, sl.size);
+  sl = Slot();
+}
+
+// After a slice: read every slot's counters, retire finished queries, and
+// rebuild the queue from untaken and carried-over tasks.
+smg_status finish_slice(smg_server *s) {
+  cudaStream_t st = s->ctx->stream;
+  smg::QueueState hq;
+  SMG_CUDA(cudaMemcpyAsync(s->h_cnt.data(), s->d_cnt, s->h_cnt.size() * sizeof(smg::QCounters),
+                           cudaMemcpyDeviceToHost, st));
+  SMG_CUDA(cudaMemcpyAsync(&hq, s->qs, sizeof(hq), cudaMemcpyDeviceToHost, st));
+  SMG_CUDA(cudaStreamSynchronize(st));
+  if (hq.error) {
+    for (Slot &sl : s->slots)
+      if (sl.used) retire(s, sl, SMG_ERR_TIMEOUT, 0);
+    return reset_queue(s);
   }
-  const double start = now_s();
-  std::vector<const smg::Plan *> plans;
-  for (auto &r : batch) plans.push_back(r.plan);
-  std::vector<smg::QueryOut> out(batch.size());
-  smg::RunStats st;
-  smg::RunOpts o;
-  smg_status rc = smg::run_queries(s->ctx, s->graph->g, plans.data(), static_cast<uint32_t>(plans.size()), o,
-                                   out.data(), &st);
-  const double fin = now_s();
-  for (size_t i = 0; i < batch.size(); ++i) {
-    smg_request_result res{};
-    res.status = rc;
-    res.count = rc ? 0 : out[i].count;
-    res.submit_s = batch[i].submit_s;
-    res.start_s = start;
-    res.finish_s = fin;
-    s->done[batch[i].ticket] = res;
+  for (size_t i = 0; i < s->slots.size(); ++i) {
+    Slot &sl = s->slots[i];
+    if (sl.used && s->h_cnt[i].pending == 0) retire(s, sl, SMG_OK, s->h_cnt[i].count);
   }
-  return rc;
+  if (!any_active(s)) return reset_queue(s);
+  const uint32_t other = 1 - s->cur;
+  const uint32_t n_old = static_cast<uint32_t>(std::min<unsigned long long>(hq.tail.v, s->cap));
+  SMG_CUDA(cudaMemsetAsync(s->ready[other], 0, static_cast<size_t>(s->cap) * 4, st));
+  smg_status rc = smg::launch_compact(s->tasks[s->cur], s->ready[s->cur], n_old, s->carry, s->carry_count,
+                                      s->carry_cap, task_words(), s->tasks[other], s->ready[other], s->qs, st);
+  if (rc) return rc;
+  SMG_CUDA(cudaMemsetAsync(s->carry_count, 0, sizeof(unsigned int), st));
+  s->cur = other;
+  return SMG_OK;
+}
+
+// Admit waiting requests (arrival order) while slots and memory allow; filter
+// them together and append their root tasks to the live queue.
+smg_status admit(smg_server *s) {
+  const smg::DevGraph &g = s->graph->g;
+  cudaStream_t st = s->ctx->stream;
+  std::vector<uint32_t> fresh;
+  std::vector<smg::QueryFootprint> fps;
+  const double t = now_s();
+  while (!s->waiting.empty()) {
+    uint32_t idx = smg::kNone;
+    for (uint32_t i = 0; i < s->slots.size(); ++i)
+      if (!s->slots[i].used) {
+        idx = i;
+        break;
+      }
+    if (idx == smg::kNone) break;
+    const Request &r = s->waiting.front();
+    const smg::QueryFootprint fp = smg::query_footprint(g, *r.plan);
+    size_t off = 0;
+    if (!s->pool.alloc(fp.total(), off)) break;  // wait for memory to free up
+    Slot &sl = s->slots[idx];
+    sl.used = true;
+    sl.ticket = r.ticket;
+    sl.plan = r.plan;
+    sl.off = off;
+    sl.size = fp.total();
+    sl.submit_s = r.submit_s;
+    sl.start_s = t;
+    s->waiting.pop_front();
+    fresh.push_back(idx);
+    fps.push_back(fp);
+  }
+  if (fresh.empty()) return SMG_OK;
+  const uint32_t n = static_cast<uint32_t>(fresh.size());
+  smg::FilterQuery *hf = static_cast<smg::FilterQuery *>(s->ctx->pinned);
+  smg::JoinQuery *hj = reinterpret_cast<smg::JoinQuery *>(hf + n);
+  uint32_t *hseed = reinterpret_cast<uint32_t *>(hj + n);
+  smg::FilterBatch fb;
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t idx = fresh[i];
+    const Slot &sl = s->slots[idx];
+    char *base = s->pool.base + sl.off;
+    smg::QueryBuffers b;
+    b.vmask = reinterpret_cast<uint32_t *>(base);
+    b.enc = reinterpret_cast<uint32_t *>(base + fps[i].vmask);
+    b.cand = reinterpret_cast<uint32_t *>(base + fps[i].vmask + fps[i].enc);
+    b.roots = reinterpret_cast<uint32_t *>(base + fps[i].vmask + fps[i].enc + fps[i].cand);
+    b.counters = s->d_cnt + idx;
+    smg_status rc = smg::make_query_records(*sl.plan, g, b, 0, hf[i], hj[i]);
+    if (rc) return rc;
+    rc = smg::append_filter_steps(*sl.plan, i, fb);
+    if (rc) return rc;
+    hseed[i] = idx;
+    SMG_CUDA(cudaMemsetAsync(b.enc, 0, fps[i].enc, st));
+    SMG_CUDA(cudaMemsetAsync(b.counters, 0, sizeof(smg::QCounters), st));
+    SMG_CUDA(cudaMemcpyAsync(s->d_jq + idx, hj + i, sizeof(smg::JoinQuery), cudaMemcpyHostToDevice, st));
+  }
+  smg_status rc = s->fdev.upload(fb, st);
+  if (rc) return rc;
+  SMG_CUDA(cudaMemcpyAsync(s->d_fq_new, hf, n * sizeof(smg::FilterQuery), cudaMemcpyHostToDevice, st));
+  SMG_CUDA(cudaMemcpyAsync(s->d_seed, hseed, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  SMG_CUDA(cudaMemsetAsync(s->walk_count, 0, smg::kMaxWalkPhases * 2 * sizeof(unsigned int), st));
+  rc = smg::launch_filter(g, s->d_fq_new, n, s->fdev, walk_overflow(s), st, s->ctx->num_sms);
+  if (rc) return rc;
+  smg::JoinLaunch jl = join_launch(s);
+  jl.seed_list = s->d_seed;
+  jl.seed_n = n;
+  rc = smg::launch_seed(jl, st);
+  if (rc) return rc;
+  // the pinned staging is reused by the next admission: finish the copies
+  SMG_CUDA(cudaStreamSynchronize(st));
+  return SMG_OK;
+}
+
+smg_status launch_slice(smg_server *s) {
+  cudaStream_t st = s->ctx->stream;
+  smg_status rc = smg::launch_slice_begin(s->qs, st);
+  if (rc) return rc;
+  rc = smg::launch_join_only(join_launch(s), st, s->ctx->num_sms);
+  if (rc) return rc;
+  SMG_CUDA(cudaEventRecord(s->ev, st));
+  s->inflight = true;
+  ++s->slices;
+  return SMG_OK;
+}
+
+smg_status step(smg_server *s) {
+  SMG_CUDA(cudaSetDevice(s->ctx->device));
+  if (s->inflight) {
+    const cudaError_t e = cudaEventQuery(s->ev);
+    if (e == cudaErrorNotReady) return SMG_OK;
+    if (e != cudaSuccess) return smg::cuda_fail(e, "server slice");
+    s->inflight = false;
+    smg_status rc = finish_slice(s);
+    if (rc) return rc;
+  }
+  smg_status rc = admit(s);
+  if (rc) return rc;
+  if (any_active(s)) return launch_slice(s);
+  return SMG_OK;
 }
 
 }  // namespace
@@ -81,36 +341,72 @@ smg_status run_admitted(smg_server *s) {
 extern "C" {
 
 smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_config *cfg, smg_server **out) {
-  if (!c || !g || !out) return smg::fail(SMG_ERR_INVALID, "null argument");
+  if (!c || !g || !out) return fail(SMG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  SMG_CUDA(cudaSetDevice(c->device));
   std::unique_ptr<smg_server> s(new smg_server);
   s->ctx = c;
   s->graph = g;
   if (cfg) s->cfg = *cfg;
-  if (!s->cfg.max_inflight) s->cfg.max_inflight = 256;
-  if (!s->cfg.memory_budget_bytes) s->cfg.memory_budget_bytes = 32ull << 30;
+  if (!s->cfg.max_inflight) s->cfg.max_inflight = 64;
+  const size_t per_rec = sizeof(smg::FilterQuery) + sizeof(smg::JoinQuery) + 4;
+  if (s->cfg.max_inflight * per_rec > smg::kPinnedBytes) return fail(SMG_ERR_LIMIT, "max_inflight too large");
+  size_t free_b = 0, total_b = 0;
+  SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (!s->cfg.memory_budget_bytes) s->cfg.memory_budget_bytes = std::min<size_t>(32ull << 30, free_b / 3);
+  const char *sl = std::getenv("SMG_SLICE_MS");
+  s->slice_ns = static_cast<uint64_t>((sl ? std::atof(sl) : 2.0) * 1e6);
+  if (!s->slice_ns) s->slice_ns = 2000000;
+  s->cap = 2u << 20;
+  s->carry_cap = 1u << 20;
+  const size_t tw = task_words();
+  SMG_CUDA(cudaMalloc(&s->pool_mem, s->cfg.memory_budget_bytes));
+  s->pool.init(s->pool_mem, s->cfg.memory_budget_bytes);
+  SMG_CUDA(cudaMalloc(&s->d_fq_new, s->cfg.max_inflight * sizeof(smg::FilterQuery)));
+  SMG_CUDA(cudaMalloc(&s->d_jq, s->cfg.max_inflight * sizeof(smg::JoinQuery)));
+  SMG_CUDA(cudaMalloc(&s->d_cnt, s->cfg.max_inflight * sizeof(smg::QCounters)));
+  SMG_CUDA(cudaMalloc(&s->d_seed, s->cfg.max_inflight * sizeof(uint32_t)));
+  for (int i = 0; i < 2; ++i) {
+    SMG_CUDA(cudaMalloc(&s->tasks[i], static_cast<size_t>(s->cap) * tw * 4));
+    SMG_CUDA(cudaMalloc(&s->ready[i], static_cast<size_t>(s->cap) * 4));
+  }
+  SMG_CUDA(cudaMalloc(&s->carry, static_cast<size_t>(s->carry_cap) * tw * 4));
+  SMG_CUDA(cudaMalloc(&s->carry_count, sizeof(unsigned int)));
+  SMG_CUDA(cudaMalloc(&s->qs, sizeof(smg::QueueState)));
+  SMG_CUDA(cudaMalloc(&s->walk_count, smg::kMaxWalkPhases * 2 * sizeof(unsigned int)));
+  SMG_CUDA(cudaMalloc(&s->walk_items, static_cast<size_t>(smg::kWalkCap) * sizeof(uint4)));
+  SMG_CUDA(cudaMemsetAsync(s->d_cnt, 0, s->cfg.max_inflight * sizeof(smg::QCounters), c->stream));
+  SMG_CUDA(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
+  s->slots.resize(s->cfg.max_inflight);
+  s->h_cnt.resize(s->cfg.max_inflight);
+  smg_status rc = reset_queue(s.get());
+  if (rc) return rc;
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
   *out = s.release();
   return SMG_OK;
 }
 
 smg_status smg_server_submit(smg_server *s, const smg_plan *p, uint64_t *ticket) {
-  if (!s || !p || !ticket) return smg::fail(SMG_ERR_INVALID, "null argument");
-  const uint64_t bytes = footprint(s->graph->g, p->p);
-  if (bytes > s->cfg.memory_budget_bytes) return smg::fail(SMG_ERR_BUDGET, "query exceeds the server memory budget");
+  if (!s || !p || !ticket) return fail(SMG_ERR_INVALID, "null argument");
+  const uint64_t bytes = smg::query_footprint(s->graph->g, p->p).total();
+  if (bytes > s->cfg.memory_budget_bytes) return fail(SMG_ERR_BUDGET, "query exceeds the server memory budget");
+  for (uint32_t u = 0; u < p->p.k; ++u)
+    if (p->p.label[u] >= smg::kMaxLabels) return fail(SMG_ERR_LIMIT, "query labels must be below 256");
   *ticket = s->next_ticket++;
-  s->queue.push_back({*ticket, &p->p, now_s(), bytes});
+  s->waiting.push_back({*ticket, &p->p, now_s(), bytes});
   return SMG_OK;
 }
 
 smg_status smg_server_step(smg_server *s) {
-  if (!s) return smg::fail(SMG_ERR_INVALID, "null server");
-  return run_admitted(s);
+  if (!s) return fail(SMG_ERR_INVALID, "null server");
+  return step(s);
 }
 
 smg_status smg_server_poll(smg_server *s, uint64_t ticket, smg_request_result *out) {
-  if (!s || !out) return smg::fail(SMG_ERR_INVALID, "null argument");
+  if (!s || !out) return fail(SMG_ERR_INVALID, "null argument");
   auto it = s->done.find(ticket);
   if (it == s->done.end()) {
-    if (ticket == 0 || ticket >= s->next_ticket) return smg::fail(SMG_ERR_INVALID, "unknown ticket");
+    if (ticket == 0 || ticket >= s->next_ticket) return fail(SMG_ERR_INVALID, "unknown ticket");
     return SMG_ERR_NOT_READY;
   }
   *out = it->second;
@@ -118,25 +414,26 @@ smg_status smg_server_poll(smg_server *s, uint64_t ticket, smg_request_result *o
 }
 
 smg_status smg_server_cancel(smg_server *s, uint64_t ticket) {
-  if (!s) return smg::fail(SMG_ERR_INVALID, "null server");
-  for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+  if (!s) return fail(SMG_ERR_INVALID, "null server");
+  for (auto it = s->waiting.begin(); it != s->waiting.end(); ++it)
     if (it->ticket == ticket) {
       smg_request_result res{};
       res.status = SMG_ERR_CANCELLED;
       res.submit_s = it->submit_s;
       res.finish_s = now_s();
       s->done[ticket] = res;
-      s->queue.erase(it);
+      s->waiting.erase(it);
       return SMG_OK;
     }
-  return smg::fail(SMG_ERR_INVALID, "ticket is not queued");
+  return fail(SMG_ERR_INVALID, "ticket is not waiting (unknown, running or finished)");
 }
 
 smg_status smg_server_drain(smg_server *s) {
-  if (!s) return smg::fail(SMG_ERR_INVALID, "null server");
-  while (!s->queue.empty()) {
-    smg_status rc = run_admitted(s);
+  if (!s) return fail(SMG_ERR_INVALID, "null server");
+  while (s->inflight || !s->waiting.empty() || any_active(s)) {
+    smg_status rc = step(s);
     if (rc) return rc;
+    if (s->inflight) SMG_CUDA(cudaEventSynchronize(s->ev));
   }
   return SMG_OK;
 }

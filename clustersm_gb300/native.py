@@ -431,3 +431,48 @@ def filter_inspect(ctx: Context, graph: DeviceGraph, plan: Plan):
     check(lib.smg_filter_inspect(ctx.handle, graph.handle, plan.handle, vm.ctypes.data_as(u32p),
                                  enc.ctypes.data_as(u32p), cm.ctypes.data_as(u32p)), "smg_filter_inspect")
     return vm, enc, cm
+
+
+class Server:
+    """Continuous-batching request loop (smg_server_*).  Plans must outlive
+    their requests; this wrapper keeps a reference until the result is read."""
+
+    def __init__(self, ctx: Context, graph: DeviceGraph, memory_budget_bytes: int = 0, max_inflight: int = 0):
+        self.ctx, self.graph = ctx, graph
+        cfg = ServerConfig(memory_budget_bytes, max_inflight, 0)
+        self._h = C.c_void_p()
+        check(lib.smg_server_create(ctx.handle, graph.handle, C.byref(cfg), C.byref(self._h)), "smg_server_create")
+        self._plans = {}
+
+    def submit(self, plan: Plan) -> int:
+        t = C.c_uint64()
+        check(lib.smg_server_submit(self._h, plan.handle, C.byref(t)), "smg_server_submit")
+        self._plans[t.value] = plan
+        return t.value
+
+    def step(self):
+        check(lib.smg_server_step(self._h), "smg_server_step")
+
+    def poll(self, ticket: int):
+        """RequestResult, or None while the request is queued or running."""
+        r = RequestResult()
+        st = lib.smg_server_poll(self._h, ticket, C.byref(r))
+        if st == 12:
+            return None
+        check(st, "smg_server_poll")
+        self._plans.pop(ticket, None)
+        return r
+
+    def cancel(self, ticket: int):
+        check(lib.smg_server_cancel(self._h, ticket), "smg_server_cancel")
+
+    def drain(self):
+        check(lib.smg_server_drain(self._h), "smg_server_drain")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.smg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

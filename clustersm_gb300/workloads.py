@@ -51,6 +51,15 @@ def load(name: str) -> Workload:
     return WORKLOADS[name]
 
 
+def shard(n: int, rank: int, world: int) -> list[int]:
+    """Query indices of `rank` when n queries are dealt round-robin to `world`
+    ranks.  Each rank matches its share against its own replica of the data
+    graph; no data moves between ranks (embeddings are independent per query)."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad rank/world")
+    return list(range(rank, n, world))
+
+
 WORKLOADS = {
     "er1k": Workload("er1k", "er", n=1000, m=4000, labels=4, zipf=False, seed=1,
                      queries_file="tests/golden/workload_er1k.json",

@@ -1,0 +1,75 @@
+"""Serving: continuous batching over one resident graph.  Every response's
+count equals the query's count alone (plain path) and the committed oracle
+count, whether it ran alone or in a mix, and requests submitted while others
+are on the device join the running work."""
+import time
+
+import pytest
+
+from clustersm_gb300 import native
+from clustersm_gb300.native import DeviceGraph, Plan, Server
+from clustersm_gb300.workloads import load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def er(ctx):
+    wl = load("er1k")
+    qs, want, _ = wl.queries()
+    host = wl.graph()
+    return DeviceGraph(ctx, host), [Plan(q) for q in qs], want
+
+
+def test_alone_equals_in_mix(ctx, er):
+    dev, plans, want = er
+    srv = Server(ctx, dev, max_inflight=16)
+    t = srv.submit(plans[0])
+    srv.drain()
+    alone = srv.poll(t)
+    assert alone.status == 0 and alone.count == want[0]
+    tickets = [srv.submit(p) for p in plans]
+    srv.drain()
+    for tk, w in zip(tickets, want):
+        r = srv.poll(tk)
+        assert r.status == 0 and r.count == w
+        assert r.finish_s >= r.start_s >= r.submit_s
+    srv.close()
+
+
+def test_arrivals_while_running(ctx):
+    wl = load("rmat22")
+    try:
+        qs, want, _ = wl.queries()
+    except FileNotFoundError:
+        pytest.skip("rmat22 workload not generated")
+    host = wl.graph()
+    dev = DeviceGraph(ctx, host)
+    plans = [Plan(q) for q in qs[:96]]
+    srv = Server(ctx, dev, max_inflight=32)
+    tickets = []
+    for i, p in enumerate(plans):
+        tickets.append(srv.submit(p))
+        if i % 8 == 7:
+            srv.step()  # non-blocking: admits, launches or retires
+    srv.drain()
+    for tk, w in zip(tickets, want[:96]):
+        r = srv.poll(tk)
+        assert r.status == 0 and r.count == w
+    for p, w in list(zip(plans, want))[:8]:
+        res, _ = native.match(ctx, dev, p)
+        assert res.count == w
+
+
+def test_cancel_and_budget(ctx, er):
+    dev, plans, want = er
+    srv = Server(ctx, dev, max_inflight=2)
+    ts = [srv.submit(p) for p in plans[:6]]
+    srv.cancel(ts[-1])
+    srv.drain()
+    assert srv.poll(ts[-1]).status == 11  # SMG_ERR_CANCELLED
+    assert all(srv.poll(t).count == w for t, w in zip(ts[:-1], want[:5]))
+    small = Server(ctx, dev, memory_budget_bytes=1024)
+    with pytest.raises(native.SmgError) as e:
+        small.submit(plans[0])
+    assert e.value.status == 10  # SMG_ERR_BUDGET
