@@ -260,6 +260,12 @@ struct Chunk {
 
 }  // namespace
 
+uint32_t plan_class(const Plan &P) {
+  const uint32_t shape = P.m + 1 == P.k ? 0u : (2 * P.m >= 3 * P.k ? 2u : 1u);
+  const uint32_t size = P.k <= 5 ? 0u : P.k <= 8 ? 1u : P.k <= 12 ? 2u : 3u;
+  return 4 * shape + size;
+}
+
 QueryFootprint query_footprint(const DevGraph &g, const Plan &P) {
   QueryFootprint f;
   uint64_t cand = 0;
@@ -426,6 +432,13 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     b.emb_cap = ch.emb ? o.emb_cap : 0;
     smg_status st = make_query_records(P, g, b, o.count_limit, hf[i], hj[i]);
     if (st) return st;
+    if (o.tuning && !o.root_chunk) {
+      const TuneSetting &t = o.tuning[plan_class(P)];
+      if (t.valid) {
+        hj[i].root_chunk = t.root_chunk;
+        hj[i].donate_min = t.donate_min;
+      }
+    }
     st = append_filter_steps(P, i, fb);
     if (st) return st;
   }
@@ -461,7 +474,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   jl.cap = ch.cap;
   jl.root_chunk = o.root_chunk;
   jl.max_seed_tasks = seed_tasks(c, o, nq);
-  jl.donate_min = 33;
+  jl.donate_min = 2;
   jl.time_limit_ns = time_limit_ns();
   jl.emit = ch.emb != nullptr;
   st->h2d += c->fdev->host.size() + nq * (sizeof(FilterQuery) + sizeof(JoinQuery));
@@ -578,6 +591,7 @@ smg_status smg_match(smg_ctx *c, const smg_graph *G, const smg_plan *p, const sm
   if (G->device != c->device) return fail(SMG_ERR_INVALID, "graph lives on another device");
   std::memset(out, 0, sizeof(*out));
   RunOpts o;
+  o.tuning = c->tuning;
   if (opts) {
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
@@ -618,6 +632,7 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
     pl[i] = &plans[i]->p;
   }
   RunOpts o;
+  o.tuning = c->tuning;
   if (opts) {
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
@@ -676,6 +691,73 @@ smg_status smg_filter_inspect(smg_ctx *c, const smg_graph *G, const smg_plan *p,
   if (candmask)
     SMG_CUDA(cudaMemcpyAsync(candmask, ch.vmask[0], static_cast<size_t>(g.n) * 4, cudaMemcpyDeviceToHost, c->stream));
   SMG_CUDA(cudaStreamSynchronize(c->stream));
+  return SMG_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+uint32_t smg_plan_class(const smg_plan *p) { return p ? plan_class(p->p) : 0u; }
+
+smg_status smg_set_tuning(smg_ctx *c, const smg_tune_entry *e, uint32_t n) {
+  if (!c || (n && !e)) return fail(SMG_ERR_INVALID, "null argument");
+  for (uint32_t i = 0; i < n; ++i) {
+    if (e[i].shape_class >= SMG_TUNE_CLASSES) return fail(SMG_ERR_INVALID, "bad shape class");
+    TuneSetting &t = c->tuning[e[i].shape_class];
+    t.root_chunk = e[i].root_chunk;
+    t.donate_min = e[i].donate_min;
+    t.valid = e[i].samples > 0;
+  }
+  return SMG_OK;
+}
+
+smg_status smg_autotune(smg_ctx *c, const smg_graph *G, const smg_plan *const *plans, uint32_t n,
+                        smg_tune_entry *out) {
+  if (!c || !G || (n && !plans)) return fail(SMG_ERR_INVALID, "null argument");
+  static const uint32_t kChunks[] = {1, 8, 64};
+  static const uint32_t kDonate[] = {2, 33, 129};
+  std::vector<std::vector<const Plan *>> by_class(SMG_TUNE_CLASSES);
+  for (uint32_t i = 0; i < n; ++i)
+    if (plans[i] && by_class[plan_class(plans[i]->p)].size() < 32) by_class[plan_class(plans[i]->p)].push_back(&plans[i]->p);
+  for (uint32_t cls = 0; cls < SMG_TUNE_CLASSES; ++cls) {
+    smg_tune_entry e{cls, 0, 0, 0, 0.f, 0.f};
+    const auto &sample = by_class[cls];
+    if (!sample.empty()) {
+      float best = -1.f;
+      for (uint32_t rc : kChunks)
+        for (uint32_t dm : kDonate) {
+          TuneSetting t[SMG_TUNE_CLASSES];
+          t[cls].root_chunk = rc;
+          t[cls].donate_min = dm;
+          t[cls].valid = true;
+          RunOpts o;
+          o.tuning = t;
+          o.profile = true;
+          std::vector<QueryOut> q(sample.size());
+          float ms = 0.f;
+          for (int rep = 0; rep < 2; ++rep) {  // first run warms caches
+            RunStats st;
+            smg_status s = run_queries(c, G->g, sample.data(), static_cast<uint32_t>(sample.size()), o, q.data(), &st);
+            if (s) return s;
+            ms = st.filter_ms + st.join_ms;
+          }
+          if (rc == kChunks[0] && dm == kDonate[0]) e.default_ms = ms;
+          if (best < 0 || ms < best) {
+            best = ms;
+            e.root_chunk = rc;
+            e.donate_min = dm;
+          }
+        }
+      e.samples = static_cast<uint32_t>(sample.size());
+      e.best_ms = best;
+      TuneSetting &t = c->tuning[cls];
+      t.root_chunk = e.root_chunk;
+      t.donate_min = e.donate_min;
+      t.valid = true;
+    }
+    if (out) out[cls] = e;
+  }
   return SMG_OK;
 }
 

@@ -42,7 +42,14 @@ static_assert(sizeof(QCounters) % 16 == 0, "QCounters must keep 16-byte alignmen
 uint64_t time_limit_ns();
 
 // Options of one run (plain path: one query; batched: many).
+struct TuneSetting {
+  uint32_t root_chunk = 0, donate_min = 0;
+  bool valid = false;
+};
+uint32_t plan_class(const Plan &P);
+
 struct RunOpts {
+  const TuneSetting *tuning = nullptr;  // per shape class, SMG_TUNE_CLASSES entries
   bool profile = false;
   uint32_t root_chunk = 0;
   uint32_t max_seed_tasks = 0;   // 0: derived from the device size
@@ -76,6 +83,7 @@ struct smg_ctx {
   void *pinned = nullptr;  // kPinnedBytes of page-locked staging
   smg::Arena arena;
   std::unique_ptr<smg::FilterDev> fdev;
+  smg::TuneSetting tuning[SMG_TUNE_CLASSES];
 };
 
 struct smg_graph {

@@ -123,6 +123,8 @@ struct JoinQuery {
   unsigned long long count_limit;  // 0: none; else stop once the count exceeds it
   uint32_t *over;             // set to 1 when the count exceeded count_limit
   unsigned long long *pending;  // tasks of this query queued or running
+  uint32_t root_chunk;        // root candidates per seeded task (0: from max_seed_tasks)
+  uint32_t donate_min;        // shortest list worth splitting off (0: launch default)
 };
 
 }  // namespace smg

@@ -100,7 +100,8 @@ __global__ void k_seed(JoinLaunch p) {
     const uint32_t q = p.seed_list ? p.seed_list[si] : si;
     const uint32_t nr = *p.queries[q].num_roots;
     if (nr == 0) continue;
-    uint32_t chunk = p.root_chunk ? p.root_chunk : 1;
+    const uint32_t rc = p.queries[q].root_chunk ? p.queries[q].root_chunk : p.root_chunk;
+    uint32_t chunk = rc ? rc : 1;
     chunk = max(chunk, (nr + p.max_seed_tasks - 1) / p.max_seed_tasks);
     const uint32_t nt = (nr + chunk - 1) / chunk;
     atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
@@ -315,7 +316,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
 // unscanned list, or else one untried candidate of a level's batch (which
 // becomes a task one level deeper).  Returns true when something was pushed.
 __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned long long *qpending, uint32_t L0,
-                           uint32_t level, uint32_t P, uint32_t lane) {
+                           uint32_t level, uint32_t P, uint32_t lane, uint32_t min_rem) {
   int pushed = 0;
   if (lane == 0) {
     QueueState *qs = p.qs;
@@ -327,7 +328,7 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, unsigne
         for (uint32_t l = L0; l <= level && tl == kNone; ++l) {
           const uint32_t c = S.cur[l], e = S.end[l];
           const uint32_t rem = e > c ? e - c : 0;
-          if (rem >= 2 || (rem == 1 && l < level)) {
+          if (rem >= min_rem || (rem >= 1 && l < level)) {
             tl = l;
             lo = c + rem / 2;
             hi = e;
@@ -505,6 +506,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     unsigned long long cnt = 0;
     uint32_t level = L0, iter = 0, tick = 0;  // tick paces donation checks
     const uint32_t *const candmask = Q.candmask;
+    const uint32_t donate_min = max(2u, Q.donate_min ? Q.donate_min : p.donate_min);
     bool aborted = false, preempted = false;
     while (true) {
       if ((++iter & 255) == 0) {
@@ -557,7 +559,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
       }
       // give the shallowest unexplored work of this stack to a waiting warp
       if ((++tick & 3) == 0) {
-        if (try_donate(S, p, q, Q.pending, L0, level, P, lane)) continue;
+        if (try_donate(S, p, q, Q.pending, L0, level, P, lane, donate_min)) continue;
       }
       if (level == P) {
         const uint32_t bc = S.bcnt[level];

@@ -166,7 +166,7 @@ smg::JoinLaunch join_launch(smg_server *s) {
   jl.ready = s->ready[s->cur];
   jl.cap = s->cap;
   jl.max_seed_tasks = 256;
-  jl.donate_min = 33;
+  jl.donate_min = 2;
   jl.time_limit_ns = smg::time_limit_ns();
   jl.slice_ns = s->slice_ns;
   jl.carry = s->carry;
@@ -284,6 +284,11 @@ smg_status admit(smg_server *s) {
     b.counters = s->d_cnt + idx;
     smg_status rc = smg::make_query_records(*sl.plan, g, b, 0, hf[i], hj[i]);
     if (rc) return rc;
+    const smg::TuneSetting &tune = s->ctx->tuning[smg::plan_class(*sl.plan)];
+    if (tune.valid) {
+      hj[i].root_chunk = tune.root_chunk;
+      hj[i].donate_min = tune.donate_min;
+    }
     rc = smg::append_filter_steps(*sl.plan, i, fb);
     if (rc) return rc;
     hseed[i] = idx;

@@ -81,6 +81,11 @@ class BatchStats(C.Structure):
                 ("chunks", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class TuneEntry(C.Structure):
+    _fields_ = [("shape_class", C.c_uint32), ("root_chunk", C.c_uint32), ("donate_min", C.c_uint32),
+                ("samples", C.c_uint32), ("best_ms", C.c_float), ("default_ms", C.c_float)]
+
+
 class GraphStats(C.Structure):
     _fields_ = [("num_vertices", C.c_uint32), ("num_edges", C.c_uint64), ("num_labels", C.c_uint32),
                 ("max_degree", C.c_uint32), ("device_bytes", C.c_uint64)]
@@ -133,6 +138,9 @@ def _load():
         "smg_match_batch": (st, [vp, vp, C.POINTER(vp), C.c_uint32, C.POINTER(MatchOpts), u64p,
                                  C.POINTER(BatchStats)]),
         "smg_filter_inspect": (st, [vp, vp, vp, u32p, u32p, u32p]),
+        "smg_autotune": (st, [vp, vp, C.POINTER(vp), C.c_uint32, C.POINTER(TuneEntry)]),
+        "smg_set_tuning": (st, [vp, C.POINTER(TuneEntry), C.c_uint32]),
+        "smg_plan_class": (C.c_uint32, [vp]),
         "smg_server_create": (st, [vp, vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
         "smg_server_submit": (st, [vp, vp, u64p]),
         "smg_server_poll": (st, [vp, C.c_uint64, C.POINTER(RequestResult)]),
@@ -421,6 +429,14 @@ def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk
     check(lib.smg_match_batch(ctx.handle, graph.handle, arr, n, C.byref(opts), counts.ctypes.data_as(u64p),
                               C.byref(st)), "smg_match_batch")
     return counts, st
+
+
+def autotune(ctx: Context, graph: DeviceGraph, plans):
+    """Tune the join per shape class on sample plans; returns the 12 entries."""
+    arr = (C.c_void_p * len(plans))(*[p.handle.value for p in plans])
+    out = (TuneEntry * 12)()
+    check(lib.smg_autotune(ctx.handle, graph.handle, arr, len(plans), out), "smg_autotune")
+    return list(out)
 
 
 def filter_inspect(ctx: Context, graph: DeviceGraph, plan: Plan):

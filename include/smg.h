@@ -269,6 +269,28 @@ smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
                            const smg_match_opts *opts, uint64_t *counts,
                            smg_batch_stats *stats);
 
+/* Autotuning.  Queries fall into shape classes: class = 4 * shape + size,
+ * shape 0 tree (m = k-1), 2 dense (2m >= 3k), 1 sparse otherwise; size 0 for
+ * k <= 5, 1 for 6..8, 2 for 9..12, 3 for 13+.  smg_autotune runs the sample
+ * plans of each class under every candidate setting of the join (root
+ * candidates per seeded task x shortest list worth splitting off to an idle
+ * warp), keeps the fastest per class in the context, and reports them; later
+ * smg_match / smg_match_batch calls on this context apply them. */
+#define SMG_TUNE_CLASSES 12u
+typedef struct smg_tune_entry {
+  uint32_t shape_class;
+  uint32_t root_chunk;
+  uint32_t donate_min;
+  uint32_t samples;  /* sample queries timed for this class (0: untuned) */
+  float best_ms;     /* device time of the sample under the kept setting */
+  float default_ms;  /* device time of the sample under the default setting */
+} smg_tune_entry;
+smg_status smg_autotune(smg_ctx *ctx, const smg_graph *g, const smg_plan *const *plans, uint32_t n,
+                        smg_tune_entry *out /* [SMG_TUNE_CLASSES] or NULL */);
+smg_status smg_set_tuning(smg_ctx *ctx, const smg_tune_entry *entries, uint32_t n);
+/* Shape class of a plan (see above). */
+uint32_t smg_plan_class(const smg_plan *p);
+
 /* Filter only (for inspection): copies to host the per-vertex initial
  * candidate masks (bit u, filter.cu:529-535), the cluster bitmap
  * (num_vertices x num_words words, filter.cu:585-873) and the final
