@@ -15,7 +15,8 @@ queries (4..16 vertices) had at most 10^8 embeddings, and none of those had
 more than 5 vertices.  A drawn query is therefore kept when its exact count is at
 most COUNT_LIMIT, decided on the GPU with the library's per-query count limit
 (the join stops a query as soon as its running count passes the limit) and a
-2 s device deadline; each slot retries new seeds up to MAX_DRAWS times.
+device deadline; each slot retries new seeds up to MAX_DRAWS times (drawn
+and screened in rounds, one batched call per round).
 Every kept count is then recomputed by the CPU oracle; a fixture is written
 only when all counts agree.
 """
@@ -59,40 +60,71 @@ def record(slot, attempt, k, shape, seed, q, count, key):
             "labels": q.labels.tolist(), "edges": q.edges.tolist(), key: int(count)}
 
 
-def gen_gpu(name):
+def gen_gpu(name, seconds=None):
+    """Screen drawn queries on the GPU in rounds: each round draws the next
+    seed of every unfilled slot and matches them all in one batched call with
+    the per-query count limit; queries that finish under the limit fill their
+    slots.  A round that hits the device deadline is re-screened one query at
+    a time."""
     from clustersm_gb300 import native
     from clustersm_gb300.native import Context, DeviceGraph, Plan
-    os.environ["SMG_TIME_LIMIT_S"] = "2"
+    os.environ["SMG_TIME_LIMIT_S"] = "20"
     wl = load(name)
+    nq, ks, shapes = SPECS[name]
     t0 = time.time()
     host = wl.graph()
     ctx = Context(0)
     dev = DeviceGraph(ctx, host)
-    out, done_slot, tried, timeouts = [], -1, 0, 0
-    for slot, attempt, k, shape, seed in draws(name):
-        if slot == done_slot:
-            continue
-        try:
-            q = Query.generate(host, k, shape, seed=seed)
-        except SmgError:
-            continue
-        tried += 1
-        try:
-            res, _ = native.match(ctx, dev, Plan(q), max_count=COUNT_LIMIT)
-        except SmgError:
-            timeouts += 1
-            continue
-        if res.limit_hit:
-            continue
-        out.append(record(slot, attempt, k, shape, seed, q, res.count, "gpu_count"))
-        done_slot = slot
+    rng = random.Random(f"{name}-slots")
+    slot_k = [rng.choice(ks) for _ in range(nq)]
+    kept = {}
+    tried = timeouts = 0
     path = ROOT / "gpurun_out" / f"workload_{name}.json"
     path.parent.mkdir(exist_ok=True)
-    path.write_text(json.dumps({"workload": name, "count_limit": COUNT_LIMIT, "max_draws": MAX_DRAWS,
-                                "slots": SPECS[name][0], "kept": len(out), "draws_total": tried,
-                                "timeouts": timeouts, "seconds": round(time.time() - t0, 1),
-                                "queries": out}, separators=(",", ":")))
-    print(f"{name}: kept {len(out)} of {SPECS[name][0]} slots, {tried} draws, {timeouts} timeouts -> {path}")
+
+    def save(complete):
+        out = [kept[s] for s in sorted(kept)]
+        path.write_text(json.dumps({"workload": name, "count_limit": COUNT_LIMIT, "max_draws": MAX_DRAWS,
+                                    "slots": nq, "kept": len(out), "draws_total": tried, "timeouts": timeouts,
+                                    "seconds": round(time.time() - t0, 1), "complete": complete,
+                                    "queries": out}, separators=(",", ":")))
+
+    for attempt in range(MAX_DRAWS):
+        if seconds and time.time() - t0 > seconds:
+            break
+        batch = []
+        for slot in range(nq):
+            if slot in kept:
+                continue
+            k, shape, seed = slot_k[slot], shapes[slot % len(shapes)], (slot << 20) | attempt
+            try:
+                batch.append((slot, k, shape, seed, Query.generate(host, k, shape, seed=seed)))
+            except SmgError:
+                pass
+        if not batch:
+            break
+        tried += len(batch)
+        plans = [Plan(b[4]) for b in batch]
+        try:
+            counts, _ = native.match_batch(ctx, dev, plans, max_count=COUNT_LIMIT)
+            results = [None if c == 2**64 - 1 else int(c) for c in counts.tolist()]
+        except SmgError:
+            results = []
+            for p in plans:
+                try:
+                    r, _ = native.match(ctx, dev, p, max_count=COUNT_LIMIT)
+                    results.append(None if r.limit_hit else int(r.count))
+                except SmgError:
+                    timeouts += 1
+                    results.append(None)
+        for (slot, k, shape, seed, q), c in zip(batch, results):
+            if c is not None:
+                kept[slot] = record(slot, attempt, k, shape, seed, q, c, "gpu_count")
+        save(False)
+        print(f"{name}: round {attempt}: {len(kept)} kept, {tried} draws, {timeouts} timeouts, "
+              f"{time.time() - t0:.0f} s", flush=True)
+    save(True)
+    print(f"{name}: kept {len(kept)} of {nq} slots, {tried} draws -> {path}", flush=True)
 
 
 def verify(name, src=None):
@@ -146,5 +178,9 @@ def gen_cpu(name):
 
 if __name__ == "__main__":
     mode, names = sys.argv[1], sys.argv[2:]
+    budget = float(os.environ.get("WORKLOAD_SECONDS", "0")) or None
     for n in names:
-        {"gpu": gen_gpu, "verify": verify, "cpu": gen_cpu}[mode](n)
+        if mode == "gpu":
+            gen_gpu(n, budget)
+        else:
+            {"verify": verify, "cpu": gen_cpu}[mode](n)
