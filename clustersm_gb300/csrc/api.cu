@@ -69,6 +69,13 @@ size_t hub_max_bytes() {
   return s ? static_cast<size_t>(std::atoll(s)) : (2ull << 30);
 }
 
+void drop_graph(smg_ctx *c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  c->graph_exec = nullptr;
+  c->graph_key.clear();
+  c->graph_gen = ~0ull;
+}
+
 uint64_t time_limit_ns() {
   const char *s = std::getenv("SMG_TIME_LIMIT_S");
   double v = s ? std::atof(s) : 120.0;
@@ -113,6 +120,7 @@ void smg_close(smg_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
   c->arena.~Arena();
   new (&c->arena) Arena();
   c->fdev.reset();
@@ -447,17 +455,13 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
   if (st) return st;
   SMG_CUDA(cudaMemcpyAsync(ch.fq, hf, nq * sizeof(FilterQuery), cudaMemcpyHostToDevice, c->stream));
   SMG_CUDA(cudaMemcpyAsync(ch.jq, hj, nq * sizeof(JoinQuery), cudaMemcpyHostToDevice, c->stream));
-  SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
   // the staging buffer is reused by the read-back: finish the copies first
   SMG_CUDA(cudaStreamSynchronize(c->stream));
   return SMG_OK;
 }
 
-smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Chunk &ch, const RunOpts &o,
-                     QueryOut *out, RunStats *st) {
+JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunOpts &o) {
   const uint32_t nq = ch.b - ch.a;
-  smg_status s = stage_chunk(c, g, plans, ch, o);
-  if (s) return s;
   JoinLaunch jl;
   std::memset(&jl, 0, sizeof(jl));
   jl.off = g.off;
@@ -477,25 +481,73 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   jl.donate_min = 2;
   jl.time_limit_ns = time_limit_ns();
   jl.emit = ch.emb != nullptr;
-  st->h2d += c->fdev->host.size() + nq * (sizeof(FilterQuery) + sizeof(JoinQuery));
-  st->d2h += nq * sizeof(QCounters) + sizeof(QueueState);
-  uint64_t walk_launches = 0;
-  for (uint32_t ng : c->fdev->phase_count)
-    if (ng) walk_launches += (ng + 65534) / 65535 + 1;  // walk + chunk pass
-  st->launches += 2 * ((nq + 65534) / 65535) + walk_launches + 2;
+  return jl;
+}
+
+// Zeroing memset, filter, seeding and join of a staged chunk on the stream
+// (also what a captured graph holds).
+smg_status enqueue_chunk(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunOpts &o) {
+  const uint32_t nq = ch.b - ch.a;
+  SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
   if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[0], c->stream));
-  s = launch_filter(g, ch.fq, nq, *c->fdev, walk_overflow(ch), c->stream, c->num_sms);
+  smg_status s = launch_filter(g, ch.fq, nq, *c->fdev, walk_overflow(ch), c->stream, c->num_sms);
   if (s) return s;
   if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[1], c->stream));
-  s = launch_join(jl, c->stream, c->num_sms);
+  s = launch_join(make_join_launch(c, g, ch, o), c->stream, c->num_sms);
   if (s) return s;
   if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[2], c->stream));
+  return SMG_OK;
+}
+
+smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Chunk &ch, const RunOpts &o,
+                     QueryOut *out, RunStats *st, const std::vector<const void *> *key) {
+  const uint32_t nq = ch.b - ch.a;
+  const bool replay = key && c->graph_exec && c->graph_gen == c->run_gen && c->graph_key == *key;
+  ++c->run_gen;
+  if (replay) {
+    SMG_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
+    c->graph_gen = c->run_gen;
+    st->launches += c->graph_launches;
+  } else {
+    smg_status s = stage_chunk(c, g, plans, ch, o);
+    if (s) return s;
+    st->h2d += c->fdev->host.size() + nq * (sizeof(FilterQuery) + sizeof(JoinQuery));
+    uint64_t walk_launches = 0;
+    for (uint32_t ng : c->fdev->phase_count)
+      if (ng) walk_launches += (ng + 65534) / 65535 + 1;  // walk + chunk pass
+    const uint64_t launches = 2 * ((nq + 65534) / 65535) + walk_launches + 2;
+    st->launches += launches;
+    if (key) {
+      drop_graph(c);
+      cudaGraph_t graph = nullptr;
+      SMG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      s = enqueue_chunk(c, g, ch, o);
+      cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+      if (s) {
+        if (graph) cudaGraphDestroy(graph);
+        return s;
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+      e = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+      c->graph_key = *key;
+      c->graph_launches = launches;
+      SMG_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
+      c->graph_gen = c->run_gen;
+    } else {
+      s = enqueue_chunk(c, g, ch, o);
+      if (s) return s;
+    }
+  }
+  st->d2h += nq * sizeof(QCounters) + sizeof(QueueState);
   QCounters *hc = static_cast<QCounters *>(c->pinned);
   QueueState *hq = reinterpret_cast<QueueState *>(static_cast<char *>(c->pinned) + al(nq * sizeof(QCounters)));
   SMG_CUDA(cudaMemcpyAsync(hc, ch.counters, nq * sizeof(QCounters), cudaMemcpyDeviceToHost, c->stream));
   SMG_CUDA(cudaMemcpyAsync(hq, ch.qs, sizeof(QueueState), cudaMemcpyDeviceToHost, c->stream));
   SMG_CUDA(cudaStreamSynchronize(c->stream));
   if (hq->error) {
+    drop_graph(c);
     const char *why = hq->error == JOIN_ERR_DEADLINE ? "join exceeded its time limit (SMG_TIME_LIMIT_S)"
                       : hq->error == JOIN_ERR_IDLE_TIMEOUT ? "join made no progress for too long"
                                                             : "a queued task was never published";
@@ -513,7 +565,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
     for (uint32_t u = 0; u < plans[ch.a + i]->k; ++u) q.initial_cands += hc[i].cand_cnt[u];
     q.emb_written = ch.emb ? std::min<uint64_t>(hc[i].emb_count, o.emb_cap) : 0;
     q.overflow = ch.emb ? (hc[i].emb_count > o.emb_cap) : 0;
-    // algorithmic bytes of the filter (see the design doc for the model)
+    // algorithmic bytes of the filter (model in the design doc)
     const Plan &P = *plans[ch.a + i];
     uint64_t lab = 0;
     std::vector<char> seen(kMaxLabels, 0);
@@ -572,9 +624,20 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     Chunk ch;
     ch.a = a;
     ch.b = b;
+    const size_t cap_before = c->arena.cap;
     smg_status s = layout_chunk(c, g, plans, ch, o);
     if (s) return s;
-    s = run_chunk(c, g, plans, ch, o, out, st);
+    if (c->arena.cap != cap_before) drop_graph(c);  // arena moved: captured pointers are stale
+    std::vector<const void *> key;
+    const bool whole = a == 0 && b == nq;
+    if (o.use_graph && whole) {
+      key.push_back(&g);
+      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.root_chunk)));
+      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.count_limit)));
+      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.profile)));
+      for (uint32_t i = 0; i < nq; ++i) key.push_back(plans[i]);
+    }
+    s = run_chunk(c, g, plans, ch, o, out, st, key.empty() ? nullptr : &key);
     if (s) return s;
     a = b;
   }
@@ -633,10 +696,12 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
   }
   RunOpts o;
   o.tuning = c->tuning;
+  o.use_graph = true;
   if (opts) {
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
     o.count_limit = opts->max_count;
+    o.use_graph = (opts->flags & SMG_FLAG_NO_GRAPH) == 0;
   }
   std::vector<QueryOut> q(n);
   RunStats st;
@@ -675,8 +740,10 @@ smg_status smg_filter_inspect(smg_ctx *c, const smg_graph *G, const smg_plan *p,
   ch.b = 1;
   smg_status s = layout_chunk(c, g, &pl, ch, o);
   if (s) return s;
+  ++c->run_gen;  // invalidates a captured batch graph
   s = stage_chunk(c, g, &pl, ch, o);
   if (s) return s;
+  SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
   s = launch_nlc_filter(g, ch.fq, 1, c->stream, c->num_sms);
   if (s) return s;
   if (vmask0)

@@ -84,6 +84,12 @@ struct smg_ctx {
   smg::Arena arena;
   std::unique_ptr<smg::FilterDev> fdev;
   smg::TuneSetting tuning[SMG_TUNE_CLASSES];
+  // CUDA graph of the last single-chunk batch, valid while no other run has
+  // touched the arena since (run_gen == graph_gen)
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<const void *> graph_key;
+  uint64_t run_gen = 0, graph_gen = ~0ull;
+  uint64_t graph_launches = 0;
 };
 
 struct smg_graph {
@@ -92,6 +98,8 @@ struct smg_graph {
 };
 
 namespace smg {
+// Forgets the captured batch graph of a context.
+void drop_graph(smg_ctx *c);
 // Device buffers holding one query's filter state and results.
 struct QueryBuffers {
   uint32_t *vmask = nullptr, *enc = nullptr, *cand = nullptr, *roots = nullptr;

@@ -25,7 +25,7 @@ STATUS = {0: "SMG_OK", 1: "SMG_ERR_INVALID", 2: "SMG_ERR_IO", 3: "SMG_ERR_FORMAT
           13: "SMG_ERR_INTERNAL"}
 SHAPES = {"tree": 0, "sparse": 1, "dense": 2, "induced": 3}
 LABELS_UNIFORM, LABELS_ZIPF1 = 0, 1
-FLAG_EMIT, FLAG_PROFILE = 1, 2
+FLAG_EMIT, FLAG_PROFILE, FLAG_NO_GRAPH = 1, 2, 4
 
 
 class SmgError(RuntimeError):
@@ -414,14 +414,15 @@ def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=F
     return res, buf
 
 
-def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk=0, profile=False, max_count=0):
+def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk=0, profile=False, max_count=0,
+                use_graph=True):
     """Batched path.  Returns (counts, BatchStats); with max_count, queries over
     the limit report 2**64-1."""
     n = len(plans)
     arr = (C.c_void_p * n)(*[p.handle.value for p in plans])
     counts = np.zeros(n, dtype=np.uint64)
     opts = MatchOpts()
-    opts.flags = FLAG_PROFILE if profile else 0
+    opts.flags = (FLAG_PROFILE if profile else 0) | (0 if use_graph else FLAG_NO_GRAPH)
     opts.bfs_depth = bfs_depth
     opts.root_chunk = root_chunk
     opts.max_count = max_count

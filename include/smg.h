@@ -215,6 +215,8 @@ smg_status smg_graph_get_stats(const smg_graph *g, smg_graph_stats *out);
 /* ------------------------------------------------------------------ match */
 #define SMG_FLAG_EMIT 1u      /* write embeddings to opts->embeddings        */
 #define SMG_FLAG_PROFILE 2u   /* record per-phase device times (adds syncs)  */
+#define SMG_FLAG_NO_GRAPH 4u  /* batched path: launch directly instead of
+                                 capturing the launches in a CUDA graph    */
 
 typedef struct smg_match_opts {
   uint32_t flags;
@@ -250,7 +252,10 @@ smg_status smg_match(smg_ctx *ctx, const smg_graph *g, const smg_plan *p,
                      const smg_match_opts *opts, smg_match_result *out);
 
 /* Batched path: all queries in one persistent launch fed by a device work
- * queue; counts[i] receives the exact count of plans[i]. */
+ * queue; counts[i] receives the exact count of plans[i].  The launches of a
+ * batch are captured in a CUDA graph; calling again with the same plans (same
+ * handles, same order) on the same context replays the graph without
+ * re-staging the query records, unless another call ran in between. */
 typedef struct smg_batch_stats {
   float filter_ms;           /* device time of the filters (PROFILE)       */
   float join_ms;             /* device time of the joins (PROFILE)         */

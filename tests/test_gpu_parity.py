@@ -158,3 +158,16 @@ def test_graph_with_isolated_vertices(ctx):
     res, emb = native.match(ctx, dev, Plan(Query([0, 0], [0, 1])), emit=4)
     assert res.count == 2
     assert sorted(tuple(r) for r in emb.tolist()) == [(0, 1), (1, 0)]
+
+
+def test_batch_graph_replay(ctx, er):
+    host, dev = er
+    plans = [Plan(q) for q in small_queries(host, ks=(4, 6), seeds=range(3))]
+    first, _ = native.match_batch(ctx, dev, plans)             # captured
+    again, _ = native.match_batch(ctx, dev, plans)             # replayed
+    profiled, st = native.match_batch(ctx, dev, plans, profile=True)
+    native.match(ctx, dev, plans[0])                           # invalidates the graph
+    after, _ = native.match_batch(ctx, dev, plans)             # re-staged and recaptured
+    direct, _ = native.match_batch(ctx, dev, plans, use_graph=False)
+    assert first.tolist() == again.tolist() == profiled.tolist() == after.tolist() == direct.tolist()
+    assert st.join_ms > 0 and st.kernel_launches > 0
