@@ -3,6 +3,12 @@ oracle checker library.  Compiles translation units in parallel, links with
 nvcc, and skips units whose object is newer than every input.
 
     python -m clustersm_gb300.build            # library, CLI, oracle
+    SMG_CHECKED=1 python -m clustersm_gb300.build   # self-checking library
+
+The self-checking library (lib_checked/libsmg.so, load it with SMG_LIB_PATH)
+bounds-checks the kernels' indexed accesses, records the first violation
+(site code and two values, readable with smg_debug_check_join/_filter) and
+skips the access instead of making it.
 """
 from __future__ import annotations
 
@@ -17,7 +23,8 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
-LIBDIR = PKG / "lib"
+CHECKED = os.environ.get("SMG_CHECKED") == "1"
+LIBDIR = PKG / ("lib_checked" if CHECKED else "lib")
 BINDIR = PKG / "bin"
 OBJDIR = LIBDIR / "obj"
 ORACLE_DIR = ROOT / "oracle"
@@ -71,7 +78,7 @@ def build(verbose: bool = False, jobs: int | None = None, ptxas_verbose: bool = 
     BINDIR.mkdir(parents=True, exist_ok=True)
     ORACLE_LIB.mkdir(parents=True, exist_ok=True)
     units = [(CSRC / s, OBJDIR / (s + ".o")) for s in HOST_SRCS + CUDA_SRCS if (CSRC / s).exists()]
-    extra_cu = ["-Xptxas", "-v"] if ptxas_verbose else []
+    extra_cu = (["-Xptxas", "-v"] if ptxas_verbose else []) + (["-DSMG_CHECKED"] if CHECKED else [])
     logs = []
     with cf.ThreadPoolExecutor(jobs) as ex:
         futs = [ex.submit(_compile, s, o, extra_cu if s.suffix == ".cu" else ()) for s, o in units]
@@ -85,7 +92,7 @@ def build(verbose: bool = False, jobs: int | None = None, ptxas_verbose: bool = 
               "-lgomp", "-lcudart"])
     cli_src = CSRC / "cli_main.cpp"
     cli = BINDIR / "ClusterSM"
-    if cli_src.exists() and _stale(cli, [cli_src, lib, *HEADERS]):
+    if not CHECKED and cli_src.exists() and _stale(cli, [cli_src, lib, *HEADERS]):
         _run(["g++", "-O2", "-std=c++17", "-I", str(INCLUDE), str(cli_src), "-o", str(cli),
               "-L", str(LIBDIR), "-lsmg", "-Wl,-rpath,$ORIGIN/../lib"])
     if verbose:

@@ -301,6 +301,7 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
   f.cand = b.cand;
   f.cand_cnt = b.counters->cand_cnt;
   f.roots = b.roots;
+  f.root_cap = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
   f.num_roots = &b.counters->num_roots;
   f.stat = b.counters->stat;
   std::memset(&j, 0, sizeof(j));
@@ -469,6 +470,9 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
   jl.hub_of = g.hub_of;
   jl.hub_bits = g.hub_bits;
   jl.hub_words = g.hub_words;
+  jl.n = g.n;
+  jl.m2 = g.m2;
+  jl.num_hubs = g.num_hubs;
   jl.queries = ch.jq;
   jl.nq = nq;
   jl.kmax = ch.kmax;
@@ -585,8 +589,8 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   st->join_bytes += 8ull * hq->scanned + 8ull * hq->descents + 4ull * hq->probes;
   if (o.profile) {
     float f = 0, j = 0;
-    cudaEventElapsedTime(&f, c->ev[0], c->ev[1]);
-    cudaEventElapsedTime(&j, c->ev[1], c->ev[2]);
+    SMG_CUDA(cudaEventElapsedTime(&f, c->ev[0], c->ev[1]));
+    SMG_CUDA(cudaEventElapsedTime(&j, c->ev[1], c->ev[2]));
     st->filter_ms += f;
     st->join_ms += j;
   }
@@ -630,11 +634,12 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     if (c->arena.cap != cap_before) drop_graph(c);  // arena moved: captured pointers are stale
     std::vector<const void *> key;
     const bool whole = a == 0 && b == nq;
-    if (o.use_graph && whole) {
+    // a profiled run times its phases with events on the stream and is not
+    // captured: events recorded into a graph give no elapsed time
+    if (o.use_graph && whole && !o.profile) {
       key.push_back(&g);
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.root_chunk)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.count_limit)));
-      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.profile)));
       for (uint32_t i = 0; i < nq; ++i) key.push_back(plans[i]);
     }
     s = run_chunk(c, g, plans, ch, o, out, st, key.empty() ? nullptr : &key);
@@ -776,6 +781,7 @@ smg_status smg_set_tuning(smg_ctx *c, const smg_tune_entry *e, uint32_t n) {
     t.donate_min = e[i].donate_min;
     t.valid = e[i].samples > 0;
   }
+  ++c->run_gen;  // the settings are staged into the query records: a captured batch is stale
   return SMG_OK;
 }
 

@@ -16,6 +16,16 @@ constexpr uint32_t kMaxK = SMG_MAX_QUERY_VERTICES;  // query vertices (u-bitmask
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kWarp = 32;
 
+// Bounds checks of the self-checking build (-DSMG_CHECKED): a failed check
+// records (site, value, limit) in a per-translation-unit device word (first
+// failure wins) and the caller skips the access.  In normal builds every
+// check is `true` and compiles away.
+#ifdef SMG_CHECKED
+#define SMG_DCHECK(cond, site, a, b) ::smg::dcheck((cond), (site), (a), (b))
+#else
+#define SMG_DCHECK(cond, site, a, b) true
+#endif
+
 // CUDA status -> smg_status with a message naming the call site.
 smg_status cuda_fail(cudaError_t e, const char *what);
 #define SMG_CUDA(call)                                                  \
@@ -104,6 +114,7 @@ struct FilterQuery {
   uint32_t root;
   uint64_t cand_off[kMaxK + 1];
   uint32_t *vmask, *enc, *cand, *cand_cnt, *roots, *num_roots;
+  uint64_t root_cap;             // entries `roots` can hold
   unsigned long long *stat;       // [0] sum over u of final |C(u)|, [1] walk list entries
 };
 
@@ -126,5 +137,18 @@ struct JoinQuery {
   uint32_t root_chunk;        // root candidates per seeded task (0: from max_seed_tasks)
   uint32_t donate_min;        // shortest list worth splitting off (0: launch default)
 };
+
+#if defined(SMG_CHECKED) && defined(__CUDACC__)
+// Defined once per translation unit that includes this header.
+static __device__ unsigned long long g_check_record[4];
+__device__ __forceinline__ bool dcheck(bool ok, int site, unsigned long long a, unsigned long long b) {
+  if (ok) return true;
+  if (atomicCAS(&g_check_record[0], 0ull, static_cast<unsigned long long>(site)) == 0ull) {
+    g_check_record[1] = a;
+    g_check_record[2] = b;
+  }
+  return false;
+}
+#endif
 
 }  // namespace smg

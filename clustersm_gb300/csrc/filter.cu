@@ -117,7 +117,10 @@ __global__ void __launch_bounds__(256) k_nlc_filter(uint32_t n, const uint32_t *
       uint32_t pos = 0;
       if (lane == 0) pos = atomicAdd(Q.cand_cnt + u, __popc(bal));
       pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
-      if ((mask >> u) & 1u) Q.cand[Q.cand_off[u] + pos + __popc(bal & ((1u << lane) - 1))] = v;
+      if ((mask >> u) & 1u) {
+        const uint64_t at = Q.cand_off[u] + pos + __popc(bal & ((1u << lane) - 1));
+        if (SMG_DCHECK(at < Q.cand_off[u + 1], 201, at, u)) Q.cand[at] = v;
+      }
     }
   }
 }
@@ -147,12 +150,13 @@ __device__ __forceinline__ void walk_neighbors(const uint32_t *__restrict__ adj,
                                                const ClusterStep *__restrict__ steps,
                                                const uint32_t *__restrict__ aux, const FilterQuery &Q,
                                                uint32_t kind, uint32_t pass, uint32_t e0, uint32_t e1,
-                                               uint32_t lane) {
+                                               uint32_t lane, uint32_t n) {
   const uint32_t W = Q.words;
   uint32_t *const enc = Q.enc;
   const uint32_t *const vmask = Q.vmask;
   for (uint32_t e = e0 + lane; e < e1; e += 32) {
     const uint32_t w = adj[e];
+    if (!SMG_DCHECK(w < n, 207, w, e)) continue;
     if (kind != 2) {
       const uint32_t xm = vmask[w];
       if (!xm) continue;
@@ -188,13 +192,15 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
   const uint32_t W = Q.words;
   uint32_t *const enc = Q.enc;
   uint32_t *const list = Q.cand + Q.cand_off[G.core];
-  const uint32_t cnt = *(volatile const uint32_t *)(Q.cand_cnt + G.core);
+  uint32_t cnt = *(volatile const uint32_t *)(Q.cand_cnt + G.core);
+  if (!SMG_DCHECK(Q.cand_off[G.core] + cnt <= Q.cand_off[G.core + 1], 202, cnt, G.core)) cnt = 0;
   const uint32_t kind = steps[G.first].kind;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   unsigned long long scanned = 0;
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < cnt; i += warps) {
     const uint32_t v = list[i];
     if (v == kNone) continue;  // removed by an earlier merge
+    if (!SMG_DCHECK(v < ov.n, 203, v, i)) continue;
     uint32_t pass = 0;         // steps of the group that v passed
     if (kind == 0) {
       const ClusterStep &st = steps[G.first];
@@ -226,6 +232,7 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
     }
     if (kind != 2 && pass == 0) continue;
     const uint32_t e0 = off[v], e1 = off[v + 1];
+    if (!SMG_DCHECK(e0 <= e1 && e1 <= ov.m2, 204, e0, e1)) continue;
     scanned += e1 - e0;
     uint32_t mine = e1;
     if (e1 - e0 > kWalkChunk) {
@@ -246,11 +253,11 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
       base = __shfl_sync(0xFFFFFFFFu, base, 0);
       if (base != kNone) {
         for (uint32_t c = lane; c < extra; c += 32)
-          ov.items[base + c] = make_uint4(gi, v, pass, e0 + (c + 1) * kWalkChunk);
+          if (SMG_DCHECK(base + c < ov.cap, 205, base + c, ov.cap)) ov.items[base + c] = make_uint4(gi, v, pass, e0 + (c + 1) * kWalkChunk);
         mine = e0 + kWalkChunk;
       }
     }
-    walk_neighbors(adj, G, steps, aux, Q, kind, pass, e0, mine, lane);
+    walk_neighbors(adj, G, steps, aux, Q, kind, pass, e0, mine, lane, ov.n);
   }
   if (lane == 0 && scanned) atomicAdd(Q.stat + 1, scanned);
 }
@@ -267,11 +274,12 @@ __global__ void __launch_bounds__(256) k_walk_chunks(const uint32_t *__restrict_
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
     const uint4 it = ov.items[i];
+    if (!SMG_DCHECK(it.x < ov.num_groups && it.y < ov.n && it.w < ov.m2, 206, i, it.x)) continue;
     const StepGroup G = groups[it.x];
     const FilterQuery &Q = qs[G.query];
     const uint32_t kind = steps[G.first].kind;
     const uint32_t e1 = min(it.w + kWalkChunk, off[it.y + 1]);
-    walk_neighbors(adj, G, steps, aux, Q, kind, it.z, it.w, e1, lane);
+    walk_neighbors(adj, G, steps, aux, Q, kind, it.z, it.w, e1, lane, ov.n);
   }
 }
 
@@ -309,7 +317,10 @@ __global__ void __launch_bounds__(256) k_collect(uint32_t n, const FilterQuery *
       uint32_t pos = 0;
       if (lane == 0) pos = atomicAdd(Q.num_roots, __popc(bal));
       pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
-      if (is_root) Q.roots[pos + __popc(bal & ((1u << lane) - 1))] = v;
+      if (is_root) {
+        const uint64_t at = pos + __popc(bal & ((1u << lane) - 1));
+        if (SMG_DCHECK(at < Q.root_cap, 208, at, Q.root_cap)) Q.roots[at] = v;
+      }
     }
   }
   for (int o = 16; o; o >>= 1) ncand += __shfl_down_sync(0xFFFFFFFFu, ncand, o);
@@ -379,6 +390,12 @@ void word_groups(const Plan &P, uint32_t c, ClusterStep &st) {
 }
 
 }  // namespace
+
+#ifdef SMG_CHECKED
+extern "C" int smg_debug_check_filter(unsigned long long *out) {
+  return static_cast<int>(cudaMemcpyFromSymbol(out, g_check_record, 3 * sizeof(unsigned long long)));
+}
+#endif
 
 smg_status append_filter_steps(const Plan &P, uint32_t qi, FilterBatch &fb) {
   const uint32_t phases = 2 * P.num_layers - 1;
@@ -523,6 +540,9 @@ smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const Filter
     if (!ng) continue;
     WalkOverflow po = ov;
     po.count = ov.count + 2 * p;  // one zeroed counter per phase
+    po.n = g.n;
+    po.m2 = g.m2;
+    po.num_groups = fd.phase_count[p];
     const uint32_t wx = std::max<uint32_t>(1, std::min<uint32_t>(2048, (num_sms * 16u + ng - 1) / ng));
     for (uint32_t y0 = 0; y0 < ng; y0 += 65535) {
       const uint32_t ny = std::min<uint32_t>(65535, ng - y0);

@@ -20,6 +20,8 @@ struct WalkOverflow {
   unsigned int *count;
   uint32_t cap;
   uint4 *items;
+  uint32_t n, num_groups;  // data vertices and the phase's step groups (bounds checks)
+  uint64_t m2;             // adjacency entries
 };
 
 // Steps of the cluster bitmap for a batch of queries, grouped into phases:

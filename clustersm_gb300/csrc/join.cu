@@ -31,7 +31,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <numeric>
+#include <string>
 
 #include "join.cuh"
 
@@ -108,6 +110,7 @@ __global__ void k_seed(JoinLaunch p) {
     atomicAdd(p.queries[q].pending, static_cast<unsigned long long>(nt));
     const unsigned long long first = atomicAdd(&p.qs->tail.v, static_cast<unsigned long long>(nt));
     const uint32_t tw = 4 + p.kmax;
+    if (!SMG_DCHECK(first + nt <= p.cap, 101, first + nt, p.cap)) continue;
     for (uint32_t i = 0; i < nt; ++i) {
       uint32_t *t = p.tasks + (first + i) * tw;
       t[0] = q;
@@ -135,10 +138,11 @@ __global__ void k_hub_bits(const uint32_t *__restrict__ off, const uint32_t *__r
 // its bitmap when it has one.
 __device__ __forceinline__ bool is_neighbor(const JoinLaunch &p, uint32_t beg, uint32_t deg, uint32_t hub,
                                             uint32_t w, uint32_t &probes) {
-  if (hub != kNone) {
+  if (hub != kNone && SMG_DCHECK(hub < p.num_hubs, 102, hub, p.num_hubs) && SMG_DCHECK(w < p.n, 103, w, p.n)) {
     ++probes;
     return (__ldg(p.hub_bits + hub * p.hub_words + (w >> 5)) >> (w & 31)) & 1u;
   }
+  if (!SMG_DCHECK(static_cast<uint64_t>(beg) + deg <= p.m2, 104, beg, deg)) return false;
   const uint32_t *a = p.adj + beg;
   uint32_t lo = 0, hi = deg;
   while (lo < hi) {
@@ -210,6 +214,7 @@ __device__ __forceinline__ uint32_t choose_pivot(const WarpView &S, uint32_t lev
 // Candidate test for list entry w at `level` (>= 1, not the last level).
 __device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const uint32_t *__restrict__ candmask,
                                        uint32_t level, uint32_t w, uint32_t &probes) {
+  if (!SMG_DCHECK(w < p.n, 105, w, level)) return false;
   if (!((__ldg(candmask + w) >> S.ord[level]) & 1u)) return false;
   for (uint32_t b = S.slab[level]; b; b &= b - 1)
     if (S.m[__ffs(b) - 1] == w) return false;
@@ -231,7 +236,8 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   const uint32_t lt = (1u << lane) - 1;
   uint32_t len = 0;
   if (lane < bc) {
-    const uint32_t v = S.batch[P * 32 + lane];
+    uint32_t v = S.batch[P * 32 + lane];
+    if (!SMG_DCHECK(v < p.n, 106, v, P)) v = 0;
     const uint32_t vb = __ldg(p.off + v), vd = __ldg(p.off + v + 1) - vb;
     uint32_t piv = 0, bd = 0xFFFFFFFFu;
     for (uint32_t b = S.bmask[L]; b; b &= b - 1) {
@@ -277,8 +283,10 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       }
       i = lo;
       const uint32_t vi = S.sv[i];
-      w = __ldg(p.adj + S.sbase[i] + (t - S.spre[i]));
-      good = (__ldg(candmask + w) >> u) & 1u;
+      const uint64_t ai = static_cast<uint64_t>(S.sbase[i]) + (t - S.spre[i]);
+      const bool in_adj = SMG_DCHECK(ai < p.m2, 107, ai, i);
+      w = in_adj ? __ldg(p.adj + ai) : 0u;
+      good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) && ((__ldg(candmask + w) >> u) & 1u);
       for (uint32_t b = same; b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
         good = (j == P ? vi : S.m[j]) != w;
@@ -435,7 +443,7 @@ __device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned l
   return ok != 0;
 }
 
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
+__device__ __forceinline__ void join_body(const JoinLaunch &p) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint32_t K = p.kmax, tw = 4 + K;
@@ -460,11 +468,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     got = __shfl_sync(0xFFFFFFFFu, got, 0);
     if (got != 1) break;
     slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-
+    // Lane 0 acquired the task's ready flag; the barrier orders that before
+    // every lane's reads, and the reads go to L2 (__ldcg): a donated task was
+    // written during this launch by another SM, and this SM's L1 may hold an
+    // older copy of the line from a neighbouring slot.
+    __syncwarp();
     const uint32_t *T = p.tasks + static_cast<uint64_t>(slot) * tw;
-    const uint32_t q = T[0], L0 = T[1], lo = T[2], hi = T[3];
+    const uint32_t q = __ldcg(T), L0 = __ldcg(T + 1), lo = __ldcg(T + 2), hi = __ldcg(T + 3);
+    if (!SMG_DCHECK(q < p.nq, 109, q, p.nq)) break;
     const JoinQuery &Q = p.queries[q];
     const uint32_t k = Q.k, P = k - 2;
+    if (!SMG_DCHECK(L0 <= P, 110, L0, k)) break;
     if (Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over)) {
       if (lane == 0) {
         atomicAdd(&qs->tasks_done, 1ull);
@@ -480,7 +494,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
       S.slab[lane] = Q.same_label[lane];
     }
     if (lane < L0) {
-      const uint32_t v = T[4 + lane];
+      uint32_t v = __ldcg(T + 4 + lane);
+      if (!SMG_DCHECK(v < p.n, 111, v, lane)) v = 0;
       S.m[lane] = v;
       const uint32_t b = __ldg(p.off + v);
       S.beg[lane] = b;
@@ -574,7 +589,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
         const uint32_t bi = S.bidx[level], bc = S.bcnt[level];
         if (bi < bc) {
           // descend into the next tested candidate
-          const uint32_t v = S.batch[level * 32 + bi];
+          uint32_t v = S.batch[level * 32 + bi];
+          if (!SMG_DCHECK(v < p.n, 113, v, level)) v = 0;
           __syncwarp();
           if (lane == 0) {
             S.bidx[level] = bi + 1;
@@ -612,7 +628,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
         uint32_t w = 0;
         if (lane < n) {
           w = __ldg(base + c + lane);
-          good = level == 0 || accept(S, p, candmask, level, w, probes);
+          good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, candmask, level, w, probes));
         }
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
         if (good) S.batch[level * 32 + __popc(bal & lt)] = w;
@@ -651,6 +667,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) {
     if (aborted || preempted) break;
   }
 }
+
+// The join at the compiler's register choice (fewer, fatter warps) and
+// bounded to 6 resident blocks per SM (more warps to hide latency, a small
+// spill).  SMG_JOIN_OCCUPANCY=high selects the second.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) { join_body(p); }
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_join_hi(JoinLaunch p) { join_body(p); }
 
 __global__ void k_slice_begin(QueueState *qs) {
   qs->start_ns = now_ns();
@@ -722,37 +744,52 @@ smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, 
   return SMG_OK;
 }
 
+#ifdef SMG_CHECKED
+extern "C" int smg_debug_check_join(unsigned long long *out) {
+  return static_cast<int>(cudaMemcpyFromSymbol(out, g_check_record, 3 * sizeof(unsigned long long)));
+}
+#endif
+
 size_t join_queue_bytes(uint32_t cap, uint32_t kmax) {
   return static_cast<size_t>(cap) * (4 + kmax) * sizeof(uint32_t) + static_cast<size_t>(cap) * sizeof(uint32_t);
 }
 
-smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
-  if (jl.nq == 0) return SMG_OK;
+namespace {
+
+bool high_occupancy() {
+  static const bool hi = [] {
+    const char *e = std::getenv("SMG_JOIN_OCCUPANCY");
+    return e && std::string(e) == "high";
+  }();
+  return hi;
+}
+
+smg_status launch_persistent(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
+  void (*kern)(JoinLaunch) = high_occupancy() ? k_join_hi : k_join;
   if (smem > 48 * 1024)
-    SMG_CUDA(cudaFuncSetAttribute(k_join, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    SMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
-  SMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join, kWarpsPerBlock * 32, smem));
+  SMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpsPerBlock * 32, smem));
   per_sm = std::max(1, per_sm);
-  const uint32_t seed_threads = 128;
-  const uint32_t nseed = jl.seed_list ? jl.seed_n : jl.nq;
-  k_seed<<<(nseed + seed_threads - 1) / seed_threads, seed_threads, 0, s>>>(jl);
-  SMG_CUDA(cudaGetLastError());
-  k_join<<<num_sms * per_sm, kWarpsPerBlock * 32, smem, s>>>(jl);
+  kern<<<num_sms * per_sm, kWarpsPerBlock * 32, smem, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }
 
-smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
-  const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
-  if (smem > 48 * 1024)
-    SMG_CUDA(cudaFuncSetAttribute(k_join, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  int per_sm = 0;
-  SMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join, kWarpsPerBlock * 32, smem));
-  per_sm = std::max(1, per_sm);
-  k_join<<<num_sms * per_sm, kWarpsPerBlock * 32, smem, s>>>(jl);
+}  // namespace
+
+smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
+  if (jl.nq == 0) return SMG_OK;
+  const uint32_t seed_threads = 128;
+  const uint32_t nseed = jl.seed_list ? jl.seed_n : jl.nq;
+  k_seed<<<(nseed + seed_threads - 1) / seed_threads, seed_threads, 0, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
-  return SMG_OK;
+  return launch_persistent(jl, s, num_sms);
+}
+
+smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
+  return launch_persistent(jl, s, num_sms);
 }
 
 smg_status launch_seed(const JoinLaunch &jl, cudaStream_t s) {

@@ -34,6 +34,9 @@ struct JoinLaunch {
   const uint32_t *hub_of;    // [n] hub index or kNone
   const uint32_t *hub_bits;  // [hubs][hub_words] neighbour bitmaps of hubs
   uint64_t hub_words;
+  uint32_t n;                // data vertices (bounds of the self-checking build)
+  uint64_t m2;               // adjacency entries
+  uint32_t num_hubs;
   const JoinQuery *queries;  // device array
   uint32_t nq, kmax;
   QueueState *qs;            // device

@@ -158,6 +158,9 @@ smg::JoinLaunch join_launch(smg_server *s) {
   jl.hub_of = g.hub_of;
   jl.hub_bits = g.hub_bits;
   jl.hub_words = g.hub_words;
+  jl.n = g.n;
+  jl.m2 = g.m2;
+  jl.num_hubs = g.num_hubs;
   jl.queries = s->d_jq;
   jl.nq = s->cfg.max_inflight;
   jl.kmax = kServerK;

@@ -13,15 +13,18 @@ graphs with Zipf labels, walk-extracted queries have embedding counts far
 beyond exact enumeration: on R-MAT 2^22 / 32 labels only 13 of 187 drawn
 queries (4..16 vertices) had at most 10^8 embeddings, and none of those had
 more than 5 vertices.  A drawn query is therefore kept when its exact count is at
-most COUNT_LIMIT, decided on the GPU with the library's per-query count limit
+most the workload's count limit, decided on the GPU with the library's per-query count limit
 (the join stops a query as soon as its running count passes the limit) and a
 device deadline; each slot retries new seeds up to MAX_DRAWS times (drawn
-and screened in rounds, one batched call per round).
+and screened in rounds, one batched call per round).  The limit is 10^8 for the 2^20-vertex and
+smaller graphs and 10^7 for the 1,024-query 2^22-vertex batch, which keeps
+one batched pass over all 1,024 queries within seconds.
 Every kept count is then recomputed by the CPU oracle; a fixture is written
 only when all counts agree.
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
 import json
 import os
 import random
@@ -35,18 +38,17 @@ sys.path.insert(0, str(ROOT))
 from clustersm_gb300.workloads import load  # noqa: E402
 from clustersm_gb300.native import Query, SmgError  # noqa: E402
 
-COUNT_LIMIT = 10**8
 MAX_DRAWS = 64
 SPECS = {
-    # name: (slots, vertex counts, shapes)
-    "er1k": (96, [4], ["induced"]),
-    "rmat20": (96, [4, 5], ["tree", "sparse", "dense"]),
-    "rmat22": (1024, [4, 5], ["tree", "sparse", "dense"]),
+    # name: (slots, vertex counts, shapes, count limit)
+    "er1k": (96, [4], ["induced"], 10**8),
+    "rmat20": (96, [4, 5], ["tree", "sparse", "dense"], 10**8),
+    "rmat22": (1024, [4, 5], ["tree", "sparse", "dense"], 10**7),
 }
 
 
 def draws(name):
-    nq, ks, shapes = SPECS[name]
+    nq, ks, shapes, _ = SPECS[name]
     rng = random.Random(f"{name}-slots")
     for slot in range(nq):
         k = rng.choice(ks)
@@ -70,7 +72,7 @@ def gen_gpu(name, seconds=None):
     from clustersm_gb300.native import Context, DeviceGraph, Plan
     os.environ["SMG_TIME_LIMIT_S"] = "20"
     wl = load(name)
-    nq, ks, shapes = SPECS[name]
+    nq, ks, shapes, limit = SPECS[name]
     t0 = time.time()
     host = wl.graph()
     ctx = Context(0)
@@ -84,7 +86,7 @@ def gen_gpu(name, seconds=None):
 
     def save(complete):
         out = [kept[s] for s in sorted(kept)]
-        path.write_text(json.dumps({"workload": name, "count_limit": COUNT_LIMIT, "max_draws": MAX_DRAWS,
+        path.write_text(json.dumps({"workload": name, "count_limit": limit, "max_draws": MAX_DRAWS,
                                     "slots": nq, "kept": len(out), "draws_total": tried, "timeouts": timeouts,
                                     "seconds": round(time.time() - t0, 1), "complete": complete,
                                     "queries": out}, separators=(",", ":")))
@@ -92,27 +94,30 @@ def gen_gpu(name, seconds=None):
     for attempt in range(MAX_DRAWS):
         if seconds and time.time() - t0 > seconds:
             break
-        batch = []
-        for slot in range(nq):
-            if slot in kept:
-                continue
-            k, shape, seed = slot_k[slot], shapes[slot % len(shapes)], (slot << 20) | attempt
+        todo = [(slot, slot_k[slot], shapes[slot % len(shapes)], (slot << 20) | attempt)
+                for slot in range(nq) if slot not in kept]
+
+        def draw(item):
             try:
-                batch.append((slot, k, shape, seed, Query.generate(host, k, shape, seed=seed)))
+                return item + (Query.generate(host, item[1], item[2], seed=item[3]),)
             except SmgError:
-                pass
+                return None
+
+        # the generator runs in C with the interpreter lock released
+        with cf.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+            batch = [b for b in ex.map(draw, todo) if b is not None]
         if not batch:
             break
         tried += len(batch)
         plans = [Plan(b[4]) for b in batch]
         try:
-            counts, _ = native.match_batch(ctx, dev, plans, max_count=COUNT_LIMIT)
+            counts, _ = native.match_batch(ctx, dev, plans, max_count=limit)
             results = [None if c == 2**64 - 1 else int(c) for c in counts.tolist()]
         except SmgError:
             results = []
             for p in plans:
                 try:
-                    r, _ = native.match(ctx, dev, p, max_count=COUNT_LIMIT)
+                    r, _ = native.match(ctx, dev, p, max_count=limit)
                     results.append(None if r.limit_hit else int(r.count))
                 except SmgError:
                     timeouts += 1
@@ -164,12 +169,12 @@ def gen_cpu(name):
             continue
         tried += 1
         c, used = oracle.count_budget(host, q, 10**9)
-        if used is None or c > COUNT_LIMIT:
+        if used is None or c > SPECS[name][3]:
             continue
         out.append(record(slot, attempt, k, shape, seed, q, c, "count"))
         done_slot = slot
     dst = ROOT / wl.queries_file
-    dst.write_text(json.dumps({"workload": name, "count_limit": COUNT_LIMIT, "max_draws": MAX_DRAWS,
+    dst.write_text(json.dumps({"workload": name, "count_limit": SPECS[name][3], "max_draws": MAX_DRAWS,
                                "slots": SPECS[name][0], "kept": len(out), "draws_total": tried,
                                "verified_by": "oracle_count (CPU backtracking)", "queries": out},
                               separators=(",", ":")))
