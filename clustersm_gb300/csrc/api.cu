@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -555,7 +556,11 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
     const char *why = hq->error == JOIN_ERR_DEADLINE ? "join exceeded its time limit (SMG_TIME_LIMIT_S)"
                       : hq->error == JOIN_ERR_IDLE_TIMEOUT ? "join made no progress for too long"
                                                             : "a queued task was never published";
-    return fail(SMG_ERR_TIMEOUT, why);
+    char msg[320];
+    std::snprintf(msg, sizeof(msg), "%s; queue: head %llu tail %llu pending %llu tasks done %llu donations %llu "
+                  "progress %llu full %d", why, hq->head.v, hq->tail.v, hq->pending.v, hq->tasks_done,
+                  hq->donations, hq->progress.v, hq->full);
+    return fail(SMG_ERR_TIMEOUT, msg);
   }
   if (hq->pending.v != 0) return fail(SMG_ERR_INTERNAL, "join ended with pending tasks");
   for (uint32_t i = 0; i < nq; ++i) {

@@ -479,7 +479,10 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     const JoinQuery &Q = p.queries[q];
     const uint32_t k = Q.k, P = k - 2;
     if (!SMG_DCHECK(L0 <= P, 110, L0, k)) break;
-    if (Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over)) {
+    int drop = 0;
+    if (lane == 0) drop = Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over);
+    drop = __shfl_sync(0xFFFFFFFFu, drop, 0);
+    if (drop) {  // the query is over its count limit
       if (lane == 0) {
         atomicAdd(&qs->tasks_done, 1ull);
         atomicAdd(&qs->progress.v, 1ull);
@@ -626,7 +629,9 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         const uint32_t *base = S.lbase[level];
         bool good = false;
         uint32_t w = 0;
-        if (lane < n) {
+        if (lane < n && SMG_DCHECK(level == 0 ? c + lane < *Q.num_roots
+                                                : static_cast<uint64_t>(base - p.adj) + c + lane < p.m2,
+                                   114, c + lane, level)) {
           w = __ldg(base + c + lane);
           good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, candmask, level, w, probes));
         }

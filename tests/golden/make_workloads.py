@@ -66,11 +66,11 @@ def gen_gpu(name, seconds=None):
     """Screen drawn queries on the GPU in rounds: each round draws the next
     seed of every unfilled slot and matches them all in one batched call with
     the per-query count limit; queries that finish under the limit fill their
-    slots.  A round that hits the device deadline is re-screened one query at
-    a time."""
+    slots.  A round that hits the device deadline (SMG_TIME_LIMIT_S, 120 s
+    unless set) is re-screened one query at a time."""
     from clustersm_gb300 import native
     from clustersm_gb300.native import Context, DeviceGraph, Plan
-    os.environ["SMG_TIME_LIMIT_S"] = "20"
+    os.environ.setdefault("SMG_TIME_LIMIT_S", "120")
     wl = load(name)
     nq, ks, shapes, limit = SPECS[name]
     t0 = time.time()
@@ -113,14 +113,17 @@ def gen_gpu(name, seconds=None):
         try:
             counts, _ = native.match_batch(ctx, dev, plans, max_count=limit)
             results = [None if c == 2**64 - 1 else int(c) for c in counts.tolist()]
-        except SmgError:
+        except SmgError as e:
+            print(f"{name}: round {attempt}: batched screening failed ({e}); screening one by one", flush=True)
             results = []
             for p in plans:
                 try:
                     r, _ = native.match(ctx, dev, p, max_count=limit)
                     results.append(None if r.limit_hit else int(r.count))
-                except SmgError:
+                except SmgError as e1:
                     timeouts += 1
+                    if timeouts <= 5:
+                        print(f"{name}: {e1}", flush=True)
                     results.append(None)
         for (slot, k, shape, seed, q), c in zip(batch, results):
             if c is not None:
