@@ -139,6 +139,7 @@ def _load():
                                  C.POINTER(BatchStats)]),
         "smg_filter_inspect": (st, [vp, vp, vp, u32p, u32p, u32p]),
         "smg_autotune": (st, [vp, vp, C.POINTER(vp), C.c_uint32, C.POINTER(TuneEntry)]),
+        "smg_join_noalloc": (st, [vp, vp, vp, C.c_void_p, C.c_void_p, C.c_uint32, u64p]),
         "smg_set_tuning": (st, [vp, C.POINTER(TuneEntry), C.c_uint32]),
         "smg_plan_class": (C.c_uint32, [vp]),
         "smg_server_create": (st, [vp, vp, C.POINTER(ServerConfig), C.POINTER(vp)]),

@@ -305,6 +305,26 @@ smg_status smg_filter_inspect(smg_ctx *ctx, const smg_graph *g,
                               const smg_plan *p, uint32_t *vmask0,
                               uint32_t *encodings, uint32_t *candmask);
 
+/* ------------------------------------------------- allocation-free join */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * while they match: code running between the capture and the replay of a
+ * larger application's CUDA graphs, callers whose device memory belongs to a
+ * framework allocator, or real-time loops that must not allocate after
+ * start-up.  Counts the embeddings of plan p from caller-owned device inputs:
+ * candmask[num_vertices] (bit u set when data vertex v may take query vertex u,
+ * as smg_filter_inspect's final masks) and roots[num_roots] (the candidates of
+ * the plan's first matched vertex, view.root).  The join's scratch (a queue of
+ * SMG_NOALLOC_MAX_TASKS tasks, its state, the query record and counters, about
+ * 10 MB) is a fixed array in the library's device image; no call allocates.
+ * The first call on a device looks that array up (cudaGetSymbolAddress) and
+ * must come before any stream capture.  All calls on a device share the
+ * array: each call clears it first, and calls that overlap on the GPU race.
+ * Rejects more roots than data vertices (SMG_ERR_LIMIT). */
+#define SMG_NOALLOC_MAX_TASKS 65536u
+smg_status smg_join_noalloc(smg_ctx *ctx, const smg_graph *g, const smg_plan *p,
+                            const uint32_t *candmask, const uint32_t *roots,
+                            uint32_t num_roots, uint64_t *count);
+
 /* ---------------------------------------------------------------- serving */
 typedef struct smg_server smg_server;
 typedef struct smg_server_config {
