@@ -42,7 +42,13 @@ smg_status Arena::reserve(size_t bytes) {
   if (base) cudaFree(base);
   base = nullptr;
   cap = 0;
-  const size_t want = bytes + bytes / 4 + (1 << 20);
+  // grow by a quarter for the next, larger batch, but never into the headroom
+  // that kernel launches (local memory), graphs and the filter's step tables
+  // need
+  size_t free_b = 0, total_b = 0;
+  SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const size_t spare = free_b > kHeadroomBytes ? free_b - kHeadroomBytes : 0;
+  const size_t want = std::max(bytes, std::min(bytes + bytes / 4 + (1 << 20), spare));
   cudaError_t e = cudaMalloc(&base, want);
   if (e != cudaSuccess) {
     e = cudaMalloc(&base, bytes);
@@ -616,7 +622,7 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
   if (o.emb_host && nq != 1) return fail(SMG_ERR_INVALID, "embeddings are returned by the plain path only");
   size_t free_b = 0, total_b = 0;
   SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const size_t budget = c->arena.cap + (free_b > (2ull << 30) ? free_b - (2ull << 30) : free_b / 2);
+  const size_t budget = c->arena.cap + (free_b > kHeadroomBytes ? free_b - kHeadroomBytes : free_b / 2);
   const size_t per_chunk_fixed = (64ull << 20) * 4;  // queue storage of a chunk (bound)
   const size_t max_q = kPinnedBytes / (sizeof(FilterQuery) + sizeof(JoinQuery) + sizeof(QCounters));
   uint32_t a = 0;

@@ -15,6 +15,10 @@ namespace smg {
 constexpr size_t kPinnedBytes = 32u << 20;
 
 // Grow-only device buffer; each run carves its scratch out of it.
+// Device memory a batch leaves free for what is allocated after its arena:
+// kernels' local memory at launch, CUDA graph instantiation, filter tables.
+constexpr size_t kHeadroomBytes = 8ull << 30;
+
 struct Arena {
   char *base = nullptr;
   size_t cap = 0;

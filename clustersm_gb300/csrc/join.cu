@@ -43,6 +43,7 @@ namespace {
 constexpr int kWarpsPerBlock = 8;
 constexpr uint64_t kReadyWaitNs = 2000000000ull;   // 2 s for a producer to publish
 constexpr uint64_t kIdleLimitNs = 30000000000ull;  // 30 s without any progress
+constexpr unsigned long long kLimitFlush = 4096;    // count-limited joins publish at this many
 
 __device__ __forceinline__ uint64_t now_ns() {
   uint64_t t;
@@ -586,6 +587,17 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
           descents += bc;
           if (lane == 0) S.bcnt[level] = 0;
           __syncwarp();
+          if (Q.count_limit && cnt >= kLimitFlush) {
+            // publish early so that a query over its limit stops soon
+            int over = 0;
+            if (lane == 0) {
+              const unsigned long long before = atomicAdd(Q.count, cnt);
+              over = before + cnt > Q.count_limit;
+              if (over) *Q.over = 1;
+            }
+            cnt = 0;
+            if (__shfl_sync(0xFFFFFFFFu, over, 0)) break;
+          }
           continue;
         }
       } else {

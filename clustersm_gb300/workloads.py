@@ -67,9 +67,9 @@ WORKLOADS = {
     "rmat20": Workload("rmat20", "rmat", scale=20, avg_degree=16, labels=16, seed=1,
                        queries_file="tests/golden/workload_rmat20.json",
                        description="R-MAT(0.57,0.19,0.19,0.05) 2^20 vertices, avg degree 16, 16 Zipf labels, "
-                                   "8-vertex tree/sparse/dense walk queries"),
+                                   "80 4-5-vertex tree/sparse/dense walk queries of at most 10^8 embeddings"),
     "rmat22": Workload("rmat22", "rmat", scale=22, avg_degree=16, labels=32, seed=1,
                        queries_file="tests/golden/workload_rmat22.json",
                        description="R-MAT(0.57,0.19,0.19,0.05) 2^22 vertices, avg degree 16, 32 Zipf labels, "
-                                   "mixed tree/sparse/dense walk queries"),
+                                   "1,024 4-5-vertex tree/sparse/dense walk queries of at most 10^7 embeddings"),
 }

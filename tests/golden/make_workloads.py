@@ -12,13 +12,15 @@ Queries are drawn by seeded random-walk extraction (smg_gen_query).  On R-MAT
 graphs with Zipf labels, walk-extracted queries have embedding counts far
 beyond exact enumeration: on R-MAT 2^22 / 32 labels only 13 of 187 drawn
 queries (4..16 vertices) had at most 10^8 embeddings, and none of those had
-more than 5 vertices.  A drawn query is therefore kept when its exact count is at
-most the workload's count limit, decided on the GPU with the library's per-query count limit
-(the join stops a query as soon as its running count passes the limit) and a
-device deadline; each slot retries new seeds up to MAX_DRAWS times (drawn
-and screened in rounds, one batched call per round).  The limit is 10^8 for the 2^20-vertex and
-smaller graphs and 10^7 for the 1,024-query 2^22-vertex batch, which keeps
-one batched pass over all 1,024 queries within seconds.
+more than 5 vertices.  A drawn query is therefore kept when its exact count
+is at most the workload's count limit, decided on the GPU with the library's
+per-query count limit (the join stops a query soon after its running count
+passes the limit) and a device deadline.  Each slot draws new seeds in the
+phases `phases()` lists (drawn and screened in rounds, one batched call per
+round) and keeps its first draw under the limit.  The limit is 10^8 for the
+2^20-vertex and smaller graphs and 10^7 for the 1,024-query 2^22-vertex batch,
+which keeps one batched pass over all 1,024 queries within seconds.
+WORKLOAD_RESUME=<earlier output> continues an interrupted screening.
 Every kept count is then recomputed by the CPU oracle; a fixture is written
 only when all counts agree.
 """
@@ -62,12 +64,36 @@ def record(slot, attempt, k, shape, seed, q, count, key):
             "labels": q.labels.tolist(), "edges": q.edges.tolist(), key: int(count)}
 
 
-def gen_gpu(name, seconds=None):
-    """Screen drawn queries on the GPU in rounds: each round draws the next
-    seed of every unfilled slot and matches them all in one batched call with
-    the per-query count limit; queries that finish under the limit fill their
-    slots.  A round that hits the device deadline (SMG_TIME_LIMIT_S, 120 s
-    unless set) is re-screened one query at a time."""
+def phases(name):
+    """Draw phases of a workload's slots: (draws, k or None for the slot's own,
+    shape or None for the slot's own).  On R-MAT 2^22, 5-vertex trees and most
+    5-vertex sparse queries exceed 10^7 embeddings in every one of 64 draws, so
+    slots still empty after the first phase fall back to 4-vertex queries of
+    their shape, and then to 4-vertex dense ones."""
+    if name == "rmat22":
+        return [(64, None, None), (256, 4, None), (64, 4, "dense")]
+    return [(MAX_DRAWS, None, None)]
+
+
+def slot_attempts(name, slot, k, shape):
+    """(attempt, k, shape, seed) for every draw of a slot, in order."""
+    a = 0
+    for draws, pk, pshape in phases(name):
+        for _ in range(draws):
+            yield a, pk or k, pshape or shape, (slot << 20) | a
+            a += 1
+
+
+def gen_gpu(name, seconds=None, resume=None, per_round=16):
+    """Screen drawn queries on the GPU in rounds.  Each round draws the next
+    `per_round` attempts of every unfilled slot and matches them all in one
+    batched call with the per-query count limit; a slot keeps its lowest
+    attempt that finishes under the limit, which is the query a one-by-one
+    draw would keep.  A round that hits the device deadline (SMG_TIME_LIMIT_S,
+    120 s unless set) is re-screened one query at a time.  `resume` names an
+    earlier output whose kept slots stand and whose `next_attempt` (or, for a
+    complete first-phase run, the first phase's size) says where each unfilled
+    slot continues."""
     from clustersm_gb300 import native
     from clustersm_gb300.native import Context, DeviceGraph, Plan
     os.environ.setdefault("SMG_TIME_LIMIT_S", "120")
@@ -79,42 +105,57 @@ def gen_gpu(name, seconds=None):
     dev = DeviceGraph(ctx, host)
     rng = random.Random(f"{name}-slots")
     slot_k = [rng.choice(ks) for _ in range(nq)]
-    kept = {}
+    plan_of = {s: list(slot_attempts(name, s, slot_k[s], shapes[s % len(shapes)])) for s in range(nq)}
+    kept, nxt = {}, {s: 0 for s in range(nq)}
     tried = timeouts = 0
+    if resume:
+        old = json.loads(Path(resume).read_text())
+        for rec in old["queries"]:
+            kept[rec["slot"]] = rec
+        first = phases(name)[0][0]
+        for s in range(nq):
+            nxt[s] = int(old.get("next_attempt", {}).get(str(s), first if old.get("complete") else 0))
+        tried = old.get("draws_total", 0)
     path = ROOT / "gpurun_out" / f"workload_{name}.json"
     path.parent.mkdir(exist_ok=True)
 
     def save(complete):
         out = [kept[s] for s in sorted(kept)]
-        path.write_text(json.dumps({"workload": name, "count_limit": limit, "max_draws": MAX_DRAWS,
+        path.write_text(json.dumps({"workload": name, "count_limit": limit, "phases": phases(name),
                                     "slots": nq, "kept": len(out), "draws_total": tried, "timeouts": timeouts,
                                     "seconds": round(time.time() - t0, 1), "complete": complete,
+                                    "next_attempt": {str(s): nxt[s] for s in range(nq) if s not in kept},
                                     "queries": out}, separators=(",", ":")))
 
-    for attempt in range(MAX_DRAWS):
+    rnd = 0
+    while True:
         if seconds and time.time() - t0 > seconds:
             break
-        todo = [(slot, slot_k[slot], shapes[slot % len(shapes)], (slot << 20) | attempt)
-                for slot in range(nq) if slot not in kept]
+        todo = []
+        for s in range(nq):
+            if s in kept:
+                continue
+            todo += [(s,) + a for a in plan_of[s][nxt[s]:nxt[s] + per_round]]
+        if not todo:
+            break
 
         def draw(item):
+            s, a, k, shape, seed = item
             try:
-                return item + (Query.generate(host, item[1], item[2], seed=item[3]),)
+                return item + (Query.generate(host, k, shape, seed=seed),)
             except SmgError:
                 return None
 
         # the generator runs in C with the interpreter lock released
         with cf.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
             batch = [b for b in ex.map(draw, todo) if b is not None]
-        if not batch:
-            break
         tried += len(batch)
-        plans = [Plan(b[4]) for b in batch]
+        plans = [Plan(b[5]) for b in batch]
         try:
             counts, _ = native.match_batch(ctx, dev, plans, max_count=limit)
             results = [None if c == 2**64 - 1 else int(c) for c in counts.tolist()]
         except SmgError as e:
-            print(f"{name}: round {attempt}: batched screening failed ({e}); screening one by one", flush=True)
+            print(f"{name}: round {rnd}: batched screening failed ({e}); screening one by one", flush=True)
             results = []
             for p in plans:
                 try:
@@ -125,12 +166,19 @@ def gen_gpu(name, seconds=None):
                     if timeouts <= 5:
                         print(f"{name}: {e1}", flush=True)
                     results.append(None)
-        for (slot, k, shape, seed, q), c in zip(batch, results):
-            if c is not None:
-                kept[slot] = record(slot, attempt, k, shape, seed, q, c, "gpu_count")
+        best = {}
+        for (s, a, k, shape, seed, q), c in zip(batch, results):
+            if c is not None and (s not in best or a < best[s][0]):
+                best[s] = (a, record(s, a, k, shape, seed, q, c, "gpu_count"))
+        for s in {t[0] for t in todo}:
+            if s in best:
+                kept[s] = best[s][1]
+            else:
+                nxt[s] += per_round
         save(False)
-        print(f"{name}: round {attempt}: {len(kept)} kept, {tried} draws, {timeouts} timeouts, "
+        print(f"{name}: round {rnd}: {len(kept)} kept, {len(batch)} screened, {tried} draws, "
               f"{time.time() - t0:.0f} s", flush=True)
+        rnd += 1
     save(True)
     print(f"{name}: kept {len(kept)} of {nq} slots, {tried} draws -> {path}", flush=True)
 
@@ -187,8 +235,9 @@ def gen_cpu(name):
 if __name__ == "__main__":
     mode, names = sys.argv[1], sys.argv[2:]
     budget = float(os.environ.get("WORKLOAD_SECONDS", "0")) or None
+    resume = os.environ.get("WORKLOAD_RESUME") or None
     for n in names:
         if mode == "gpu":
-            gen_gpu(n, budget)
+            gen_gpu(n, budget, resume)
         else:
             {"verify": verify, "cpu": gen_cpu}[mode](n)
