@@ -16,6 +16,9 @@ the device-resident data graph.  Prints one JSON line (rank 0).
              against the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (backtracking, all host cores) on a bounded
              sample of the same queries
+  serving    p50 / p99 latency and sustained rate of the continuous-batching
+             server (smg_server_*) under seeded Poisson arrivals of the same
+             queries at 100, 1,000 and 5,000 queries/s offered
 
 --impl reference times the reference's algorithm on the host cores instead:
 the reference has no CPU implementation of its path and its GPU binary cannot
@@ -55,6 +58,8 @@ def parse():
     ap.add_argument("--subset", type=int, default=0, help="use only the first N queries (profiling runs)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-rates", default="100,1000,5000")
     return ap.parse_args()
 
 
@@ -126,6 +131,43 @@ def cpu_baseline(host, queries, seconds):
     return {"value": done / dt, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
             "sample": f"first {done} of {len(queries)} queries of the workload, oracle_count with "
                       f"{os.cpu_count()} OpenMP threads, {dt:.1f} s", "embeddings_per_s": emb / dt}
+
+
+def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
+    """Poisson arrivals into the continuous-batching server (smg_server_*).
+    Per rate, requests cycle through the workload's queries with seeded
+    exponential gaps; between arrivals the loop calls the non-blocking
+    smg_server_step.  Latency = finish - submit as the server stamps them;
+    sustained rate = requests / (last finish - first submit)."""
+    import random
+    from clustersm_gb300.native import Server
+    out = []
+    for rate in rates:
+        rng = random.Random(f"serve-{rate}")
+        n = max(64, min(max_requests, int(rate * seconds)))
+        srv = Server(ctx, dev, max_inflight=256)
+        tickets = []
+        t_next = time.perf_counter()
+        while len(tickets) < n:
+            if time.perf_counter() >= t_next:
+                j = len(tickets) % len(plans)
+                tickets.append((srv.submit(plans[j]), j))
+                t_next += rng.expovariate(rate)
+            else:
+                srv.step()
+        srv.drain()
+        lat, ok, first, last = [], 0, None, None
+        for tk, j in tickets:
+            r = srv.poll(tk)
+            lat.append((r.finish_s - r.submit_s) * 1e3)
+            ok += int(r.status == 0 and (want[j] is None or int(r.count) == int(want[j])))
+            first = r.submit_s if first is None else min(first, r.submit_s)
+            last = r.finish_s if last is None else max(last, r.finish_s)
+        srv.close()
+        lat.sort()
+        out.append({"offered_qps": rate, "requests": n, "p50_ms": lat[n // 2], "p99_ms": lat[(99 * (n - 1)) // 100],
+                    "sustained_qps": n / (last - first), "counts_ok": ok})
+    return out
 
 
 def run_reference(args, wl, host, queries, rank):
@@ -201,8 +243,10 @@ def main():
     counts, _ = native.match_batch(ctx, dev, plans)
     want = [expected[i] for i in mine]
     mismatches = sum(1 for c, w in zip(counts.tolist(), want) if w is not None and int(c) != int(w))
+    # warm-up with the timed call: the first captures the batch's CUDA graph
+    # (with its filter/join event nodes), the rest replay it
     for _ in range(args.warmup):
-        native.match_batch(ctx, dev, plans)
+        native.match_batch(ctx, dev, plans, profile=True)
 
     step_ms, join_ms, filt_ms, jbytes, fbytes, launches = [], 0.0, 0.0, 0, 0, 0
     h2d = d2h = 0
@@ -254,6 +298,10 @@ def main():
             native.match(ctx, dev, p)
         plain_qps = ns / (time.perf_counter() - t)
 
+    serve = None
+    if not args.no_serve and world == 1:
+        serve = serving(ctx, dev, plans, want, [float(r) for r in args.serve_rates.split(",") if r])
+
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = jbytes / (join_ms / 1e3) / 1e9 if join_ms > 0 else 0.0
@@ -283,6 +331,7 @@ def main():
                          "traffic": traffic,
                          "algorithmic_bytes_per_step": jbytes / args.steps},
             "clocks": clocks,
+            "serving": serve,
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(host, queries_all, args.cpu_seconds)

@@ -281,11 +281,82 @@ uint32_t plan_class(const Plan &P) {
   return 4 * shape + size;
 }
 
+namespace {
+
+uint64_t label_cands(const DevGraph &g, uint32_t l) { return l < g.label_count.size() ? g.label_count[l] : 0; }
+
+bool use_plan_order() {
+  static const bool v = [] {
+    const char *e = std::getenv("SMG_JOIN_ORDER");
+    return e && std::strcmp(e, "plan") == 0;
+  }();
+  return v;
+}
+
+}  // namespace
+
+// First vertex of the join's matching order: the fewest candidates (data
+// vertices with its label) per query edge; ties go to the lower index.
+uint32_t join_root(const Plan &P, const DevGraph &g) {
+  if (use_plan_order()) return P.root;
+  uint32_t root = 0;
+  for (uint32_t u = 1; u < P.k; ++u)
+    if (label_cands(g, P.label[u]) * P.deg[root] < label_cands(g, P.label[root]) * P.deg[u]) root = u;
+  return root;
+}
+
+// The join's matching order.  Every connected order yields the same
+// embeddings, so the join takes one chosen for the resident graph instead of
+// the order the reference's edge order (order.cpp getBFSEdgeOrder) reaches
+// the vertices in: after join_root, each next vertex has the most edges back
+// to the vertices already placed, then the fewest candidates, then the
+// highest degree.  SMG_JOIN_ORDER=plan selects the reference-derived order.
+void join_order(const Plan &P, const DevGraph &g, uint32_t *order, uint32_t *back, uint32_t *same) {
+  const uint32_t k = P.k;
+  std::vector<uint32_t> level(k, kNone);
+  if (use_plan_order()) {
+    for (uint32_t l = 0; l < k; ++l) order[l] = P.order[l];
+  } else {
+    order[0] = join_root(P, g);
+    level[order[0]] = 0;
+    for (uint32_t l = 1; l < k; ++l) {
+      uint32_t best = kNone, best_back = 0;
+      for (uint32_t u = 0; u < k; ++u) {
+        if (level[u] != kNone) continue;
+        uint32_t nb = 0;
+        for (uint32_t e = P.q_off[u]; e < P.q_off[u + 1]; ++e) nb += level[P.q_nbr[e]] != kNone;
+        if (!nb) continue;
+        bool better = best == kNone || nb > best_back;
+        if (!better && nb == best_back) {
+          const uint64_t cu = label_cands(g, P.label[u]), cb = label_cands(g, P.label[best]);
+          better = cu < cb || (cu == cb && P.deg[u] > P.deg[best]);
+        }
+        if (better) {
+          best = u;
+          best_back = nb;
+        }
+      }
+      order[l] = best;  // a connected query always has one
+      level[best] = l;
+    }
+  }
+  for (uint32_t l = 0; l < k; ++l) level[order[l]] = l;
+  for (uint32_t l = 0; l < k; ++l) {
+    const uint32_t u = order[l];
+    back[l] = 0;
+    same[l] = 0;
+    for (uint32_t e = P.q_off[u]; e < P.q_off[u + 1]; ++e)
+      if (level[P.q_nbr[e]] < l) back[l] |= 1u << level[P.q_nbr[e]];
+    for (uint32_t lw = 0; lw < l; ++lw)
+      if (P.label[order[lw]] == P.label[u]) same[l] |= 1u << lw;
+  }
+}
+
 QueryFootprint query_footprint(const DevGraph &g, const Plan &P) {
   QueryFootprint f;
   uint64_t cand = 0;
-  for (uint32_t u = 0; u < P.k; ++u) cand += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
-  const uint64_t rc = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
+  for (uint32_t u = 0; u < P.k; ++u) cand += label_cands(g, P.label[u]);
+  const uint64_t rc = label_cands(g, P.label[join_root(P, g)]);
   f.vmask = al(static_cast<size_t>(g.n) * 4);
   f.enc = al(static_cast<size_t>(g.n) * P.num_words * 4);
   f.cand = al(std::max<uint64_t>(cand, 1) * 4);
@@ -308,16 +379,13 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
   f.cand = b.cand;
   f.cand_cnt = b.counters->cand_cnt;
   f.roots = b.roots;
-  f.root_cap = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
+  std::memset(&j, 0, sizeof(j));
+  join_order(P, g, j.order, j.back_mask, j.same_label);
+  f.root = j.order[0];  // k_collect gathers the join's first vertex's candidates
+  f.root_cap = label_cands(g, P.label[f.root]);
   f.num_roots = &b.counters->num_roots;
   f.stat = b.counters->stat;
-  std::memset(&j, 0, sizeof(j));
   j.k = P.k;
-  for (uint32_t l = 0; l < P.k; ++l) {
-    j.order[l] = P.order[l];
-    j.back_mask[l] = P.back_mask[l];
-    j.same_label[l] = P.same_label_mask[l];
-  }
   j.candmask = b.vmask;
   j.roots = b.roots;
   j.num_roots = &b.counters->num_roots;
@@ -345,7 +413,7 @@ size_t query_bytes(const DevGraph &g, const Plan &P, uint64_t &cand_total) {
   cand_total = 0;
   for (uint32_t u = 0; u < P.k; ++u)
     cand_total += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
-  const uint64_t rc = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
+  const uint64_t rc = label_cands(g, P.label[join_root(P, g)]);
   return al(static_cast<size_t>(g.n) * 4) + al(static_cast<size_t>(g.n) * P.num_words * 4) + al(cand_total * 4) +
          al(rc * 4) + sizeof(QCounters) + al(sizeof(FilterQuery)) + al(sizeof(JoinQuery));
 }
@@ -388,7 +456,7 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
     o_cand[i] = off;
     off += al(ch.cand_total[i] * 4);
     o_root[i] = off;
-    const uint64_t rc = P.label[P.root] < g.label_count.size() ? g.label_count[P.label[P.root]] : 0;
+    const uint64_t rc = label_cands(g, P.label[join_root(P, g)]);
     off += al(std::max<uint64_t>(rc, 1) * 4);
   }
   const size_t o_tasks = off;
@@ -496,17 +564,20 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
 }
 
 // Zeroing memset, filter, seeding and join of a staged chunk on the stream
-// (also what a captured graph holds).
-smg_status enqueue_chunk(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunOpts &o) {
+// (also what a captured graph holds).  A profiled run brackets the filter and
+// the join with events; under capture they become event-record nodes
+// (cudaEventRecordExternal), recorded at every replay.
+smg_status enqueue_chunk(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunOpts &o, bool capturing) {
   const uint32_t nq = ch.b - ch.a;
+  const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
-  if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[0], c->stream));
+  if (o.profile) SMG_CUDA(cudaEventRecordWithFlags(c->ev[0], c->stream, ev_flags));
   smg_status s = launch_filter(g, ch.fq, nq, *c->fdev, walk_overflow(ch), c->stream, c->num_sms);
   if (s) return s;
-  if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[1], c->stream));
+  if (o.profile) SMG_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, ev_flags));
   s = launch_join(make_join_launch(c, g, ch, o), c->stream, c->num_sms);
   if (s) return s;
-  if (o.profile) SMG_CUDA(cudaEventRecord(c->ev[2], c->stream));
+  if (o.profile) SMG_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, ev_flags));
   return SMG_OK;
 }
 
@@ -532,7 +603,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
       drop_graph(c);
       cudaGraph_t graph = nullptr;
       SMG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      s = enqueue_chunk(c, g, ch, o);
+      s = enqueue_chunk(c, g, ch, o, true);
       cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
       if (s) {
         if (graph) cudaGraphDestroy(graph);
@@ -547,7 +618,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
       SMG_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
       c->graph_gen = c->run_gen;
     } else {
-      s = enqueue_chunk(c, g, ch, o);
+      s = enqueue_chunk(c, g, ch, o, false);
       if (s) return s;
     }
   }
@@ -645,12 +716,11 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     if (c->arena.cap != cap_before) drop_graph(c);  // arena moved: captured pointers are stale
     std::vector<const void *> key;
     const bool whole = a == 0 && b == nq;
-    // a profiled run times its phases with events on the stream and is not
-    // captured: events recorded into a graph give no elapsed time
-    if (o.use_graph && whole && !o.profile) {
+    if (o.use_graph && whole) {
       key.push_back(&g);
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.root_chunk)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.count_limit)));
+      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.profile)));
       for (uint32_t i = 0; i < nq; ++i) key.push_back(plans[i]);
     }
     s = run_chunk(c, g, plans, ch, o, out, st, key.empty() ? nullptr : &key);

@@ -44,6 +44,7 @@ constexpr int kWarpsPerBlock = 8;
 constexpr uint64_t kReadyWaitNs = 2000000000ull;   // 2 s for a producer to publish
 constexpr uint64_t kIdleLimitNs = 30000000000ull;  // 30 s without any progress
 constexpr unsigned long long kLimitFlush = 4096;    // count-limited joins publish at this many
+constexpr uint32_t kSplitLen = 8192;                // last-level lists are cut into slices this long
 
 __device__ __forceinline__ uint64_t now_ns() {
   uint64_t t;
@@ -226,11 +227,101 @@ __device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, c
   return true;
 }
 
+// A last-level list longer than kSplitLen is cut into slices of that length:
+// the first stays with this lane, the others become tasks (level P + 1, range
+// [lo, hi) of the list, prefix m[0..P-1] plus candidate v) when warps are
+// waiting for work or the list is very long.  Returns the length this lane
+// keeps (all of it when the queue has no room).
+__device__ uint32_t split_last(const WarpView &S, const JoinLaunch &p, const JoinQuery &Q, uint32_t q, uint32_t P,
+                               uint32_t v, uint32_t len) {
+  QueueState *qs = p.qs;
+  const unsigned long long h = vload(qs->head), t = vload(qs->tail);
+  if (!(h > t || len > 8 * kSplitLen)) return len;
+  const uint32_t slices = (len - 1) / kSplitLen;  // beyond the first
+  const unsigned long long first = atomicAdd(&qs->tail.v, static_cast<unsigned long long>(slices));
+  if (first + slices > p.cap) {
+    // no room: the slot numbers taken stay unpublished and are never waited
+    // for beyond the end of the run (their tickets see pending reach zero)
+    atomicExch(&qs->full, 1);
+    return len;
+  }
+  atomicAdd(&qs->pending.v, static_cast<unsigned long long>(slices));
+  atomicAdd(Q.pending, static_cast<unsigned long long>(slices));
+  const uint32_t tw = 4 + p.kmax;
+  for (uint32_t i = 0; i < slices; ++i) {
+    uint32_t *T = p.tasks + (first + i) * tw;
+    T[0] = q;
+    T[1] = P + 1;
+    T[2] = (i + 1) * kSplitLen;
+    T[3] = min(len, (i + 2) * kSplitLen);
+    for (uint32_t j = 0; j < P; ++j) T[4 + j] = S.m[j];
+    T[4 + P] = v;
+  }
+  __threadfence();
+  for (uint32_t i = 0; i < slices; ++i) atomicExch(p.ready + first + i, 1u);
+  atomicAdd(&qs->donations, static_cast<unsigned long long>(slices));
+  return kSplitLen;
+}
+
+// Counts (and optionally emits) the last level over entries [lo, hi) of one
+// list: the prefix m[0..P] is matched, the list is that of the last vertex's
+// back neighbour with the shortest list (the pivot last_level chose).
+__device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p, const JoinQuery &Q,
+                                               const uint32_t *__restrict__ candmask, uint32_t P, uint32_t lo,
+                                               uint32_t hi, uint32_t lane, unsigned long long &scanned,
+                                               uint32_t &probes) {
+  const uint32_t L = P + 1;
+  uint32_t piv = 0, bd = 0xFFFFFFFFu;
+  for (uint32_t b = S.bmask[L]; b; b &= b - 1) {
+    const uint32_t j = __ffs(b) - 1;
+    if (S.deg[j] < bd) {
+      bd = S.deg[j];
+      piv = j;
+    }
+  }
+  hi = min(hi, bd);
+  if (lo >= hi) return 0;
+  scanned += hi - lo;
+  const uint32_t *base = p.adj + S.beg[piv];
+  const uint32_t u = S.ord[L], back = S.bmask[L] & ~(1u << piv), same = S.slab[L];
+  const uint32_t lt = (1u << lane) - 1;
+  unsigned long long cnt = 0;
+  for (uint32_t t0 = lo; t0 < hi; t0 += 32) {
+    const uint32_t t = t0 + lane;
+    bool good = false;
+    uint32_t w = 0;
+    if (t < hi) {
+      w = __ldg(base + t);
+      good = SMG_DCHECK(w < p.n, 115, w, t) && ((__ldg(candmask + w) >> u) & 1u);
+      for (uint32_t b = same; b && good; b &= b - 1) good = S.m[__ffs(b) - 1] != w;
+      for (uint32_t b = back; b && good; b &= b - 1) {
+        const uint32_t j = __ffs(b) - 1;
+        good = is_neighbor(p, S.beg[j], S.deg[j], S.hub[j], w, probes);
+      }
+    }
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
+    cnt += __popc(bal);
+    if (p.emit && bal) {
+      unsigned long long pos = 0;
+      if (lane == 0) pos = atomicAdd(Q.emb_count, static_cast<unsigned long long>(__popc(bal)));
+      pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+      const unsigned long long r = pos + __popc(bal & lt);
+      if (good && r < Q.emb_cap) {
+        uint32_t *row = Q.emb + r * Q.k;
+        for (uint32_t j = 0; j <= P; ++j) row[S.ord[j]] = S.m[j];
+        row[S.ord[L]] = w;
+      }
+    }
+  }
+  __syncwarp();
+  return cnt;
+}
+
 // Counts (and optionally emits) the last level for every candidate of the
 // batch of level P = k-2: the candidates' last-level lists are concatenated
 // and walked 32 entries at a time, each lane finding its candidate by binary
 // search over the segment starts.  Returns the count (same in every lane).
-__device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const JoinQuery &Q,
+__device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const JoinQuery &Q, uint32_t q,
                                          const uint32_t *__restrict__ candmask, uint32_t P, uint32_t bc,
                                          uint32_t lane, unsigned long long &scanned, uint32_t &probes) {
   const uint32_t L = P + 1;
@@ -250,6 +341,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       }
     }
     len = bd;
+    if (len > kSplitLen) len = split_last(S, p, Q, q, P, v, len);
     S.sv[lane] = v;
     S.sbeg[lane] = vb;
     S.sdeg[lane] = vd;
@@ -479,7 +571,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     if (!SMG_DCHECK(q < p.nq, 109, q, p.nq)) break;
     const JoinQuery &Q = p.queries[q];
     const uint32_t k = Q.k, P = k - 2;
-    if (!SMG_DCHECK(L0 <= P, 110, L0, k)) break;
+    if (!SMG_DCHECK(L0 <= P + 1, 110, L0, k)) break;
     int drop = 0;
     if (lane == 0) drop = Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over);
     drop = __shfl_sync(0xFFFFFFFFu, drop, 0);
@@ -507,6 +599,12 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       S.hub[lane] = __ldg(p.hub_of + v);
     }
     __syncwarp();
+    unsigned long long cnt = 0;
+    bool aborted = false, preempted = false;
+    if (L0 == P + 1) {
+      // a slice of one last-level list, split off by last_level
+      cnt = last_level_range(S, p, Q, Q.candmask, P, lo, hi, lane, scanned, probes);
+    } else {
     if (lane == 0) {
       if (L0 == 0) {
         S.lbase[0] = Q.roots;
@@ -522,11 +620,9 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     }
     __syncwarp();
 
-    unsigned long long cnt = 0;
     uint32_t level = L0, iter = 0, tick = 0;  // tick paces donation checks
     const uint32_t *const candmask = Q.candmask;
     const uint32_t donate_min = max(2u, Q.donate_min ? Q.donate_min : p.donate_min);
-    bool aborted = false, preempted = false;
     while (true) {
       if ((++iter & 255) == 0) {
         int stop = 0;
@@ -583,7 +679,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       if (level == P) {
         const uint32_t bc = S.bcnt[level];
         if (bc) {
-          cnt += last_level(S, p, Q, candmask, P, bc, lane, scanned, probes);
+          cnt += last_level(S, p, Q, q, candmask, P, bc, lane, scanned, probes);
           descents += bc;
           if (lane == 0) S.bcnt[level] = 0;
           __syncwarp();
@@ -661,6 +757,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       if (level == L0) break;
       --level;
     }
+    }  // L0 <= P
     unsigned long long pr = probes;
     probes = 0;
     for (int o = 16; o; o >>= 1) pr += __shfl_down_sync(0xFFFFFFFFu, pr, o);

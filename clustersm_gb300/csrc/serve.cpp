@@ -95,6 +95,7 @@ struct Pool {
 
 struct smg_server {
   smg_ctx *ctx = nullptr;
+  int device = 0;
   const smg_graph *graph = nullptr;
   smg_server_config cfg{};
   uint64_t next_ticket = 1;
@@ -123,8 +124,11 @@ struct smg_server {
   smg::FilterDev fdev;
   std::vector<smg::QCounters> h_cnt;
 
+  // The context may already be closed (closing it synchronised its stream),
+  // so only the device is used here.
   ~smg_server() {
-    if (ctx) cudaStreamSynchronize(ctx->stream);
+    cudaSetDevice(device);
+    cudaDeviceSynchronize();
     for (void *p : {static_cast<void *>(pool_mem), static_cast<void *>(d_fq_new), static_cast<void *>(d_jq),
                     static_cast<void *>(d_cnt), static_cast<void *>(d_seed), static_cast<void *>(tasks[0]),
                     static_cast<void *>(tasks[1]), static_cast<void *>(ready[0]), static_cast<void *>(ready[1]),
@@ -354,6 +358,7 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   SMG_CUDA(cudaSetDevice(c->device));
   std::unique_ptr<smg_server> s(new smg_server);
   s->ctx = c;
+  s->device = c->device;
   s->graph = g;
   if (cfg) s->cfg = *cfg;
   if (!s->cfg.max_inflight) s->cfg.max_inflight = 64;

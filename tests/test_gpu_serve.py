@@ -53,8 +53,9 @@ def test_arrivals_while_running(ctx):
         if i % 8 == 7:
             srv.step()  # non-blocking: admits, launches or retires
     srv.drain()
-    for tk, w in zip(tickets, want[:96]):
-        r = srv.poll(tk)
+    results = [srv.poll(tk) for tk in tickets]
+    srv.close()
+    for r, w in zip(results, want[:96]):
         assert r.status == 0 and r.count == w
     for p, w in list(zip(plans, want))[:8]:
         res, _ = native.match(ctx, dev, p)
