@@ -133,7 +133,7 @@ def cpu_baseline(host, queries, seconds):
                       f"{os.cpu_count()} OpenMP threads, {dt:.1f} s", "embeddings_per_s": emb / dt}
 
 
-def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
+def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=512):
     """Poisson arrivals into the continuous-batching server (smg_server_*).
     Per rate, requests cycle through the workload's queries with seeded
     exponential gaps; between arrivals the loop calls the non-blocking
@@ -284,8 +284,9 @@ def main():
             barrier()
             t = time.perf_counter()
             ps = [Plan(q) for q in queries]
-            native.match_batch(ctx, dev, ps)
+            _, est = native.match_batch(ctx, dev, ps)
             e2e_t.append(time.perf_counter() - t)
+            h2d, d2h = est.h2d_bytes, est.d2h_bytes
         e2e_value = nq_all / (max(e2e_t) if world > 1 else statistics.median(e2e_t))
 
     # plain path (one query per call) on a sample

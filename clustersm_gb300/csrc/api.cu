@@ -269,9 +269,11 @@ struct Chunk {
   uint32_t walk_cap = 0;
   FilterQuery *fq = nullptr;
   JoinQuery *jq = nullptr;
-  std::vector<uint32_t *> vmask, enc, cand, roots;
+  std::vector<uint32_t *> vmask, enc, cand, roots, cbits;
   std::vector<uint64_t> cand_total;
 };
+
+size_t cbits_bytes(const DevGraph &g, uint32_t k) { return static_cast<size_t>(k) * ((g.n + 31ull) / 32) * 4; }
 
 }  // namespace
 
@@ -361,6 +363,7 @@ QueryFootprint query_footprint(const DevGraph &g, const Plan &P) {
   f.enc = al(static_cast<size_t>(g.n) * P.num_words * 4);
   f.cand = al(std::max<uint64_t>(cand, 1) * 4);
   f.roots = al(std::max<uint64_t>(rc, 1) * 4);
+  f.cbits = al(cbits_bytes(g, P.k));
   return f;
 }
 
@@ -387,6 +390,13 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
   f.stat = b.counters->stat;
   j.k = P.k;
   j.candmask = b.vmask;
+  if (b.cbits) {
+    j.cbits = b.cbits;
+    j.cwords = (g.n + 31ull) / 32;
+    j.lastcnt = b.vmask;
+    const uint32_t last_back = j.back_mask[P.k - 1];
+    if (last_back && !(last_back & (last_back - 1))) j.fast_last = static_cast<uint32_t>(__builtin_ctz(last_back)) + 1;
+  }
   j.roots = b.roots;
   j.num_roots = &b.counters->num_roots;
   j.count = &b.counters->count;
@@ -415,7 +425,7 @@ size_t query_bytes(const DevGraph &g, const Plan &P, uint64_t &cand_total) {
     cand_total += P.label[u] < g.label_count.size() ? g.label_count[P.label[u]] : 0;
   const uint64_t rc = label_cands(g, P.label[join_root(P, g)]);
   return al(static_cast<size_t>(g.n) * 4) + al(static_cast<size_t>(g.n) * P.num_words * 4) + al(cand_total * 4) +
-         al(rc * 4) + sizeof(QCounters) + al(sizeof(FilterQuery)) + al(sizeof(JoinQuery));
+         al(rc * 4) + al(cbits_bytes(g, P.k)) + sizeof(QCounters) + al(sizeof(FilterQuery)) + al(sizeof(JoinQuery));
 }
 
 uint32_t seed_tasks(const smg_ctx *c, const RunOpts &o, uint32_t nq) {
@@ -442,7 +452,7 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   off += al(nq * sizeof(QCounters));
   const size_t o_wcnt = off;
   off += al(kMaxWalkPhases * 2 * sizeof(unsigned int));
-  std::vector<size_t> o_enc(nq), o_vm(nq), o_cand(nq), o_root(nq);
+  std::vector<size_t> o_enc(nq), o_vm(nq), o_cand(nq), o_root(nq), o_cb(nq);
   for (uint32_t i = 0; i < nq; ++i) {
     o_enc[i] = off;
     off += al(static_cast<size_t>(g.n) * plans[ch.a + i]->num_words * 4);
@@ -458,6 +468,8 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
     o_root[i] = off;
     const uint64_t rc = label_cands(g, P.label[join_root(P, g)]);
     off += al(std::max<uint64_t>(rc, 1) * 4);
+    o_cb[i] = off;
+    off += al(cbits_bytes(g, P.k));
   }
   const size_t o_tasks = off;
   off += al(static_cast<size_t>(ch.cap) * (4 + ch.kmax) * 4);
@@ -487,7 +499,9 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   ch.enc.resize(nq);
   ch.cand.resize(nq);
   ch.roots.resize(nq);
+  ch.cbits.resize(nq);
   for (uint32_t i = 0; i < nq; ++i) {
+    ch.cbits[i] = reinterpret_cast<uint32_t *>(B + o_cb[i]);
     ch.enc[i] = reinterpret_cast<uint32_t *>(B + o_enc[i]);
     ch.vmask[i] = reinterpret_cast<uint32_t *>(B + o_vm[i]);
     ch.cand[i] = reinterpret_cast<uint32_t *>(B + o_cand[i]);
@@ -511,6 +525,7 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     b.enc = ch.enc[i];
     b.cand = ch.cand[i];
     b.roots = ch.roots[i];
+    b.cbits = ch.cbits[i];
     b.counters = ch.counters + i;
     b.emb = ch.emb;
     b.emb_cap = ch.emb ? o.emb_cap : 0;
@@ -630,14 +645,15 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   SMG_CUDA(cudaStreamSynchronize(c->stream));
   if (hq->error) {
     drop_graph(c);
-    const char *why = hq->error == JOIN_ERR_DEADLINE ? "join exceeded its time limit (SMG_TIME_LIMIT_S)"
+    const char *why = hq->error == JOIN_ERR_DEADLINE       ? "join exceeded its time limit (SMG_TIME_LIMIT_S)"
                       : hq->error == JOIN_ERR_IDLE_TIMEOUT ? "join made no progress for too long"
-                                                            : "a queued task was never published";
+                      : hq->error == JOIN_ERR_QUEUE_FULL   ? "join task queue full"
+                                                           : "a queued task was never published";
     char msg[320];
     std::snprintf(msg, sizeof(msg), "%s; queue: head %llu tail %llu pending %llu tasks done %llu donations %llu "
                   "progress %llu full %d", why, hq->head.v, hq->tail.v, hq->pending.v, hq->tasks_done,
                   hq->donations, hq->progress.v, hq->full);
-    return fail(SMG_ERR_TIMEOUT, msg);
+    return fail(hq->error == JOIN_ERR_QUEUE_FULL ? SMG_ERR_LIMIT : SMG_ERR_TIMEOUT, msg);
   }
   if (hq->pending.v != 0) return fail(SMG_ERR_INTERNAL, "join ended with pending tasks");
   for (uint32_t i = 0; i < nq; ++i) {
@@ -662,13 +678,14 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
       }
     st->filter_bytes += 12ull * g.n + lab * (8 + 32) + 8ull * q.initial_cands + 8ull * q.walk_entries +
                         4ull * q.num_roots;
+    st->join_bytes += 4ull * g.n + cbits_bytes(g, P.k);  // candidate bitmaps: masks read, rows written
   }
   st->tasks += hq->tasks_done;
   st->donations += hq->donations;
   st->scanned += hq->scanned;
   st->descents += hq->descents;
   st->probes += hq->probes;
-  st->join_bytes += 8ull * hq->scanned + 8ull * hq->descents + 4ull * hq->probes;
+  st->join_bytes += 8ull * hq->scanned + 8ull * hq->descents + 4ull * hq->probes + 8ull * hq->last_count_entries;
   if (o.profile) {
     float f = 0, j = 0;
     SMG_CUDA(cudaEventElapsedTime(&f, c->ev[0], c->ev[1]));

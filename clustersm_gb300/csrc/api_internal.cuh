@@ -107,14 +107,15 @@ void drop_graph(smg_ctx *c);
 // Device buffers holding one query's filter state and results.
 struct QueryBuffers {
   uint32_t *vmask = nullptr, *enc = nullptr, *cand = nullptr, *roots = nullptr;
+  uint32_t *cbits = nullptr;  // candidate bitmaps (null: the join tests vmask)
   QCounters *counters = nullptr;
   uint32_t *emb = nullptr;
   uint64_t emb_cap = 0;
 };
 // Sizes of those buffers for one plan (bytes, each rounded to 256).
 struct QueryFootprint {
-  size_t vmask, enc, cand, roots;
-  size_t total() const { return vmask + enc + cand + roots; }
+  size_t vmask, enc, cand, roots, cbits;
+  size_t total() const { return vmask + enc + cand + roots + cbits; }
 };
 QueryFootprint query_footprint(const DevGraph &g, const Plan &P);
 // Fills the filter and join records of one query whose state lives in `b`.

@@ -124,7 +124,18 @@ struct JoinQuery {
   uint32_t order[kMaxK];      // query vertex matched at each level
   uint32_t back_mask[kMaxK];  // earlier levels adjacent to the level's vertex
   uint32_t same_label[kMaxK]; // earlier levels with the same label (injectivity)
-  const uint32_t *candmask;   // [n] final candidate masks
+  const uint32_t *candmask;   // [n] final candidate masks (bit u: may take query vertex u)
+  // The same candidates as one bitmap per query vertex, cbits[u * cwords +
+  // v / 32] bit v % 32, built after the filter: a random candidate test then
+  // reads a 512 KB row (at 2^22 vertices) instead of a 16 MB mask array, so
+  // the rows of many concurrent queries stay in L2.  Null: the join tests
+  // candmask (caller-provided masks, smg_join_noalloc).
+  uint32_t *cbits;
+  uint64_t cwords;
+  // Count-only runs with fast_last set: the last level's per-vertex
+  // neighbour counts (see k_last_counts), written over candmask once cbits
+  // holds the candidates.
+  uint32_t *lastcnt;
   const uint32_t *roots;      // root candidates
   const uint32_t *num_roots;  // device counter
   unsigned long long *count;  // result
@@ -136,6 +147,17 @@ struct JoinQuery {
   unsigned long long *pending;  // tasks of this query queued or running
   uint32_t root_chunk;        // root candidates per seeded task (0: from max_seed_tasks)
   uint32_t donate_min;        // shortest list worth splitting off (0: launch default)
+  // Completion notice (serving; null: none).  The warp that finishes the
+  // query's last task writes the final count to done_count and then `gen` to
+  // done_gen, both in host-mapped memory, so the host sees the result while
+  // the slice is still running.
+  unsigned long long *done_count;
+  uint32_t *done_gen;
+  uint32_t gen;
+  // 1 + the level of the last vertex's only back neighbour when the last
+  // level can be counted from per-vertex neighbour counts (one back edge and
+  // cbits present); 0: the last level is always scanned.
+  uint32_t fast_last;
 };
 
 #if defined(SMG_CHECKED) && defined(__CUDACC__)

@@ -8,9 +8,10 @@
 // injective mappings whose every vertex passes its candidate bit and whose
 // every query edge is present.  This kernel computes the same set:
 //
-//  * vertices are matched in the order the reference's edge order first
-//    reaches them; each level checks, for a new vertex, its tree edge and
-//    every non-tree edge back to a matched vertex at once;
+//  * vertices are matched in the order of JoinQuery::order (a cost-based
+//    order chosen on the host; every connected order gives the same set);
+//    each level checks, for a new vertex, every query edge back to a matched
+//    vertex at once;
 //  * a persistent grid pulls tasks (a matched prefix plus a slice of the next
 //    level's list) from a device work queue and finishes each depth-first, so
 //    memory stays bounded instead of growing with the level sizes;
@@ -108,11 +109,14 @@ __global__ void k_seed(JoinLaunch p) {
     uint32_t chunk = rc ? rc : 1;
     chunk = max(chunk, (nr + p.max_seed_tasks - 1) / p.max_seed_tasks);
     const uint32_t nt = (nr + chunk - 1) / chunk;
-    atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
-    atomicAdd(p.queries[q].pending, static_cast<unsigned long long>(nt));
     const unsigned long long first = atomicAdd(&p.qs->tail.v, static_cast<unsigned long long>(nt));
     const uint32_t tw = 4 + p.kmax;
-    if (!SMG_DCHECK(first + nt <= p.cap, 101, first + nt, p.cap)) continue;
+    if (first + nt > p.cap) {  // no room: the run fails (batches size the queue for every seed)
+      set_error(p.qs, JOIN_ERR_QUEUE_FULL);
+      continue;
+    }
+    atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
+    atomicAdd(p.queries[q].pending, static_cast<unsigned long long>(nt));
     for (uint32_t i = 0; i < nt; ++i) {
       uint32_t *t = p.tasks + (first + i) * tw;
       t[0] = q;
@@ -134,6 +138,101 @@ __global__ void k_hub_bits(const uint32_t *__restrict__ off, const uint32_t *__r
     const uint32_t w = adj[e];
     atomicOr(row + (w >> 5), 1u << (w & 31));
   }
+}
+
+// Candidate test of data vertex w for query vertex u: one bit of u's row of
+// the candidate bitmaps, or bit u of w's mask when a query has no bitmaps.
+struct CandView {
+  const uint32_t *bits;  // cbits
+  uint64_t words;        // cwords
+  const uint32_t *mask;  // candmask
+  __device__ __forceinline__ bool has(uint32_t u, uint32_t w) const {
+    if (bits) return (__ldg(bits + u * words + (w >> 5)) >> (w & 31)) & 1u;
+    return (__ldg(mask + w) >> u) & 1u;
+  }
+};
+
+// Builds a query's candidate bitmaps from its final masks: a warp reads 32
+// consecutive masks (one coalesced line) and one ballot per query vertex is
+// that vertex's bitmap word.
+__global__ void __launch_bounds__(256) k_cand_bits(const JoinQuery *__restrict__ queries,
+                                                   const uint32_t *__restrict__ list, uint32_t nq, uint32_t n) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t qi = blockIdx.y; qi < nq; qi += gridDim.y) {
+    const JoinQuery &Q = queries[list ? list[qi] : qi];
+    if (!Q.cbits) continue;
+    const uint32_t k = Q.k;
+    const uint64_t words = Q.cwords;
+    for (uint64_t wi = warp; wi < words; wi += nwarps) {
+      const uint64_t v = wi * 32 + lane;
+      const uint32_t m = v < n ? __ldg(Q.candmask + v) : 0u;
+      uint32_t mine = 0;
+      for (uint32_t u = 0; u < k; ++u) {
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, (m >> u) & 1u);
+        if (lane == u) mine = b;
+      }
+      if (lane < k) Q.cbits[lane * words + wi] = mine;
+    }
+  }
+}
+
+// Last-level counts.  In a count-only run, when the last query vertex u_L
+// has a single edge back to the matched prefix (to level b), the last level
+// of a prefix m[0..k-2] accepts exactly the neighbours w of m[b] that are
+// candidates of u_L (which implies u_L's label) and differ from the matched
+// vertices of u_L's label.  Its count is therefore the number of such
+// neighbours of m[b], stored once per query for every candidate of order[b],
+// less the same-label matched vertices among them.  The counts overwrite the
+// final masks (the join tests candidates in the bitmaps); kNone marks a
+// vertex whose count is not stored (degree above kLastCountMaxDeg), whose
+// list the join scans as before.
+constexpr uint32_t kLastCountMaxDeg = 8192;
+
+// A warp takes 32 consecutive vertices, picks the candidates of order[b]
+// with a ballot and counts each one's qualifying neighbours with its lanes
+// (four independent list entries per lane per step).
+__global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict__ queries,
+                                                     const uint32_t *__restrict__ list, uint32_t nq,
+                                                     const uint32_t *__restrict__ off,
+                                                     const uint32_t *__restrict__ adj, uint32_t n, QueueState *qs) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  unsigned long long read = 0;
+  for (uint32_t qi = blockIdx.y; qi < nq; qi += gridDim.y) {
+    const JoinQuery &Q = queries[list ? list[qi] : qi];
+    if (!Q.fast_last) continue;
+    const uint32_t ub = Q.order[Q.fast_last - 1], ul = Q.order[Q.k - 1];
+    const uint32_t *row = Q.cbits + ul * Q.cwords;
+    uint32_t *cnt = Q.lastcnt;
+    for (uint64_t v0 = static_cast<uint64_t>(warp) * 32; v0 < n; v0 += static_cast<uint64_t>(nwarps) * 32) {
+      const uint64_t v = v0 + lane;
+      const uint32_t mine = v < n ? cnt[v] : 0u;  // the final mask, until overwritten below
+      for (uint32_t bal = __ballot_sync(0xFFFFFFFFu, (mine >> ub) & 1u); bal; bal &= bal - 1) {
+        const uint32_t src = __ffs(bal) - 1;
+        const uint64_t x = v0 + src;
+        const uint32_t beg = __ldg(off + x), end = __ldg(off + x + 1);
+        uint32_t c = kNone;
+        if (end - beg <= kLastCountMaxDeg) {
+          uint32_t part = 0;
+          for (uint32_t e = beg + lane; e < end; e += 128) {
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) w[i] = e + 32 * i < end ? __ldg(adj + e + 32 * i) : kNone;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (w[i] != kNone && SMG_DCHECK(w[i] < n, 120, w[i], x)) part += (__ldg(row + (w[i] >> 5)) >> (w[i] & 31)) & 1u;
+          }
+          c = __reduce_add_sync(0xFFFFFFFFu, part);
+          read += end - beg;
+        }
+        if (lane == src) cnt[x] = c;
+      }
+    }
+  }
+  if (lane == 0 && read) atomicAdd(&qs->last_count_entries, read);
 }
 
 // Is w in the neighbour list (beg, deg) of a matched vertex?  `hub` selects
@@ -214,10 +313,10 @@ __device__ __forceinline__ uint32_t choose_pivot(const WarpView &S, uint32_t lev
 }
 
 // Candidate test for list entry w at `level` (>= 1, not the last level).
-__device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const uint32_t *__restrict__ candmask,
-                                       uint32_t level, uint32_t w, uint32_t &probes) {
+__device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const CandView &cv, uint32_t level,
+                                       uint32_t w, uint32_t &probes) {
   if (!SMG_DCHECK(w < p.n, 105, w, level)) return false;
-  if (!((__ldg(candmask + w) >> S.ord[level]) & 1u)) return false;
+  if (!cv.has(S.ord[level], w)) return false;
   for (uint32_t b = S.slab[level]; b; b &= b - 1)
     if (S.m[__ffs(b) - 1] == w) return false;
   for (uint32_t b = S.bmask[level] & ~(1u << S.piv[level]); b; b &= b - 1) {
@@ -237,6 +336,7 @@ __device__ uint32_t split_last(const WarpView &S, const JoinLaunch &p, const Joi
   QueueState *qs = p.qs;
   const unsigned long long h = vload(qs->head), t = vload(qs->tail);
   if (!(h > t || len > 8 * kSplitLen)) return len;
+  if (*reinterpret_cast<volatile int *>(&qs->closing)) return len;
   const uint32_t slices = (len - 1) / kSplitLen;  // beyond the first
   const unsigned long long first = atomicAdd(&qs->tail.v, static_cast<unsigned long long>(slices));
   if (first + slices > p.cap) {
@@ -267,7 +367,7 @@ __device__ uint32_t split_last(const WarpView &S, const JoinLaunch &p, const Joi
 // list: the prefix m[0..P] is matched, the list is that of the last vertex's
 // back neighbour with the shortest list (the pivot last_level chose).
 __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p, const JoinQuery &Q,
-                                               const uint32_t *__restrict__ candmask, uint32_t P, uint32_t lo,
+                                               const CandView &cv, uint32_t P, uint32_t lo,
                                                uint32_t hi, uint32_t lane, unsigned long long &scanned,
                                                uint32_t &probes) {
   const uint32_t L = P + 1;
@@ -292,7 +392,7 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
     uint32_t w = 0;
     if (t < hi) {
       w = __ldg(base + t);
-      good = SMG_DCHECK(w < p.n, 115, w, t) && ((__ldg(candmask + w) >> u) & 1u);
+      good = SMG_DCHECK(w < p.n, 115, w, t) && cv.has(u, w);
       for (uint32_t b = same; b && good; b &= b - 1) good = S.m[__ffs(b) - 1] != w;
       for (uint32_t b = back; b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
@@ -322,11 +422,12 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
 // and walked 32 entries at a time, each lane finding its candidate by binary
 // search over the segment starts.  Returns the count (same in every lane).
 __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const JoinQuery &Q, uint32_t q,
-                                         const uint32_t *__restrict__ candmask, uint32_t P, uint32_t bc,
+                                         const CandView &cv, uint32_t P, uint32_t bc,
                                          uint32_t lane, unsigned long long &scanned, uint32_t &probes) {
   const uint32_t L = P + 1;
   const uint32_t lt = (1u << lane) - 1;
-  uint32_t len = 0;
+  const bool fast_ok = Q.fast_last && !p.emit;  // k_last_counts ran only then
+  uint32_t len = 0, fast = 0;
   if (lane < bc) {
     uint32_t v = S.batch[P * 32 + lane];
     if (!SMG_DCHECK(v < p.n, 106, v, P)) v = 0;
@@ -341,6 +442,25 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       }
     }
     len = bd;
+    if (fast_ok) {
+      // one back edge (to level piv): the stored neighbour count of its vertex
+      // a, less the matched vertices of the last vertex's label adjacent to a
+      const uint32_t a = piv == P ? v : S.m[piv];
+      const uint32_t c = __ldg(Q.lastcnt + a);
+      if (c != kNone) {
+        const uint32_t ab = piv == P ? vb : S.beg[piv], ad = piv == P ? vd : S.deg[piv];
+        const uint32_t ah = piv == P ? __ldg(p.hub_of + v) : S.hub[piv];
+        const uint32_t u = S.ord[L];
+        uint32_t corr = 0;
+        for (uint32_t b = S.slab[L]; b; b &= b - 1) {
+          const uint32_t j = __ffs(b) - 1;
+          const uint32_t x = j == P ? v : S.m[j];
+          if (x != a && cv.has(u, x) && is_neighbor(p, ab, ad, ah, x, probes)) ++corr;
+        }
+        fast = c - corr;
+        len = 0;
+      }
+    }
     if (len > kSplitLen) len = split_last(S, p, Q, q, P, v, len);
     S.sv[lane] = v;
     S.sbeg[lane] = vb;
@@ -358,7 +478,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   S.spre[lane] = incl - len;
   __syncwarp();
   scanned += total;
-  unsigned long long cnt = 0;
+  unsigned long long cnt = fast_ok ? __reduce_add_sync(0xFFFFFFFFu, fast) : 0u;
   const uint32_t u = S.ord[L];
   const uint32_t back = S.bmask[L], same = S.slab[L];
   for (uint32_t t0 = 0; t0 < total; t0 += 32) {
@@ -379,7 +499,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       const uint64_t ai = static_cast<uint64_t>(S.sbase[i]) + (t - S.spre[i]);
       const bool in_adj = SMG_DCHECK(ai < p.m2, 107, ai, i);
       w = in_adj ? __ldg(p.adj + ai) : 0u;
-      good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) && ((__ldg(candmask + w) >> u) & 1u);
+      good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) && cv.has(u, w);
       for (uint32_t b = same; b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
         good = (j == P ? vi : S.m[j]) != w;
@@ -424,7 +544,7 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, unsigne
     const unsigned long long h = vload(qs->head), t = vload(qs->tail);
     {
       // tickets beyond the tail are warps waiting for work
-      if (h > t && t < p.cap) {
+      if (h > t && t < p.cap && !*reinterpret_cast<volatile int *>(&qs->closing)) {
         uint32_t tl = kNone, lo = 0, hi = 0, item = 0;
         for (uint32_t l = L0; l <= level && tl == kNone; ++l) {
           const uint32_t c = S.cur[l], e = S.end[l];
@@ -478,9 +598,11 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, unsigne
 }
 
 // End of a time slice: every part of this warp's stack that is not done
-// becomes a carry-over task: the unscanned rest of each level's list, and each
-// untried batch candidate (as a task one level deeper).  Returns false (and
-// the warp keeps working) if the carry buffer cannot take them all.
+// becomes a task of the next slice's queue: the unscanned rest of each level's
+// list, and each untried batch candidate (as a task one level deeper).  The
+// next queue must also take this queue's untaken tasks (at most its tail) and
+// what racing warps still push (kPreemptSlack).  Returns false (and the warp
+// keeps working) when they would not fit.
 __device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned long long *qpending, uint32_t L0,
                         uint32_t level, uint32_t P, uint32_t lane) {
   int ok = 0;
@@ -493,10 +615,11 @@ __device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned l
     if (n == 0) {
       ok = 1;
     } else {
-      unsigned int old = *reinterpret_cast<volatile unsigned int *>(p.carry_count);
+      const unsigned long long tail = vload(p.qs->tail);
+      unsigned int old = *reinterpret_cast<volatile unsigned int *>(p.next_count);
       unsigned int base = kNone;
-      while (old + n <= p.carry_cap) {
-        const unsigned int seen = atomicCAS(p.carry_count, old, old + n);
+      while (static_cast<unsigned long long>(old) + n + tail + kPreemptSlack <= p.cap) {
+        const unsigned int seen = atomicCAS(p.next_count, old, old + n);
         if (seen == old) {
           base = old;
           break;
@@ -508,22 +631,24 @@ __device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned l
         uint32_t idx = base;
         for (uint32_t l = L0; l <= level; ++l) {
           if (S.cur[l] < S.end[l]) {
-            uint32_t *T = p.carry + static_cast<uint64_t>(idx++) * tw;
+            uint32_t *T = p.next_tasks + static_cast<uint64_t>(idx) * tw;
             T[0] = q;
             T[1] = l;
             T[2] = S.cur[l];
             T[3] = S.end[l];
             for (uint32_t j = 0; j < l; ++j) T[4 + j] = S.m[j];
+            p.next_ready[idx++] = 1;
           }
           if (l < P)
             for (uint32_t b = S.bidx[l]; b < S.bcnt[l]; ++b) {
-              uint32_t *T = p.carry + static_cast<uint64_t>(idx++) * tw;
+              uint32_t *T = p.next_tasks + static_cast<uint64_t>(idx) * tw;
               T[0] = q;
               T[1] = l + 1;
               T[2] = 0;
               T[3] = kNone;
               for (uint32_t j = 0; j < l; ++j) T[4 + j] = S.m[j];
               T[4 + l] = S.batch[l * 32 + b];
+              p.next_ready[idx++] = 1;
             }
         }
         atomicAdd(qpending, static_cast<unsigned long long>(n));
@@ -534,6 +659,18 @@ __device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned l
   ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
   __syncwarp();
   return ok != 0;
+}
+
+// The warp that took a served query's pending count to zero publishes the
+// final count to the host-mapped completion record.  Every warp added its
+// share to Q.count before a fence and its pending decrement, so the count
+// read here after the last decrement is final.
+__device__ __forceinline__ void notify_done(const JoinQuery &Q) {
+  __threadfence();
+  const unsigned long long total = atomicAdd(Q.count, 0ull);
+  *reinterpret_cast<volatile unsigned long long *>(Q.done_count) = total;
+  __threadfence_system();
+  *reinterpret_cast<volatile uint32_t *>(Q.done_gen) = Q.gen;
 }
 
 __device__ __forceinline__ void join_body(const JoinLaunch &p) {
@@ -599,11 +736,15 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       S.hub[lane] = __ldg(p.hub_of + v);
     }
     __syncwarp();
+    CandView cv;
+    cv.bits = Q.cbits;
+    cv.words = Q.cwords;
+    cv.mask = Q.candmask;
     unsigned long long cnt = 0;
     bool aborted = false, preempted = false;
     if (L0 == P + 1) {
       // a slice of one last-level list, split off by last_level
-      cnt = last_level_range(S, p, Q, Q.candmask, P, lo, hi, lane, scanned, probes);
+      cnt = last_level_range(S, p, Q, cv, P, lo, hi, lane, scanned, probes);
     } else {
     if (lane == 0) {
       if (L0 == 0) {
@@ -621,7 +762,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     __syncwarp();
 
     uint32_t level = L0, iter = 0, tick = 0;  // tick paces donation checks
-    const uint32_t *const candmask = Q.candmask;
+
     const uint32_t donate_min = max(2u, Q.donate_min ? Q.donate_min : p.donate_min);
     while (true) {
       if ((++iter & 255) == 0) {
@@ -661,9 +802,12 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         if (lane == 0) {
           if (*reinterpret_cast<volatile int *>(&qs->closing)) {
             close = 1;
-          } else if (now_ns() - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.slice_ns) {
-            atomicExch(&qs->closing, 1);
-            close = 1;
+          } else {
+            const uint64_t el = now_ns() - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns);
+            if (el > p.slice_ns || (el > p.slice_min_ns && p.bell && *p.bell)) {
+              atomicExch(&qs->closing, 1);
+              close = 1;
+            }
           }
         }
         close = __shfl_sync(0xFFFFFFFFu, close, 0);
@@ -679,7 +823,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       if (level == P) {
         const uint32_t bc = S.bcnt[level];
         if (bc) {
-          cnt += last_level(S, p, Q, q, candmask, P, bc, lane, scanned, probes);
+          cnt += last_level(S, p, Q, q, cv, P, bc, lane, scanned, probes);
           descents += bc;
           if (lane == 0) S.bcnt[level] = 0;
           __syncwarp();
@@ -741,7 +885,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
                                                 : static_cast<uint64_t>(base - p.adj) + c + lane < p.m2,
                                    114, c + lane, level)) {
           w = __ldg(base + c + lane);
-          good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, candmask, level, w, probes));
+          good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, cv, level, w, probes));
         }
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
         if (good) S.batch[level * 32 + __popc(bal & lt)] = w;
@@ -772,8 +916,10 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       if (!aborted) {
         atomicAdd(&qs->tasks_done, 1ull);
         atomicAdd(&qs->progress.v, 1ull);
-        atomicAdd(Q.pending, ~0ull);       // -1
-        atomicAdd(&qs->pending.v, ~0ull);  // -1
+        if (Q.done_gen) __threadfence();  // this task's count before its pending decrement
+        const unsigned long long left = atomicAdd(Q.pending, ~0ull);  // -1
+        atomicAdd(&qs->pending.v, ~0ull);                             // -1
+        if (left == 1 && Q.done_gen) notify_done(Q);
       }
     }
     scanned = 0;
@@ -782,10 +928,11 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
   }
 }
 
-// The join at the compiler's register choice (fewer, fatter warps) and
-// bounded to 6 resident blocks per SM (more warps to hide latency, a small
-// spill).  SMG_JOIN_OCCUPANCY=high selects the second.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_join(JoinLaunch p) { join_body(p); }
+// The join bounded to 4 resident blocks per SM (64 registers, 32 warps per
+// SM to hide the latency of its scattered reads; at the compiler's own
+// choice of 80 registers only 3 fit) and to 6 (40 registers and a spill).
+// SMG_JOIN_OCCUPANCY=high selects the second.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4) k_join(JoinLaunch p) { join_body(p); }
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_join_hi(JoinLaunch p) { join_body(p); }
 
 __global__ void k_slice_begin(QueueState *qs) {
@@ -793,52 +940,49 @@ __global__ void k_slice_begin(QueueState *qs) {
   qs->closing = 0;
 }
 
-// Single block: keep the published-but-untaken tasks of the old queue
-// (ready == 1) in order, then append the carry-over tasks.
-__global__ void __launch_bounds__(1024) k_compact(const uint32_t *__restrict__ tasks_old,
-                                                  const uint32_t *__restrict__ ready_old, uint32_t n_old,
-                                                  const uint32_t *__restrict__ carry,
-                                                  const unsigned int *__restrict__ carry_count, uint32_t carry_cap,
-                                                  uint32_t tw, uint32_t *__restrict__ tasks_new,
-                                                  uint32_t *__restrict__ ready_new, QueueState *qs) {
-  __shared__ uint32_t warp_sum[32];
-  __shared__ uint32_t running;
-  const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  if (tid == 0) running = 0;
-  __syncthreads();
-  for (uint32_t base = 0; base < n_old; base += blockDim.x) {
-    const uint32_t i = base + tid;
+// Appends the published-but-untaken tasks of the old queue (ready == 1) to
+// the new queue behind what preempted warps wrote there.  A warp takes 32
+// slots, claims room for its kept tasks with one atomic and copies them with
+// its lanes over the task's words.  A task that would not fit records
+// JOIN_ERR_QUEUE_FULL (preempt leaves room for every untaken task, so this is
+// a guard, not a path).
+__global__ void k_compact(const uint32_t *__restrict__ tasks_old, const uint32_t *__restrict__ ready_old,
+                          uint32_t cap, uint32_t tw, uint32_t *__restrict__ tasks_new,
+                          uint32_t *__restrict__ ready_new, unsigned int *new_count, QueueState *qs) {
+  const unsigned long long tail = *reinterpret_cast<volatile unsigned long long *>(&qs->tail.v);
+  const uint32_t n_old = static_cast<uint32_t>(min(tail, static_cast<unsigned long long>(cap)));
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint64_t base = static_cast<uint64_t>(warp) * 32; base < n_old; base += static_cast<uint64_t>(nwarps) * 32) {
+    const uint64_t i = base + lane;
     const bool keep = i < n_old && ready_old[i] == 1;
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
-    if (lane == 0) warp_sum[wid] = __popc(bal);
-    __syncthreads();
-    uint32_t before = running;
-    for (uint32_t w = 0; w < wid; ++w) before += warp_sum[w];
-    if (keep) {
-      const uint32_t dst = before + __popc(bal & ((1u << lane) - 1));
-      for (uint32_t j = 0; j < tw; ++j) tasks_new[static_cast<uint64_t>(dst) * tw + j] = tasks_old[static_cast<uint64_t>(i) * tw + j];
-      ready_new[dst] = 1;
+    if (!bal) continue;
+    unsigned int first = 0;
+    if (lane == 0) first = atomicAdd(new_count, static_cast<unsigned int>(__popc(bal)));
+    first = __shfl_sync(0xFFFFFFFFu, first, 0);
+    uint32_t r = 0;
+    for (uint32_t bb = bal; bb; bb &= bb - 1, ++r) {
+      const uint64_t src = base + __ffs(bb) - 1, dst = static_cast<uint64_t>(first) + r;
+      if (dst >= cap) {
+        if (lane == 0) atomicCAS(&qs->error, 0, JOIN_ERR_QUEUE_FULL);
+        break;
+      }
+      for (uint32_t j = lane; j < tw; j += 32) tasks_new[dst * tw + j] = tasks_old[src * tw + j];
+      if (lane == 0) ready_new[dst] = 1;
     }
-    __syncthreads();
-    if (tid == 0) {
-      uint32_t tot = 0;
-      for (uint32_t w = 0; w < blockDim.x / 32; ++w) tot += warp_sum[w];
-      running += tot;
-    }
-    __syncthreads();
   }
-  const uint32_t kept = running;
-  const uint32_t nc = min(*carry_count, carry_cap);
-  for (uint32_t i = tid; i < nc; i += blockDim.x) {
-    for (uint32_t j = 0; j < tw; ++j) tasks_new[static_cast<uint64_t>(kept + i) * tw + j] = carry[static_cast<uint64_t>(i) * tw + j];
-    ready_new[kept + i] = 1;
-  }
-  if (tid == 0) {
-    qs->head.v = 0;
-    qs->tail.v = kept + nc;
-    qs->pending.v = kept + nc;
-    qs->closing = 0;
-  }
+}
+
+// The new queue holds new_count tasks: head 0, tail = pending = that count.
+__global__ void k_compact_finish(QueueState *qs, unsigned int *new_count, uint32_t cap) {
+  const unsigned long long n = min(static_cast<unsigned long long>(*new_count), static_cast<unsigned long long>(cap));
+  qs->head.v = 0;
+  qs->tail.v = n;
+  qs->pending.v = n;
+  qs->closing = 0;
+  *new_count = 0;
 }
 
 }  // namespace
@@ -849,11 +993,13 @@ smg_status launch_slice_begin(QueueState *qs, cudaStream_t s) {
   return SMG_OK;
 }
 
-smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, uint32_t n_old,
-                          const uint32_t *carry, const unsigned int *carry_count, uint32_t carry_cap, uint32_t tw,
-                          uint32_t *tasks_new, uint32_t *ready_new, QueueState *qs, cudaStream_t s) {
-  k_compact<<<1, 1024, 0, s>>>(tasks_old, ready_old, n_old, carry, carry_count, carry_cap, tw, tasks_new, ready_new,
-                               qs);
+smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, uint32_t cap, uint32_t tw,
+                          uint32_t *tasks_new, uint32_t *ready_new, unsigned int *new_count, QueueState *qs,
+                          cudaStream_t s, int num_sms) {
+  k_compact<<<std::max(num_sms, 1) * 4, 256, 0, s>>>(tasks_old, ready_old, cap, tw, tasks_new, ready_new, new_count,
+                                                      qs);
+  SMG_CUDA(cudaGetLastError());
+  k_compact_finish<<<1, 1, 0, s>>>(qs, new_count, cap);
   SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }
@@ -897,6 +1043,8 @@ smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   if (jl.nq == 0) return SMG_OK;
   const uint32_t seed_threads = 128;
   const uint32_t nseed = jl.seed_list ? jl.seed_n : jl.nq;
+  smg_status rc = launch_join_prep(jl, s, num_sms);
+  if (rc) return rc;
   k_seed<<<(nseed + seed_threads - 1) / seed_threads, seed_threads, 0, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
   return launch_persistent(jl, s, num_sms);
@@ -904,6 +1052,23 @@ smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
 
 smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   return launch_persistent(jl, s, num_sms);
+}
+
+smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
+  const uint32_t nq = jl.seed_list ? jl.seed_n : jl.nq;
+  if (!nq || !jl.n) return SMG_OK;
+  const uint64_t words = (static_cast<uint64_t>(jl.n) + 31) / 32;
+  const uint32_t want = std::max<uint32_t>(1, static_cast<uint32_t>(std::max(num_sms, 1)) * 16 / nq);
+  const uint32_t span_bits = static_cast<uint32_t>((words + 7) / 8);  // 8 warps per block, a word each
+  const dim3 g1(std::min(span_bits, want), std::min<uint32_t>(nq, 65535));
+  k_cand_bits<<<g1, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.n);
+  SMG_CUDA(cudaGetLastError());
+  if (jl.emit) return SMG_OK;
+  const uint32_t span = static_cast<uint32_t>((static_cast<uint64_t>(jl.n) + 255) / 256);  // 32 vertices a warp
+  const dim3 g2(std::min(span, want), std::min<uint32_t>(nq, 65535));
+  k_last_counts<<<g2, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.off, jl.adj, jl.n, jl.qs);
+  SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
 }
 
 smg_status launch_seed(const JoinLaunch &jl, cudaStream_t s) {

@@ -20,6 +20,7 @@ struct alignas(128) QLine {
 struct QueueState {
   QLine head, tail, pending, progress;
   unsigned long long tasks_done, donations, start_ns, scanned, descents, probes;
+  unsigned long long last_count_entries;  // list entries read by k_last_counts
   int error;  // JOIN_ERR_* below, first one wins
   int abort;  // set on error or deadline: every warp leaves
   int full;   // a donation found the queue full (load balance only)
@@ -28,6 +29,10 @@ struct QueueState {
 constexpr int JOIN_ERR_READY_TIMEOUT = 1;  // a claimed task was never published
 constexpr int JOIN_ERR_DEADLINE = 2;       // the run exceeded its time limit
 constexpr int JOIN_ERR_IDLE_TIMEOUT = 3;   // no warp made progress for too long
+constexpr int JOIN_ERR_QUEUE_FULL = 4;     // a time slice's leftover tasks did not fit the next queue
+// Queue slots kept free for tasks that racing warps push after a slice's
+// preemptions sized the next queue (at most about 12 per resident warp).
+constexpr uint32_t kPreemptSlack = 1u << 16;
 
 struct JoinLaunch {
   const uint32_t *off, *adj;
@@ -48,12 +53,17 @@ struct JoinLaunch {
   uint32_t donate_min;       // shortest remaining list worth donating
   uint64_t time_limit_ns;    // device-side deadline for the whole run
   int emit;
-  // time-sliced runs (serving): after slice_ns every warp pushes what is left
-  // of its stack to `carry` and leaves; 0 = run to completion
+  // Time-sliced runs (serving).  A slice closes after slice_ns, or after
+  // slice_min_ns once the host has rung `bell` (a host-mapped word: requests
+  // are waiting and slots are free).  Then every warp writes what is left of
+  // its stack into the next slice's queue and leaves.  slice_ns = 0: run to
+  // completion.
   uint64_t slice_ns;
-  uint32_t *carry;           // [carry_cap][4 + kmax]
-  uint32_t carry_cap;
-  unsigned int *carry_count;
+  uint64_t slice_min_ns;
+  const volatile uint32_t *bell;
+  uint32_t *next_tasks;      // [cap][4 + kmax]
+  uint32_t *next_ready;      // [cap], zero on entry
+  unsigned int *next_count;  // tasks written to the next queue, zero on entry
   const uint32_t *seed_list; // seed only these query indices (null: 0 .. nq-1)
   uint32_t seed_n;
 };
@@ -71,12 +81,20 @@ smg_status launch_slice_begin(QueueState *qs, cudaStream_t s);
 smg_status launch_seed(const JoinLaunch &jl, cudaStream_t s);
 // Persistent join without seeding (tasks already queued).
 smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms);
-// Rebuilds the queue after a slice: published-but-untaken tasks of the old
-// queue, then the carry-over tasks, into `tasks_new` (ready_new zeroed on
-// entry); resets head/tail/pending.  Single block.
-smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, uint32_t n_old,
-                          const uint32_t *carry, const unsigned int *carry_count, uint32_t carry_cap, uint32_t tw,
-                          uint32_t *tasks_new, uint32_t *ready_new, QueueState *qs, cudaStream_t s);
+// Rebuilds the queue after a slice: appends the published-but-untaken tasks
+// of the old queue (ready == 1) to the new one, behind the tasks preempted
+// warps wrote there (new_count of them), then resets head/tail/pending to the
+// new queue and clears new_count.  A whole grid; order is not kept.
+smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, uint32_t cap, uint32_t tw,
+                          uint32_t *tasks_new, uint32_t *ready_new, unsigned int *new_count, QueueState *qs,
+                          cudaStream_t s, int num_sms);
+// Join inputs built after the filter for the queries jl.seed_list names (all
+// jl.nq when it is null): each query's candidate bitmaps (cbits) from its
+// final masks, then, unless the run emits embeddings, its last-level counts
+// (fast_last queries): for every candidate v of the last vertex's back
+// neighbour, how many neighbours of v are candidates of the last vertex.
+// launch_join runs it itself.
+smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms);
 // Neighbour bitmaps of the highest-degree vertices (degree >= min_degree,
 // at most max_bytes of bitmaps), built once per resident graph.
 smg_status build_hub_bitmaps(DevGraph &g, uint32_t min_degree, size_t max_bytes, cudaStream_t s,

@@ -10,20 +10,27 @@
 //     budget; admission order is arrival order;
 //   * newly admitted queries are filtered together and their root tasks are
 //     appended to the live queue;
-//   * the join runs in time slices (SMG_SLICE_MS, default 2 ms): at the end of
-//     a slice every warp hands the unfinished part of its depth-first stack
-//     back as tasks, so requests that arrived meanwhile start in the next
+//   * the join runs in slices.  A slice ends when its work is done, after
+//     SMG_SLICE_MS (default 250 ms), or, once SMG_SLICE_MIN_MS (default 2 ms)
+//     have passed, when the host rings a doorbell in host-mapped memory
+//     because requests are waiting and slots are free.  At the end of a slice
+//     every warp writes the unfinished part of its depth-first stack into the
+//     next slice's queue, so requests that arrived meanwhile start in the next
 //     slice alongside the ones still running;
-//   * a query is finished when its count of queued and running tasks is zero;
-//     its slot and memory are released and its count is final.
+//   * a query is finished when its count of queued and running tasks reaches
+//     zero.  The warp that brings it there writes the final count to a
+//     host-mapped completion record, so the host retires the request (and
+//     frees its slot and memory) while the slice is still running.
 //
-// smg_server_step never blocks while a slice is on the device.
+// smg_server_step never blocks while a slice is on the device; between
+// slices it synchronises once (counters, queue state, admission staging).
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
+#include <thread>
 
 #include "api_internal.cuh"
 
@@ -45,9 +52,17 @@ struct Request {
 struct Slot {
   bool used = false;
   uint64_t ticket = 0;
+  uint32_t gen = 0;          // admission number, echoed by the completion record
   const smg::Plan *plan = nullptr;
   size_t off = 0, size = 0;  // pool range
   double submit_s = 0, start_s = 0;
+};
+
+// Host-mapped completion record of one slot (written by the join).
+struct alignas(16) Done {
+  unsigned long long count;
+  uint32_t gen;
+  uint32_t pad;
 };
 
 // First-fit allocator over one device buffer, with coalescing frees.
@@ -99,8 +114,10 @@ struct smg_server {
   const smg_graph *graph = nullptr;
   smg_server_config cfg{};
   uint64_t next_ticket = 1;
+  uint32_t next_gen = 0;
   std::deque<Request> waiting;
   std::vector<Slot> slots;
+  uint32_t free_slots = 0;
   std::map<uint64_t, smg_request_result> done;
   Pool pool;
   // device allocations
@@ -111,18 +128,24 @@ struct smg_server {
   uint32_t *d_seed = nullptr;            // slots to seed
   uint32_t *tasks[2] = {nullptr, nullptr};
   uint32_t *ready[2] = {nullptr, nullptr};
-  uint32_t *carry = nullptr;
-  unsigned int *carry_count = nullptr;
+  unsigned int *next_count = nullptr;    // tasks preempted into the other queue
   smg::QueueState *qs = nullptr;
   unsigned int *walk_count = nullptr;
   uint4 *walk_items = nullptr;
-  uint32_t cap = 0, carry_cap = 0, cur = 0;
-  uint64_t slice_ns = 0;
+  uint32_t cap = 0, cur = 0;
+  uint64_t slice_ns = 0, slice_min_ns = 0;
   cudaEvent_t ev = nullptr;
-  bool inflight = false;
+  bool inflight = false, bell_rung = false;
+  double slice_start_s = 0;
   uint64_t slices = 0;
   smg::FilterDev fdev;
-  std::vector<smg::QCounters> h_cnt;
+  // page-locked host memory: counters and queue state read back between
+  // slices; the doorbell and the completion records are also mapped into the
+  // device's address space
+  smg::QCounters *h_cnt = nullptr;
+  smg::QueueState *h_qs = nullptr;
+  uint32_t *h_bell = nullptr, *d_bell = nullptr;
+  Done *h_done = nullptr, *d_done = nullptr;
 
   // The context may already be closed (closing it synchronised its stream),
   // so only the device is used here.
@@ -132,9 +155,12 @@ struct smg_server {
     for (void *p : {static_cast<void *>(pool_mem), static_cast<void *>(d_fq_new), static_cast<void *>(d_jq),
                     static_cast<void *>(d_cnt), static_cast<void *>(d_seed), static_cast<void *>(tasks[0]),
                     static_cast<void *>(tasks[1]), static_cast<void *>(ready[0]), static_cast<void *>(ready[1]),
-                    static_cast<void *>(carry), static_cast<void *>(carry_count), static_cast<void *>(qs),
-                    static_cast<void *>(walk_count), static_cast<void *>(walk_items)})
+                    static_cast<void *>(next_count), static_cast<void *>(qs), static_cast<void *>(walk_count),
+                    static_cast<void *>(walk_items)})
       if (p) cudaFree(p);
+    for (void *p : {static_cast<void *>(h_cnt), static_cast<void *>(h_qs), static_cast<void *>(h_bell),
+                    static_cast<void *>(h_done)})
+      if (p) cudaFreeHost(p);
     if (ev) cudaEventDestroy(ev);
   }
 };
@@ -176,17 +202,15 @@ smg::JoinLaunch join_launch(smg_server *s) {
   jl.donate_min = 2;
   jl.time_limit_ns = smg::time_limit_ns();
   jl.slice_ns = s->slice_ns;
-  jl.carry = s->carry;
-  jl.carry_cap = s->carry_cap;
-  jl.carry_count = s->carry_count;
+  jl.slice_min_ns = s->slice_min_ns;
+  jl.bell = s->d_bell;
+  jl.next_tasks = s->tasks[1 - s->cur];
+  jl.next_ready = s->ready[1 - s->cur];
+  jl.next_count = s->next_count;
   return jl;
 }
 
-bool any_active(const smg_server *s) {
-  for (const Slot &sl : s->slots)
-    if (sl.used) return true;
-  return false;
-}
+bool any_active(const smg_server *s) { return s->free_slots < s->slots.size(); }
 
 // Empty queue: head = tail = pending = 0, every ready flag clear.
 smg_status reset_queue(smg_server *s) {
@@ -194,7 +218,7 @@ smg_status reset_queue(smg_server *s) {
   SMG_CUDA(cudaMemsetAsync(s->qs, 0, sizeof(smg::QueueState), st));
   SMG_CUDA(cudaMemsetAsync(s->ready[0], 0, static_cast<size_t>(s->cap) * 4, st));
   SMG_CUDA(cudaMemsetAsync(s->ready[1], 0, static_cast<size_t>(s->cap) * 4, st));
-  SMG_CUDA(cudaMemsetAsync(s->carry_count, 0, sizeof(unsigned int), st));
+  SMG_CUDA(cudaMemsetAsync(s->next_count, 0, sizeof(unsigned int), st));
   s->cur = 0;
   return SMG_OK;
 }
@@ -209,54 +233,57 @@ void retire(smg_server *s, Slot &sl, smg_status status, uint64_t count) {
   s->done[sl.ticket] = r;
   s->pool.release(sl.off, sl.size);
   sl = Slot();
+  ++s->free_slots;
 }
 
-// After a slice: read every slot's counters, retire finished queries, and
-// rebuild the queue from untaken and carried-over tasks.
-smg_status finish_slice(smg_server *s) {
+// Retires the requests whose completion records the join has published.
+void poll_done(smg_server *s) {
+  for (Slot &sl : s->slots) {
+    if (!sl.used) continue;
+    const uint32_t i = static_cast<uint32_t>(&sl - s->slots.data());
+    if (__atomic_load_n(&s->h_done[i].gen, __ATOMIC_ACQUIRE) != sl.gen) continue;
+    retire(s, sl, SMG_OK, __atomic_load_n(&s->h_done[i].count, __ATOMIC_RELAXED));
+  }
+}
+
+// While a slice runs: ring the doorbell once requests wait and enough slots
+// are free to admit them in a batch (an eighth of the slots), or any slot is
+// free and the slice has run 10 ms, so that the slice closes and the next one
+// admits them.  (The device closes a slice no earlier than SMG_SLICE_MIN_MS.)
+void maybe_ring(smg_server *s) {
+  if (s->bell_rung || s->waiting.empty() || s->free_slots == 0) return;
+  const uint32_t want = std::max<uint32_t>(1, static_cast<uint32_t>(s->slots.size()) / 8);
+  if (s->free_slots >= want || now_s() - s->slice_start_s > 0.010) {
+    __atomic_store_n(s->h_bell, 1u, __ATOMIC_RELEASE);
+    s->bell_rung = true;
+  }
+}
+
+// After a slice: move untaken and preempted tasks into the other queue (on
+// the device; the one just run becomes the next preemption target).
+smg_status end_slice(smg_server *s) {
   cudaStream_t st = s->ctx->stream;
-  smg::QueueState hq;
-  SMG_CUDA(cudaMemcpyAsync(s->h_cnt.data(), s->d_cnt, s->h_cnt.size() * sizeof(smg::QCounters),
-                           cudaMemcpyDeviceToHost, st));
-  SMG_CUDA(cudaMemcpyAsync(&hq, s->qs, sizeof(hq), cudaMemcpyDeviceToHost, st));
-  SMG_CUDA(cudaStreamSynchronize(st));
-  if (hq.error) {
-    for (Slot &sl : s->slots)
-      if (sl.used) retire(s, sl, SMG_ERR_TIMEOUT, 0);
-    return reset_queue(s);
-  }
-  for (size_t i = 0; i < s->slots.size(); ++i) {
-    Slot &sl = s->slots[i];
-    if (sl.used && s->h_cnt[i].pending == 0) retire(s, sl, SMG_OK, s->h_cnt[i].count);
-  }
-  if (!any_active(s)) return reset_queue(s);
   const uint32_t other = 1 - s->cur;
-  const uint32_t n_old = static_cast<uint32_t>(std::min<unsigned long long>(hq.tail.v, s->cap));
-  SMG_CUDA(cudaMemsetAsync(s->ready[other], 0, static_cast<size_t>(s->cap) * 4, st));
-  smg_status rc = smg::launch_compact(s->tasks[s->cur], s->ready[s->cur], n_old, s->carry, s->carry_count,
-                                      s->carry_cap, task_words(), s->tasks[other], s->ready[other], s->qs, st);
+  smg_status rc = smg::launch_compact(s->tasks[s->cur], s->ready[s->cur], s->cap, task_words(), s->tasks[other],
+                                      s->ready[other], s->next_count, s->qs, st, s->ctx->num_sms);
   if (rc) return rc;
-  SMG_CUDA(cudaMemsetAsync(s->carry_count, 0, sizeof(unsigned int), st));
+  SMG_CUDA(cudaMemsetAsync(s->ready[s->cur], 0, static_cast<size_t>(s->cap) * 4, st));
   s->cur = other;
   return SMG_OK;
 }
 
 // Admit waiting requests (arrival order) while slots and memory allow; filter
-// them together and append their root tasks to the live queue.
+// them together and append their root tasks to the live queue.  Only
+// enqueues: the caller synchronises once for admission and read-back.
 smg_status admit(smg_server *s) {
   const smg::DevGraph &g = s->graph->g;
   cudaStream_t st = s->ctx->stream;
   std::vector<uint32_t> fresh;
   std::vector<smg::QueryFootprint> fps;
   const double t = now_s();
-  while (!s->waiting.empty()) {
-    uint32_t idx = smg::kNone;
-    for (uint32_t i = 0; i < s->slots.size(); ++i)
-      if (!s->slots[i].used) {
-        idx = i;
-        break;
-      }
-    if (idx == smg::kNone) break;
+  uint32_t idx = 0;
+  while (!s->waiting.empty() && s->free_slots) {
+    while (s->slots[idx].used) ++idx;
     const Request &r = s->waiting.front();
     const smg::QueryFootprint fp = smg::query_footprint(g, *r.plan);
     size_t off = 0;
@@ -264,11 +291,13 @@ smg_status admit(smg_server *s) {
     Slot &sl = s->slots[idx];
     sl.used = true;
     sl.ticket = r.ticket;
+    sl.gen = ++s->next_gen;
     sl.plan = r.plan;
     sl.off = off;
     sl.size = fp.total();
     sl.submit_s = r.submit_s;
     sl.start_s = t;
+    --s->free_slots;
     s->waiting.pop_front();
     fresh.push_back(idx);
     fps.push_back(fp);
@@ -288,6 +317,7 @@ smg_status admit(smg_server *s) {
     b.enc = reinterpret_cast<uint32_t *>(base + fps[i].vmask);
     b.cand = reinterpret_cast<uint32_t *>(base + fps[i].vmask + fps[i].enc);
     b.roots = reinterpret_cast<uint32_t *>(base + fps[i].vmask + fps[i].enc + fps[i].cand);
+    b.cbits = reinterpret_cast<uint32_t *>(base + fps[i].vmask + fps[i].enc + fps[i].cand + fps[i].roots);
     b.counters = s->d_cnt + idx;
     smg_status rc = smg::make_query_records(*sl.plan, g, b, 0, hf[i], hj[i]);
     if (rc) return rc;
@@ -296,6 +326,9 @@ smg_status admit(smg_server *s) {
       hj[i].root_chunk = tune.root_chunk;
       hj[i].donate_min = tune.donate_min;
     }
+    hj[i].done_count = &s->d_done[idx].count;
+    hj[i].done_gen = &s->d_done[idx].gen;
+    hj[i].gen = sl.gen;
     rc = smg::append_filter_steps(*sl.plan, i, fb);
     if (rc) return rc;
     hseed[i] = idx;
@@ -313,21 +346,49 @@ smg_status admit(smg_server *s) {
   smg::JoinLaunch jl = join_launch(s);
   jl.seed_list = s->d_seed;
   jl.seed_n = n;
-  rc = smg::launch_seed(jl, st);
+  rc = smg::launch_join_prep(jl, st, s->ctx->num_sms);
   if (rc) return rc;
-  // the pinned staging is reused by the next admission: finish the copies
+  return smg::launch_seed(jl, st);
+}
+
+// Between slices: admit, read every slot's counters and the queue state back
+// (one synchronisation, which also releases the admission's pinned staging),
+// retire what finished (queries without root candidates never run a task),
+// and fail every active request if the join reported an error.
+smg_status settle(smg_server *s) {
+  cudaStream_t st = s->ctx->stream;
+  smg_status rc = admit(s);
+  if (rc) return rc;
+  SMG_CUDA(cudaMemcpyAsync(s->h_cnt, s->d_cnt, s->slots.size() * sizeof(smg::QCounters), cudaMemcpyDeviceToHost,
+                           st));
+  SMG_CUDA(cudaMemcpyAsync(s->h_qs, s->qs, sizeof(smg::QueueState), cudaMemcpyDeviceToHost, st));
   SMG_CUDA(cudaStreamSynchronize(st));
+  poll_done(s);
+  if (s->h_qs->error) {
+    const smg_status why = s->h_qs->error == smg::JOIN_ERR_QUEUE_FULL ? SMG_ERR_LIMIT : SMG_ERR_TIMEOUT;
+    for (Slot &sl : s->slots)
+      if (sl.used) retire(s, sl, why, 0);
+    return reset_queue(s);
+  }
+  for (size_t i = 0; i < s->slots.size(); ++i) {
+    Slot &sl = s->slots[i];
+    if (sl.used && s->h_cnt[i].pending == 0) retire(s, sl, SMG_OK, s->h_cnt[i].count);
+  }
+  if (!any_active(s)) return reset_queue(s);
   return SMG_OK;
 }
 
 smg_status launch_slice(smg_server *s) {
   cudaStream_t st = s->ctx->stream;
+  __atomic_store_n(s->h_bell, 0u, __ATOMIC_RELEASE);
+  s->bell_rung = false;
   smg_status rc = smg::launch_slice_begin(s->qs, st);
   if (rc) return rc;
   rc = smg::launch_join_only(join_launch(s), st, s->ctx->num_sms);
   if (rc) return rc;
   SMG_CUDA(cudaEventRecord(s->ev, st));
   s->inflight = true;
+  s->slice_start_s = now_s();
   ++s->slices;
   return SMG_OK;
 }
@@ -336,16 +397,28 @@ smg_status step(smg_server *s) {
   SMG_CUDA(cudaSetDevice(s->ctx->device));
   if (s->inflight) {
     const cudaError_t e = cudaEventQuery(s->ev);
-    if (e == cudaErrorNotReady) return SMG_OK;
+    if (e == cudaErrorNotReady) {
+      poll_done(s);
+      maybe_ring(s);
+      return SMG_OK;
+    }
     if (e != cudaSuccess) return smg::cuda_fail(e, "server slice");
     s->inflight = false;
-    smg_status rc = finish_slice(s);
+    smg_status rc = end_slice(s);
     if (rc) return rc;
+  } else if (s->waiting.empty() && !any_active(s)) {
+    return SMG_OK;  // idle
   }
-  smg_status rc = admit(s);
+  smg_status rc = settle(s);
   if (rc) return rc;
   if (any_active(s)) return launch_slice(s);
   return SMG_OK;
+}
+
+double env_ms(const char *name, double dflt) {
+  const char *v = std::getenv(name);
+  const double x = v ? std::atof(v) : dflt;
+  return x > 0 ? x : dflt;
 }
 
 }  // namespace
@@ -367,31 +440,37 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   size_t free_b = 0, total_b = 0;
   SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
   if (!s->cfg.memory_budget_bytes) s->cfg.memory_budget_bytes = std::min<size_t>(32ull << 30, free_b / 3);
-  const char *sl = std::getenv("SMG_SLICE_MS");
-  s->slice_ns = static_cast<uint64_t>((sl ? std::atof(sl) : 2.0) * 1e6);
-  if (!s->slice_ns) s->slice_ns = 2000000;
+  s->slice_ns = static_cast<uint64_t>(env_ms("SMG_SLICE_MS", 250.0) * 1e6);
+  s->slice_min_ns = std::min(s->slice_ns, static_cast<uint64_t>(env_ms("SMG_SLICE_MIN_MS", 2.0) * 1e6));
   s->cap = 2u << 20;
-  s->carry_cap = 1u << 20;
   const size_t tw = task_words();
+  const uint32_t m = s->cfg.max_inflight;
   SMG_CUDA(cudaMalloc(&s->pool_mem, s->cfg.memory_budget_bytes));
   s->pool.init(s->pool_mem, s->cfg.memory_budget_bytes);
-  SMG_CUDA(cudaMalloc(&s->d_fq_new, s->cfg.max_inflight * sizeof(smg::FilterQuery)));
-  SMG_CUDA(cudaMalloc(&s->d_jq, s->cfg.max_inflight * sizeof(smg::JoinQuery)));
-  SMG_CUDA(cudaMalloc(&s->d_cnt, s->cfg.max_inflight * sizeof(smg::QCounters)));
-  SMG_CUDA(cudaMalloc(&s->d_seed, s->cfg.max_inflight * sizeof(uint32_t)));
+  SMG_CUDA(cudaMalloc(&s->d_fq_new, m * sizeof(smg::FilterQuery)));
+  SMG_CUDA(cudaMalloc(&s->d_jq, m * sizeof(smg::JoinQuery)));
+  SMG_CUDA(cudaMalloc(&s->d_cnt, m * sizeof(smg::QCounters)));
+  SMG_CUDA(cudaMalloc(&s->d_seed, m * sizeof(uint32_t)));
   for (int i = 0; i < 2; ++i) {
     SMG_CUDA(cudaMalloc(&s->tasks[i], static_cast<size_t>(s->cap) * tw * 4));
     SMG_CUDA(cudaMalloc(&s->ready[i], static_cast<size_t>(s->cap) * 4));
   }
-  SMG_CUDA(cudaMalloc(&s->carry, static_cast<size_t>(s->carry_cap) * tw * 4));
-  SMG_CUDA(cudaMalloc(&s->carry_count, sizeof(unsigned int)));
+  SMG_CUDA(cudaMalloc(&s->next_count, sizeof(unsigned int)));
   SMG_CUDA(cudaMalloc(&s->qs, sizeof(smg::QueueState)));
   SMG_CUDA(cudaMalloc(&s->walk_count, smg::kMaxWalkPhases * 2 * sizeof(unsigned int)));
   SMG_CUDA(cudaMalloc(&s->walk_items, static_cast<size_t>(smg::kWalkCap) * sizeof(uint4)));
-  SMG_CUDA(cudaMemsetAsync(s->d_cnt, 0, s->cfg.max_inflight * sizeof(smg::QCounters), c->stream));
+  SMG_CUDA(cudaHostAlloc(&s->h_cnt, m * sizeof(smg::QCounters), cudaHostAllocDefault));
+  SMG_CUDA(cudaHostAlloc(&s->h_qs, sizeof(smg::QueueState), cudaHostAllocDefault));
+  SMG_CUDA(cudaHostAlloc(&s->h_bell, sizeof(uint32_t), cudaHostAllocMapped));
+  SMG_CUDA(cudaHostAlloc(&s->h_done, m * sizeof(Done), cudaHostAllocMapped));
+  SMG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_bell), s->h_bell, 0));
+  SMG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_done), s->h_done, 0));
+  *s->h_bell = 0;
+  std::memset(s->h_done, 0, m * sizeof(Done));
+  SMG_CUDA(cudaMemsetAsync(s->d_cnt, 0, m * sizeof(smg::QCounters), c->stream));
   SMG_CUDA(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming));
-  s->slots.resize(s->cfg.max_inflight);
-  s->h_cnt.resize(s->cfg.max_inflight);
+  s->slots.resize(m);
+  s->free_slots = m;
   smg_status rc = reset_queue(s.get());
   if (rc) return rc;
   SMG_CUDA(cudaStreamSynchronize(c->stream));
@@ -446,7 +525,8 @@ smg_status smg_server_drain(smg_server *s) {
   while (s->inflight || !s->waiting.empty() || any_active(s)) {
     smg_status rc = step(s);
     if (rc) return rc;
-    if (s->inflight) SMG_CUDA(cudaEventSynchronize(s->ev));
+    // completions and the doorbell are served while the slice runs
+    if (s->inflight) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
   return SMG_OK;
 }

@@ -171,3 +171,35 @@ def test_batch_graph_replay(ctx, er):
     direct, _ = native.match_batch(ctx, dev, plans, use_graph=False)
     assert first.tolist() == again.tolist() == profiled.tolist() == after.tolist() == direct.tolist()
     assert st.join_ms > 0 and st.kernel_launches > 0
+
+
+PLAN_ORDER_SCRIPT = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+from clustersm_gb300 import native
+from clustersm_gb300.native import Context, DeviceGraph, Plan
+from clustersm_gb300.workloads import load
+wl = load("er1k")
+qs, want, _ = wl.queries()
+ctx = Context(0)
+dev = DeviceGraph(ctx, wl.graph())
+counts, _ = native.match_batch(ctx, dev, [Plan(q) for q in qs])
+bad = [i for i, (c, w) in enumerate(zip(counts.tolist(), want)) if int(c) != int(w)]
+print("mismatches", bad)
+sys.exit(1 if bad else 0)
+"""
+
+
+def test_reference_edge_order_gives_same_counts(ctx):
+    """SMG_JOIN_ORDER=plan matches vertices in the order the reference's edge
+    order (order.cpp getBFSEdgeOrder) reaches them instead of the cost-based
+    order; the counts are the same (the setting is read once per process)."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, SMG_JOIN_ORDER="plan")
+    r = subprocess.run([sys.executable, "-c", PLAN_ORDER_SCRIPT, str(root)], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -37,15 +37,18 @@ def test_alone_equals_in_mix(ctx, er):
     srv.close()
 
 
-def test_arrivals_while_running(ctx):
+@pytest.fixture(scope="module")
+def rmat22(ctx):
     wl = load("rmat22")
     try:
         qs, want, _ = wl.queries()
     except FileNotFoundError:
         pytest.skip("rmat22 workload not generated")
-    host = wl.graph()
-    dev = DeviceGraph(ctx, host)
-    plans = [Plan(q) for q in qs[:96]]
+    return DeviceGraph(ctx, wl.graph()), [Plan(q) for q in qs[:96]], want[:96]
+
+
+def test_arrivals_while_running(ctx, rmat22):
+    dev, plans, want = rmat22
     srv = Server(ctx, dev, max_inflight=32)
     tickets = []
     for i, p in enumerate(plans):
@@ -55,11 +58,34 @@ def test_arrivals_while_running(ctx):
     srv.drain()
     results = [srv.poll(tk) for tk in tickets]
     srv.close()
-    for r, w in zip(results, want[:96]):
+    for r, w in zip(results, want):
         assert r.status == 0 and r.count == w
     for p, w in list(zip(plans, want))[:8]:
         res, _ = native.match(ctx, dev, p)
         assert res.count == w
+
+
+@pytest.mark.parametrize("slice_ms,min_ms", [("0.3", "0.1"), ("250", "0.2")])
+def test_preempted_slices_keep_counts(ctx, rmat22, monkeypatch, slice_ms, min_ms):
+    """Sub-millisecond slices (every warp's stack is handed over to the next
+    queue hundreds of times) and doorbell-driven closings (arrivals while
+    slots are free) leave every count exact."""
+    dev, plans, want = rmat22
+    monkeypatch.setenv("SMG_SLICE_MS", slice_ms)
+    monkeypatch.setenv("SMG_SLICE_MIN_MS", min_ms)
+    srv = Server(ctx, dev, max_inflight=24)
+    tickets = []
+    for i, p in enumerate(plans):
+        tickets.append(srv.submit(p))
+        for _ in range(4):
+            srv.step()
+        if i % 16 == 15:
+            time.sleep(0.002)
+    srv.drain()
+    results = [srv.poll(tk) for tk in tickets]
+    srv.close()
+    assert [r.status for r in results] == [0] * len(plans)
+    assert [int(r.count) for r in results] == [int(w) for w in want]
 
 
 def test_cancel_and_budget(ctx, er):
