@@ -685,6 +685,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   st->scanned += hq->scanned;
   st->descents += hq->descents;
   st->probes += hq->probes;
+  st->last_count_entries += hq->last_count_entries;
   st->join_bytes += 8ull * hq->scanned + 8ull * hq->descents + 4ull * hq->probes + 8ull * hq->last_count_entries;
   if (o.profile) {
     float f = 0, j = 0;
@@ -827,6 +828,11 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
     stats->filter_bytes = st.filter_bytes;
     stats->join_bytes = st.join_bytes;
     stats->chunks = st.chunks;
+    stats->scanned = st.scanned;
+    stats->descents = st.descents;
+    stats->probes = st.probes;
+    stats->last_count_entries = st.last_count_entries;
+    stats->donations = st.donations;
   }
   return SMG_OK;
 }

@@ -71,7 +71,7 @@ struct QueryOut {
 
 struct RunStats {
   float filter_ms = 0, join_ms = 0;
-  uint64_t tasks = 0, donations = 0, scanned = 0, descents = 0, probes = 0;
+  uint64_t tasks = 0, donations = 0, scanned = 0, descents = 0, probes = 0, last_count_entries = 0;
   uint64_t filter_bytes = 0, join_bytes = 0;
   uint64_t launches = 0, h2d = 0, d2h = 0;
   uint32_t chunks = 0;

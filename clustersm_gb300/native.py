@@ -78,7 +78,9 @@ class BatchStats(C.Structure):
     _fields_ = [("filter_ms", C.c_float), ("join_ms", C.c_float), ("tasks", C.c_uint64),
                 ("total_embeddings", C.c_uint64), ("kernel_launches", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("d2h_bytes", C.c_uint64), ("filter_bytes", C.c_uint64), ("join_bytes", C.c_uint64),
-                ("chunks", C.c_uint32), ("reserved", C.c_uint32)]
+                ("chunks", C.c_uint32), ("reserved", C.c_uint32), ("scanned", C.c_uint64),
+                ("descents", C.c_uint64), ("probes", C.c_uint64), ("last_count_entries", C.c_uint64),
+                ("donations", C.c_uint64)]
 
 
 class TuneEntry(C.Structure):

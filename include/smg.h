@@ -268,6 +268,11 @@ typedef struct smg_batch_stats {
   uint64_t join_bytes;       /* algorithmic bytes of the joins             */
   uint32_t chunks;           /* memory-bounded sub-batches                 */
   uint32_t reserved;
+  uint64_t scanned;          /* join list entries tested                   */
+  uint64_t descents;         /* partial matches extended (and counted ends)*/
+  uint64_t probes;           /* membership probes (bitmap words, searches) */
+  uint64_t last_count_entries; /* list entries read to build last counts   */
+  uint64_t donations;        /* tasks split off to idle warps              */
 } smg_batch_stats;
 smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
                            const smg_plan *const *plans, uint32_t n,
