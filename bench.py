@@ -145,7 +145,7 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=512):
     for rate in rates:
         rng = random.Random(f"serve-{rate}")
         n = max(64, min(max_requests, int(rate * seconds)))
-        srv = Server(ctx, dev, max_inflight=256)
+        srv = Server(ctx, dev, max_inflight=512, memory_budget_bytes=64 << 30)
         tickets = []
         t_next = time.perf_counter()
         while len(tickets) < n:
@@ -156,6 +156,7 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=512):
             else:
                 srv.step()
         srv.drain()
+        ss = srv.stats()
         lat, ok, first, last = [], 0, None, None
         for tk, j in tickets:
             r = srv.poll(tk)
@@ -166,7 +167,8 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=512):
         srv.close()
         lat.sort()
         out.append({"offered_qps": rate, "requests": n, "p50_ms": lat[n // 2], "p99_ms": lat[(99 * (n - 1)) // 100],
-                    "sustained_qps": n / (last - first), "counts_ok": ok})
+                    "sustained_qps": n / (last - first), "counts_ok": ok, "slices": ss.slices, "bells": ss.bells,
+                    "retired_in_slice": ss.retired_in_slice, "slice_s": ss.slice_s, "between_s": ss.between_s})
     return out
 
 

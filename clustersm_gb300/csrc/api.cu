@@ -76,6 +76,19 @@ size_t hub_max_bytes() {
   return s ? static_cast<size_t>(std::atoll(s)) : (2ull << 30);
 }
 
+// Vertices of at least this degree get a label run table (the join scans
+// only the neighbours of the label it needs), up to 1 GB of tables.
+// SMG_LABEL_INDEX=0 leaves the index out (whole lists are scanned).
+uint32_t label_index_min_degree() {
+  const char *s = std::getenv("SMG_LABEL_INDEX_MIN_DEGREE");
+  return s ? static_cast<uint32_t>(std::atol(s)) : 64u;
+}
+
+bool label_index_enabled() {
+  const char *s = std::getenv("SMG_LABEL_INDEX");
+  return !(s && std::strcmp(s, "0") == 0);
+}
+
 void drop_graph(smg_ctx *c) {
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   c->graph_exec = nullptr;
@@ -219,6 +232,11 @@ smg_status smg_graph_upload(smg_ctx *c, const smg_csr *in, smg_graph **out) {
     st = build_hub_bitmaps(g, hub_min_degree(), hub_max_bytes(), c->stream, deg);
     if (st) return st;
   }
+  if (label_index_enabled()) {
+    // the id-ordered lists the device got (the caller's, or their sorted copy)
+    st = build_label_index(g, in->offsets, adj_src, in->labels, label_index_min_degree(), 1ull << 30, c->stream);
+    if (st) return st;
+  }
   SMG_CUDA(cudaStreamSynchronize(c->stream));
   G->device = c->device;
   *out = G.release();
@@ -235,6 +253,9 @@ void smg_graph_free(smg_graph *G) {
   if (g.nlc) cudaFree(g.nlc);
   if (g.hub_of) cudaFree(g.hub_of);
   if (g.hub_bits) cudaFree(g.hub_bits);
+  if (g.adjl) cudaFree(g.adjl);
+  if (g.lab_of) cudaFree(g.lab_of);
+  if (g.lab_off) cudaFree(g.lab_off);
   delete G;
 }
 
@@ -390,6 +411,10 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
   f.stat = b.counters->stat;
   j.k = P.k;
   j.candmask = b.vmask;
+  if (g.adjl) {
+    j.use_labels = 1;
+    for (uint32_t l = 0; l < P.k; ++l) j.level_bucket[l] = std::min(P.label[j.order[l]], g.lab_buckets - 1);
+  }
   if (b.cbits) {
     j.cbits = b.cbits;
     j.cwords = (g.n + 31ull) / 32;
@@ -560,6 +585,10 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
   jl.hub_of = g.hub_of;
   jl.hub_bits = g.hub_bits;
   jl.hub_words = g.hub_words;
+  jl.adjl = g.adjl;
+  jl.lab_of = g.lab_of;
+  jl.lab_off = g.lab_off;
+  jl.lab_buckets = g.lab_buckets;
   jl.n = g.n;
   jl.m2 = g.m2;
   jl.num_hubs = g.num_hubs;

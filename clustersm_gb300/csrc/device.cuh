@@ -51,6 +51,15 @@ struct DevGraph {
   uint32_t *hub_bits = nullptr;  // [num_hubs][hub_words]
   uint32_t num_hubs = 0;
   uint64_t hub_words = 0;
+  // Label index: every neighbour list again, ordered by (label bucket, id),
+  // where bucket(l) = min(l, lab_buckets - 1); and, for the vertices of high
+  // degree, where each bucket's run starts (relative to off[v]; lab_buckets + 1
+  // entries, the last = degree).  The join scans only the run of the label it
+  // needs; membership tests keep the id-ordered `adj`.
+  uint32_t *adjl = nullptr;     // [2|E|]
+  uint32_t *lab_of = nullptr;   // [n] row of the vertex's run table, or kNone
+  uint32_t *lab_off = nullptr;  // [indexed][lab_buckets + 1]
+  uint32_t lab_buckets = 0, lab_indexed = 0;
   std::vector<uint64_t> label_count;  // vertices per label (host copy)
   uint64_t bytes = 0;
 };
@@ -154,6 +163,10 @@ struct JoinQuery {
   unsigned long long *done_count;
   uint32_t *done_gen;
   uint32_t gen;
+  // Label bucket of each level's query vertex, for the label index (valid
+  // when use_labels is set; otherwise the join scans whole lists).
+  uint32_t level_bucket[kMaxK];
+  uint32_t use_labels;
   // 1 + the level of the last vertex's only back neighbour when the last
   // level can be counted from per-vertex neighbour counts (one back edge and
   // cbits present); 0: the last level is always scanned.

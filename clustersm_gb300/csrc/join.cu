@@ -35,7 +35,9 @@
 #include <cstdlib>
 #include <numeric>
 #include <string>
+#include <vector>
 
+#include "filter.cuh"  // kMaxLabels
 #include "join.cuh"
 
 namespace smg {
@@ -195,7 +197,11 @@ constexpr uint32_t kLastCountMaxDeg = 8192;
 __global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict__ queries,
                                                      const uint32_t *__restrict__ list, uint32_t nq,
                                                      const uint32_t *__restrict__ off,
-                                                     const uint32_t *__restrict__ adj, uint32_t n, QueueState *qs) {
+                                                     const uint32_t *__restrict__ adj,
+                                                     const uint32_t *__restrict__ adjl,
+                                                     const uint32_t *__restrict__ lab_of,
+                                                     const uint32_t *__restrict__ lab_off, uint32_t lab_buckets,
+                                                     uint32_t n, QueueState *qs) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
@@ -205,6 +211,7 @@ __global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict
     if (!Q.fast_last) continue;
     const uint32_t ub = Q.order[Q.fast_last - 1], ul = Q.order[Q.k - 1];
     const uint32_t *row = Q.cbits + ul * Q.cwords;
+    const uint32_t bk = Q.level_bucket[Q.k - 1];
     uint32_t *cnt = Q.lastcnt;
     for (uint64_t v0 = static_cast<uint64_t>(warp) * 32; v0 < n; v0 += static_cast<uint64_t>(nwarps) * 32) {
       const uint64_t v = v0 + lane;
@@ -212,14 +219,27 @@ __global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict
       for (uint32_t bal = __ballot_sync(0xFFFFFFFFu, (mine >> ub) & 1u); bal; bal &= bal - 1) {
         const uint32_t src = __ffs(bal) - 1;
         const uint64_t x = v0 + src;
-        const uint32_t beg = __ldg(off + x), end = __ldg(off + x + 1);
+        // the neighbours of x with the last vertex's label bucket (its run
+        // when x has a run table, else the whole list)
+        uint32_t beg = __ldg(off + x), end = __ldg(off + x + 1);
+        const uint32_t *lst = adj;
+        if (Q.use_labels) {
+          const uint32_t li = __ldg(lab_of + x);
+          if (li != kNone) {
+            const uint32_t *t = lab_off + static_cast<uint64_t>(li) * (lab_buckets + 1) + bk;
+            const uint32_t lo = __ldg(t), hi = __ldg(t + 1);
+            lst = adjl;
+            end = beg + hi;
+            beg += lo;
+          }
+        }
         uint32_t c = kNone;
         if (end - beg <= kLastCountMaxDeg) {
           uint32_t part = 0;
           for (uint32_t e = beg + lane; e < end; e += 128) {
             uint32_t w[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) w[i] = e + 32 * i < end ? __ldg(adj + e + 32 * i) : kNone;
+            for (int i = 0; i < 4; ++i) w[i] = e + 32 * i < end ? __ldg(lst + e + 32 * i) : kNone;
 #pragma unroll
             for (int i = 0; i < 4; ++i)
               if (w[i] != kNone && SMG_DCHECK(w[i] < n, 120, w[i], x)) part += (__ldg(row + (w[i] >> 5)) >> (w[i] & 31)) & 1u;
@@ -263,14 +283,16 @@ __device__ __forceinline__ bool is_neighbor(const JoinLaunch &p, uint32_t beg, u
 //   piv           level whose matched vertex's list feeds this level
 //   ord, bmask, slab  the task's query: vertex, backward-edge mask and
 //                 same-label mask per level
+//   lbk           the task's query: label bucket per level (label index)
 //   lbase         base pointer of the level's source list
 //   batch         [K][32] tested candidates
-//   seg*          per-candidate segments of the segmented last level
-__host__ __device__ inline uint32_t scalar_words(uint32_t K) { return (12 * K + 1) & ~1u; }
+//   seg*          per-candidate segments of the segmented last level; bit 31
+//                 of spiv marks a segment read from the label-ordered lists
+__host__ __device__ inline uint32_t scalar_words(uint32_t K) { return (13 * K + 1) & ~1u; }
 __host__ __device__ inline uint32_t warp_words(uint32_t K) { return scalar_words(K) + 2 * K + 32 * K + 7 * 32; }
 
 struct WarpView {
-  uint32_t *m, *beg, *deg, *hub, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *batch;
+  uint32_t *m, *beg, *deg, *hub, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *lbk, *batch;
   uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv;
   const uint32_t **lbase;
   __device__ WarpView(uint32_t *W, uint32_t K) {
@@ -286,6 +308,7 @@ struct WarpView {
     ord = W + 9 * K;
     bmask = W + 10 * K;
     slab = W + 11 * K;
+    lbk = W + 12 * K;
     const uint32_t s = scalar_words(K);
     lbase = reinterpret_cast<const uint32_t **>(W + s);
     batch = W + s + 2 * K;
@@ -298,6 +321,34 @@ struct WarpView {
     spiv = spre + 32;
   }
 };
+
+constexpr uint32_t kFromLabelIndex = 1u << 31;  // spiv flag: segment in adjl
+
+// Self-checking build: does `e` point into adj or adjl?
+__device__ __forceinline__ bool in_lists(const JoinLaunch &p, const uint32_t *e) {
+  return (e >= p.adj && e < p.adj + p.m2) || (p.adjl && e >= p.adjl && e < p.adjl + p.m2);
+}
+
+// The list that level `level` scans: the neighbours of matched vertex x (its
+// id-ordered list starts at beg and holds deg entries), narrowed to the run
+// of the level's label bucket when x has a run table.  Every path that
+// derives a level's list (task start, descent, last level, split slices)
+// calls this, so a task's [lo, hi) means the same entries to every warp.
+__device__ __forceinline__ const uint32_t *scan_list(const JoinLaunch &p, const WarpView &S, bool use_labels,
+                                                     uint32_t level, uint32_t x, uint32_t beg, uint32_t deg,
+                                                     uint32_t &len) {
+  if (use_labels) {
+    const uint32_t li = __ldg(p.lab_of + x);
+    if (li != kNone) {
+      const uint32_t *t = p.lab_off + static_cast<uint64_t>(li) * (p.lab_buckets + 1) + S.lbk[level];
+      const uint32_t lo = __ldg(t);
+      len = __ldg(t + 1) - lo;
+      return p.adjl + beg + lo;
+    }
+  }
+  len = deg;
+  return p.adj + beg;
+}
 
 __device__ __forceinline__ uint32_t choose_pivot(const WarpView &S, uint32_t level) {
   uint32_t best = 0, bd = 0xFFFFFFFFu;
@@ -378,10 +429,11 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
       piv = j;
     }
   }
-  hi = min(hi, bd);
+  uint32_t len = 0;
+  const uint32_t *base = scan_list(p, S, Q.use_labels, L, S.m[piv], S.beg[piv], S.deg[piv], len);
+  hi = min(hi, len);
   if (lo >= hi) return 0;
   scanned += hi - lo;
-  const uint32_t *base = p.adj + S.beg[piv];
   const uint32_t u = S.ord[L], back = S.bmask[L] & ~(1u << piv), same = S.slab[L];
   const uint32_t lt = (1u << lane) - 1;
   unsigned long long cnt = 0;
@@ -430,43 +482,59 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   if (lane < bc) {
     uint32_t v = S.batch[P * 32 + lane];
     if (!SMG_DCHECK(v < p.n, 106, v, P)) v = 0;
-    const uint32_t vb = __ldg(p.off + v), vd = __ldg(p.off + v + 1) - vb;
-    uint32_t piv = 0, bd = 0xFFFFFFFFu;
-    for (uint32_t b = S.bmask[L]; b; b &= b - 1) {
-      const uint32_t j = __ffs(b) - 1;
-      const uint32_t d = j == P ? vd : S.deg[j];
-      if (d < bd) {
-        bd = d;
-        piv = j;
-      }
-    }
-    len = bd;
+    bool counted = false;
     if (fast_ok) {
-      // one back edge (to level piv): the stored neighbour count of its vertex
+      // one back edge, to level fb: the stored neighbour count of its vertex
       // a, less the matched vertices of the last vertex's label adjacent to a
-      const uint32_t a = piv == P ? v : S.m[piv];
+      const uint32_t fb = Q.fast_last - 1;
+      const uint32_t a = fb == P ? v : S.m[fb];
       const uint32_t c = __ldg(Q.lastcnt + a);
       if (c != kNone) {
-        const uint32_t ab = piv == P ? vb : S.beg[piv], ad = piv == P ? vd : S.deg[piv];
-        const uint32_t ah = piv == P ? __ldg(p.hub_of + v) : S.hub[piv];
-        const uint32_t u = S.ord[L];
         uint32_t corr = 0;
-        for (uint32_t b = S.slab[L]; b; b &= b - 1) {
-          const uint32_t j = __ffs(b) - 1;
-          const uint32_t x = j == P ? v : S.m[j];
-          if (x != a && cv.has(u, x) && is_neighbor(p, ab, ad, ah, x, probes)) ++corr;
+        if (S.slab[L]) {
+          uint32_t ab, ad, ah;
+          if (fb == P) {
+            ab = __ldg(p.off + v);
+            ad = __ldg(p.off + v + 1) - ab;
+            ah = __ldg(p.hub_of + v);
+          } else {
+            ab = S.beg[fb];
+            ad = S.deg[fb];
+            ah = S.hub[fb];
+          }
+          const uint32_t u = S.ord[L];
+          for (uint32_t b = S.slab[L]; b; b &= b - 1) {
+            const uint32_t j = __ffs(b) - 1;
+            const uint32_t x = j == P ? v : S.m[j];
+            if (x != a && cv.has(u, x) && is_neighbor(p, ab, ad, ah, x, probes)) ++corr;
+          }
         }
         fast = c - corr;
-        len = 0;
+        counted = true;  // a zero-length segment: the scan below never visits it
       }
     }
-    if (len > kSplitLen) len = split_last(S, p, Q, q, P, v, len);
-    S.sv[lane] = v;
-    S.sbeg[lane] = vb;
-    S.sdeg[lane] = vd;
-    S.shub[lane] = __ldg(p.hub_of + v);
-    S.sbase[lane] = piv == P ? vb : S.beg[piv];
-    S.spiv[lane] = piv;
+    if (!counted) {
+      const uint32_t vb = __ldg(p.off + v), vd = __ldg(p.off + v + 1) - vb;
+      uint32_t piv = 0, bd = 0xFFFFFFFFu;
+      for (uint32_t b = S.bmask[L]; b; b &= b - 1) {
+        const uint32_t j = __ffs(b) - 1;
+        const uint32_t d = j == P ? vd : S.deg[j];
+        if (d < bd) {
+          bd = d;
+          piv = j;
+        }
+      }
+      const uint32_t pb = piv == P ? vb : S.beg[piv];
+      const uint32_t *lst = scan_list(p, S, Q.use_labels, L, piv == P ? v : S.m[piv], pb, bd, len);
+      const bool from_l = lst != p.adj + pb;
+      if (len > kSplitLen) len = split_last(S, p, Q, q, P, v, len);
+      S.sv[lane] = v;
+      S.sbeg[lane] = vb;
+      S.sdeg[lane] = vd;
+      S.shub[lane] = __ldg(p.hub_of + v);
+      S.sbase[lane] = static_cast<uint32_t>(lst - (from_l ? p.adjl : p.adj));
+      S.spiv[lane] = piv | (from_l ? kFromLabelIndex : 0u);
+    }
   }
   uint32_t incl = len;
   for (int o = 1; o < 32; o <<= 1) {
@@ -497,14 +565,15 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       const uint32_t vi = S.sv[i];
       const uint64_t ai = static_cast<uint64_t>(S.sbase[i]) + (t - S.spre[i]);
       const bool in_adj = SMG_DCHECK(ai < p.m2, 107, ai, i);
-      w = in_adj ? __ldg(p.adj + ai) : 0u;
+      const uint32_t sp = S.spiv[i];
+      w = in_adj ? __ldg(((sp & kFromLabelIndex) ? p.adjl : p.adj) + ai) : 0u;
       good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) && cv.has(u, w);
       for (uint32_t b = same; b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
         good = (j == P ? vi : S.m[j]) != w;
       }
       // back edges other than the pivot's (whose list w comes from)
-      for (uint32_t b = back & ~(1u << S.spiv[i]); b && good; b &= b - 1) {
+      for (uint32_t b = back & ~(1u << (sp & 31u)); b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
         if (j == P)
           good = is_neighbor(p, S.sbeg[i], S.sdeg[i], S.shub[i], w, probes);
@@ -724,6 +793,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       S.ord[lane] = Q.order[lane];
       S.bmask[lane] = Q.back_mask[lane];
       S.slab[lane] = Q.same_label[lane];
+      S.lbk[lane] = Q.level_bucket[lane];
     }
     if (lane < L0) {
       uint32_t v = __ldcg(T + 4 + lane);
@@ -748,13 +818,16 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     if (lane == 0) {
       if (L0 == 0) {
         S.lbase[0] = Q.roots;
+        S.cur[L0] = lo;
+        S.end[L0] = hi;
       } else {
         const uint32_t pv = choose_pivot(S, L0);
+        uint32_t len = 0;
         S.piv[L0] = pv;
-        S.lbase[L0] = p.adj + S.beg[pv];
+        S.lbase[L0] = scan_list(p, S, Q.use_labels, L0, S.m[pv], S.beg[pv], S.deg[pv], len);
+        S.cur[L0] = lo;
+        S.end[L0] = hi == kNone ? len : min(hi, len);
       }
-      S.cur[L0] = lo;
-      S.end[L0] = (hi == kNone && L0 > 0) ? S.deg[S.piv[L0]] : hi;
       S.bcnt[L0] = 0;
       S.bidx[L0] = 0;
     }
@@ -858,10 +931,11 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
           const uint32_t nl = level + 1;
           if (lane == 0) {
             const uint32_t pv = choose_pivot(S, nl);
+            uint32_t len = 0;
             S.piv[nl] = pv;
-            S.lbase[nl] = p.adj + S.beg[pv];
+            S.lbase[nl] = scan_list(p, S, Q.use_labels, nl, S.m[pv], S.beg[pv], S.deg[pv], len);
             S.cur[nl] = 0;
-            S.end[nl] = S.deg[pv];
+            S.end[nl] = len;
             S.bcnt[nl] = 0;
             S.bidx[nl] = 0;
           }
@@ -881,7 +955,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         bool good = false;
         uint32_t w = 0;
         if (lane < n && SMG_DCHECK(level == 0 ? c + lane < *Q.num_roots
-                                                : static_cast<uint64_t>(base - p.adj) + c + lane < p.m2,
+                                                : in_lists(p, base + c + lane),
                                    114, c + lane, level)) {
           w = __ldg(base + c + lane);
           good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, cv, level, w, probes));
@@ -928,13 +1002,16 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
 }
 
 // The join is bound by the latency of its scattered reads, so it trades
-// registers for resident warps: 6 blocks (48 warps) per SM at 40 registers
-// and a small spill.  On the 2^22 R-MAT workload that is 19% faster than 4
-// blocks at 64 registers (the compiler's own choice, 80 registers, fits 3).
-// SMG_JOIN_OCCUPANCY=mid selects 4 blocks, =max 8 blocks (32 registers).
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_join(JoinLaunch p) { join_body(p); }
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4) k_join_mid(JoinLaunch p) { join_body(p); }
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 8) k_join_max(JoinLaunch p) { join_body(p); }
+// registers for resident warps.  On the 2^22 R-MAT workload (scanning whole
+// lists), 8 blocks of 8 warps per SM (32 registers, a 476-byte spill)
+// measured 501 queries/s, 6 blocks (40 registers) 426 and 4 blocks (64
+// registers) 357; the compiler's own choice, 80 registers, fits 3.  With the
+// label index, 6 and 8 blocks run at the same speed and 6 spills less (its
+// local-memory traffic reaches DRAM), so 6 is the default.  A launch takes
+// the most blocks its shared memory allows; SMG_JOIN_OCCUPANCY=4|6|8 caps it.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 8) k_join(JoinLaunch p) { join_body(p); }
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_join6(JoinLaunch p) { join_body(p); }
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4) k_join4(JoinLaunch p) { join_body(p); }
 
 __global__ void k_slice_begin(QueueState *qs) {
   qs->start_ns = now_ns();
@@ -1019,18 +1096,28 @@ namespace {
 
 using JoinKernel = void (*)(JoinLaunch);
 
-JoinKernel join_kernel() {
-  static const JoinKernel k = [] {
+uint32_t occupancy_cap() {
+  static const uint32_t cap = [] {
     const char *e = std::getenv("SMG_JOIN_OCCUPANCY");
-    const std::string v = e ? e : "";
-    return v == "mid" ? k_join_mid : v == "max" ? k_join_max : k_join;
+    const int v = e ? std::atoi(e) : 6;
+    return static_cast<uint32_t>(v >= 8 ? 8 : v >= 6 ? 6 : 4);
   }();
-  return k;
+  return cap;
+}
+
+// The variant whose register budget matches the blocks that fit: 8 or 6 only
+// when that many blocks' shared memory fits an SM.
+JoinKernel join_kernel(size_t smem_per_block) {
+  const size_t sm_bytes = 227 * 1024;
+  const uint32_t cap = occupancy_cap();
+  if (cap >= 8 && 8 * (smem_per_block + 1024) <= sm_bytes) return k_join;
+  if (cap >= 6 && 6 * (smem_per_block + 1024) <= sm_bytes) return k_join6;
+  return k_join4;
 }
 
 smg_status launch_persistent(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
-  const JoinKernel kern = join_kernel();
+  const JoinKernel kern = join_kernel(smem);
   if (smem > 48 * 1024)
     SMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
@@ -1070,7 +1157,8 @@ smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   if (jl.emit) return SMG_OK;
   const uint32_t span = static_cast<uint32_t>((static_cast<uint64_t>(jl.n) + 255) / 256);  // 32 vertices a warp
   const dim3 g2(std::min(span, want), std::min<uint32_t>(nq, 65535));
-  k_last_counts<<<g2, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.off, jl.adj, jl.n, jl.qs);
+  k_last_counts<<<g2, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.off, jl.adj, jl.adjl, jl.lab_of, jl.lab_off,
+                                    jl.lab_buckets, jl.n, jl.qs);
   SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }
@@ -1080,6 +1168,63 @@ smg_status launch_seed(const JoinLaunch &jl, cudaStream_t s) {
   if (!n) return SMG_OK;
   k_seed<<<(n + 127) / 128, 128, 0, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
+
+smg_status build_label_index(DevGraph &g, const uint64_t *offsets, const uint32_t *adj, const uint32_t *labels,
+                             uint32_t min_degree, size_t max_bytes, cudaStream_t s) {
+  const uint32_t n = g.n;
+  g.lab_buckets = std::max<uint32_t>(1, std::min<uint32_t>(g.num_labels, kMaxLabels));
+  const uint32_t B = g.lab_buckets;
+  if (!n || !g.m2) return SMG_OK;
+  auto bucket = [&](uint32_t w) { return std::min(labels[w], B - 1); };
+  // lists ordered by (bucket, id): a stable counting pass per vertex over the
+  // id-ordered list keeps ids ascending within a bucket
+  std::vector<uint32_t> adjl(g.m2);
+#pragma omp parallel
+  {
+    std::vector<uint32_t> cnt(B + 1);
+#pragma omp for schedule(dynamic, 1024)
+    for (int64_t v = 0; v < static_cast<int64_t>(n); ++v) {
+      const uint64_t a = offsets[v], b = offsets[v + 1];
+      if (b - a < 2) {
+        if (b > a) adjl[a] = adj[a];
+        continue;
+      }
+      std::fill(cnt.begin(), cnt.end(), 0u);
+      for (uint64_t e = a; e < b; ++e) ++cnt[bucket(adj[e]) + 1];
+      for (uint32_t i = 0; i < B; ++i) cnt[i + 1] += cnt[i];
+      for (uint64_t e = a; e < b; ++e) adjl[a + cnt[bucket(adj[e])]++] = adj[e];
+    }
+  }
+  // run tables for the highest-degree vertices
+  std::vector<uint32_t> cand;
+  for (uint32_t v = 0; v < n; ++v)
+    if (offsets[v + 1] - offsets[v] >= std::max<uint32_t>(min_degree, 1)) cand.push_back(v);
+  std::stable_sort(cand.begin(), cand.end(),
+                   [&](uint32_t x, uint32_t y) { return offsets[x + 1] - offsets[x] > offsets[y + 1] - offsets[y]; });
+  const size_t row = static_cast<size_t>(B + 1) * 4;
+  if (cand.size() > max_bytes / row) cand.resize(max_bytes / row);
+  g.lab_indexed = static_cast<uint32_t>(cand.size());
+  std::vector<uint32_t> lab_of(n, kNone), lab_off(std::max<size_t>(cand.size(), 1) * (B + 1));
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < static_cast<int64_t>(cand.size()); ++i) {
+    const uint32_t v = cand[i];
+    lab_of[v] = static_cast<uint32_t>(i);
+    uint32_t *t = lab_off.data() + static_cast<size_t>(i) * (B + 1);
+    std::fill(t, t + B + 1, 0u);
+    const uint64_t a = offsets[v], b = offsets[v + 1];
+    for (uint64_t e = a; e < b; ++e) ++t[bucket(adj[e]) + 1];
+    for (uint32_t j = 0; j < B; ++j) t[j + 1] += t[j];  // t[j] = start of bucket j, t[B] = degree
+  }
+  SMG_CUDA(cudaMalloc(&g.adjl, g.m2 * 4));
+  SMG_CUDA(cudaMalloc(&g.lab_of, static_cast<size_t>(n) * 4));
+  SMG_CUDA(cudaMalloc(&g.lab_off, lab_off.size() * 4));
+  SMG_CUDA(cudaMemcpyAsync(g.adjl, adjl.data(), g.m2 * 4, cudaMemcpyHostToDevice, s));
+  SMG_CUDA(cudaMemcpyAsync(g.lab_of, lab_of.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, s));
+  SMG_CUDA(cudaMemcpyAsync(g.lab_off, lab_off.data(), lab_off.size() * 4, cudaMemcpyHostToDevice, s));
+  SMG_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  g.bytes += g.m2 * 4 + static_cast<size_t>(n) * 4 + lab_off.size() * 4;
   return SMG_OK;
 }
 

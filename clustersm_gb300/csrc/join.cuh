@@ -39,6 +39,9 @@ struct JoinLaunch {
   const uint32_t *hub_of;    // [n] hub index or kNone
   const uint32_t *hub_bits;  // [hubs][hub_words] neighbour bitmaps of hubs
   uint64_t hub_words;
+  const uint32_t *adjl;      // label index (DevGraph::adjl, lab_of, lab_off)
+  const uint32_t *lab_of, *lab_off;
+  uint32_t lab_buckets;
   uint32_t n;                // data vertices (bounds of the self-checking build)
   uint64_t m2;               // adjacency entries
   uint32_t num_hubs;
@@ -95,6 +98,11 @@ smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, 
 // neighbour, how many neighbours of v are candidates of the last vertex.
 // launch_join runs it itself.
 smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms);
+// Label index of a resident graph (DevGraph::adjl, lab_of, lab_off) from the
+// host's id-ordered lists: vertices of degree >= min_degree get a run table,
+// highest degree first, up to max_bytes of tables.
+smg_status build_label_index(DevGraph &g, const uint64_t *offsets, const uint32_t *adj, const uint32_t *labels,
+                             uint32_t min_degree, size_t max_bytes, cudaStream_t s);
 // Neighbour bitmaps of the highest-degree vertices (degree >= min_degree,
 // at most max_bytes of bitmaps), built once per resident graph.
 smg_status build_hub_bitmaps(DevGraph &g, uint32_t min_degree, size_t max_bytes, cudaStream_t s,

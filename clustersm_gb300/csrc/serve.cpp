@@ -137,6 +137,7 @@ struct smg_server {
   cudaEvent_t ev = nullptr;
   bool inflight = false, bell_rung = false;
   double slice_start_s = 0;
+  smg_server_stats stats{};
   uint64_t slices = 0;
   smg::FilterDev fdev;
   // page-locked host memory: counters and queue state read back between
@@ -188,6 +189,10 @@ smg::JoinLaunch join_launch(smg_server *s) {
   jl.hub_of = g.hub_of;
   jl.hub_bits = g.hub_bits;
   jl.hub_words = g.hub_words;
+  jl.adjl = g.adjl;
+  jl.lab_of = g.lab_of;
+  jl.lab_off = g.lab_off;
+  jl.lab_buckets = g.lab_buckets;
   jl.n = g.n;
   jl.m2 = g.m2;
   jl.num_hubs = g.num_hubs;
@@ -243,6 +248,7 @@ void poll_done(smg_server *s) {
     const uint32_t i = static_cast<uint32_t>(&sl - s->slots.data());
     if (__atomic_load_n(&s->h_done[i].gen, __ATOMIC_ACQUIRE) != sl.gen) continue;
     retire(s, sl, SMG_OK, __atomic_load_n(&s->h_done[i].count, __ATOMIC_RELAXED));
+    if (s->inflight) ++s->stats.retired_in_slice;
   }
 }
 
@@ -256,6 +262,7 @@ void maybe_ring(smg_server *s) {
   if (s->free_slots >= want || now_s() - s->slice_start_s > 0.010) {
     __atomic_store_n(s->h_bell, 1u, __ATOMIC_RELEASE);
     s->bell_rung = true;
+    ++s->stats.bells;
   }
 }
 
@@ -298,6 +305,7 @@ smg_status admit(smg_server *s) {
     sl.submit_s = r.submit_s;
     sl.start_s = t;
     --s->free_slots;
+    ++s->stats.admitted;
     s->waiting.pop_front();
     fresh.push_back(idx);
     fps.push_back(fp);
@@ -363,6 +371,7 @@ smg_status settle(smg_server *s) {
                            st));
   SMG_CUDA(cudaMemcpyAsync(s->h_qs, s->qs, sizeof(smg::QueueState), cudaMemcpyDeviceToHost, st));
   SMG_CUDA(cudaStreamSynchronize(st));
+  s->stats.carried_tasks += s->h_qs->tail.v;  // the queue the next slice starts with
   poll_done(s);
   if (s->h_qs->error) {
     const smg_status why = s->h_qs->error == smg::JOIN_ERR_QUEUE_FULL ? SMG_ERR_LIMIT : SMG_ERR_TIMEOUT;
@@ -404,15 +413,18 @@ smg_status step(smg_server *s) {
     }
     if (e != cudaSuccess) return smg::cuda_fail(e, "server slice");
     s->inflight = false;
+    s->stats.slice_s += now_s() - s->slice_start_s;
     smg_status rc = end_slice(s);
     if (rc) return rc;
   } else if (s->waiting.empty() && !any_active(s)) {
     return SMG_OK;  // idle
   }
+  const double t0 = now_s();
   smg_status rc = settle(s);
   if (rc) return rc;
-  if (any_active(s)) return launch_slice(s);
-  return SMG_OK;
+  if (any_active(s)) rc = launch_slice(s);
+  s->stats.between_s += now_s() - t0;
+  return rc;
 }
 
 double env_ms(const char *name, double dflt) {
@@ -439,7 +451,7 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   if (s->cfg.max_inflight * per_rec > smg::kPinnedBytes) return fail(SMG_ERR_LIMIT, "max_inflight too large");
   size_t free_b = 0, total_b = 0;
   SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  if (!s->cfg.memory_budget_bytes) s->cfg.memory_budget_bytes = std::min<size_t>(32ull << 30, free_b / 3);
+  if (!s->cfg.memory_budget_bytes) s->cfg.memory_budget_bytes = std::min<size_t>(64ull << 30, free_b / 3);
   s->slice_ns = static_cast<uint64_t>(env_ms("SMG_SLICE_MS", 250.0) * 1e6);
   s->slice_min_ns = std::min(s->slice_ns, static_cast<uint64_t>(env_ms("SMG_SLICE_MIN_MS", 2.0) * 1e6));
   s->cap = 2u << 20;
@@ -528,6 +540,13 @@ smg_status smg_server_drain(smg_server *s) {
     // completions and the doorbell are served while the slice runs
     if (s->inflight) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
+  return SMG_OK;
+}
+
+smg_status smg_server_get_stats(const smg_server *s, smg_server_stats *out) {
+  if (!s || !out) return fail(SMG_ERR_INVALID, "null argument");
+  *out = s->stats;
+  out->slices = s->slices;
   return SMG_OK;
 }
 

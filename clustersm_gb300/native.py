@@ -97,6 +97,12 @@ class ServerConfig(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_inflight", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("slices", C.c_uint64), ("bells", C.c_uint64), ("admitted", C.c_uint64),
+                ("retired_in_slice", C.c_uint64), ("carried_tasks", C.c_uint64), ("slice_s", C.c_double),
+                ("between_s", C.c_double)]
+
+
 class RequestResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("reserved", C.c_uint32), ("count", C.c_uint64),
                 ("submit_s", C.c_double), ("start_s", C.c_double), ("finish_s", C.c_double)]
@@ -151,6 +157,7 @@ def _load():
         "smg_server_drain": (st, [vp]),
         "smg_server_step": (st, [vp]),
         "smg_server_destroy": (None, [vp]),
+        "smg_server_get_stats": (st, [vp, C.POINTER(ServerStats)]),
     }
     sig.update(dev)
     for name, (res, args) in sig.items():
@@ -472,6 +479,11 @@ class Server:
 
     def step(self):
         check(lib.smg_server_step(self._h), "smg_server_step")
+
+    def stats(self) -> ServerStats:
+        out = ServerStats()
+        check(lib.smg_server_get_stats(self._h, C.byref(out)), "smg_server_get_stats")
+        return out
 
     def poll(self, ticket: int):
         """RequestResult, or None while the request is queued or running."""

@@ -355,6 +355,18 @@ smg_status smg_server_cancel(smg_server *s, uint64_t ticket);
 smg_status smg_server_drain(smg_server *s);
 /* Make progress once without blocking (admit, launch, retire). */
 smg_status smg_server_step(smg_server *s);
+/* Counters since creation (host clock for the times). */
+typedef struct smg_server_stats {
+  uint64_t slices;          /* join slices launched                          */
+  uint64_t bells;           /* slices the doorbell asked to end early        */
+  uint64_t admitted;        /* requests admitted                             */
+  uint64_t retired_in_slice;/* requests retired from completion records     */
+  uint64_t carried_tasks;   /* tasks moved into the next slice's queue       */
+  double slice_s;           /* time from a slice's launch to its end seen    */
+  double between_s;         /* time between slices (compaction, admission,
+                               read-back) with requests active or waiting    */
+} smg_server_stats;
+smg_status smg_server_get_stats(const smg_server *s, smg_server_stats *out);
 void smg_server_destroy(smg_server *s);
 
 #ifdef __cplusplus

@@ -83,7 +83,9 @@ def test_preempted_slices_keep_counts(ctx, rmat22, monkeypatch, slice_ms, min_ms
             time.sleep(0.002)
     srv.drain()
     results = [srv.poll(tk) for tk in tickets]
+    ss = srv.stats()
     srv.close()
+    assert ss.admitted == len(plans) and ss.slices >= 1
     assert [r.status for r in results] == [0] * len(plans)
     assert [int(r.count) for r in results] == [int(w) for w in want]
 
