@@ -416,6 +416,8 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
     for (uint32_t l = 0; l < P.k; ++l) j.level_bucket[l] = std::min(P.label[j.order[l]], g.lab_buckets - 1);
   }
   if (b.cbits) {
+    f.cbits = b.cbits;  // k_collect writes them with the final masks
+    f.cwords = (g.n + 31ull) / 32;
     j.cbits = b.cbits;
     j.cwords = (g.n + 31ull) / 32;
     j.lastcnt = b.vmask;
@@ -707,7 +709,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
       }
     st->filter_bytes += 12ull * g.n + lab * (8 + 32) + 8ull * q.initial_cands + 8ull * q.walk_entries +
                         4ull * q.num_roots;
-    st->join_bytes += 4ull * g.n + cbits_bytes(g, P.k);  // candidate bitmaps: masks read, rows written
+    st->filter_bytes += cbits_bytes(g, P.k);  // candidate bitmap rows written by collect
   }
   st->tasks += hq->tasks_done;
   st->donations += hq->donations;
@@ -738,10 +740,20 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
                        QueryOut *out, RunStats *st) {
   SMG_CUDA(cudaSetDevice(c->device));
   if (o.emb_host && nq != 1) return fail(SMG_ERR_INVALID, "embeddings are returned by the plain path only");
-  size_t free_b = 0, total_b = 0;
-  SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const size_t budget = c->arena.cap + (free_b > kHeadroomBytes ? free_b - kHeadroomBytes : free_b / 2);
   const size_t per_chunk_fixed = (64ull << 20) * 4;  // queue storage of a chunk (bound)
+  // device memory is asked for only when the batch may not fit the arena
+  // (cudaMemGetInfo is a driver round trip, too slow for every plain call)
+  size_t need = per_chunk_fixed;
+  for (uint32_t i = 0; i < nq && need <= c->arena.cap; ++i) {
+    uint64_t ct;
+    need += query_bytes(g, *plans[i], ct);
+  }
+  size_t budget = c->arena.cap;
+  if (need > c->arena.cap) {
+    size_t free_b = 0, total_b = 0;
+    SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    budget += free_b > kHeadroomBytes ? free_b - kHeadroomBytes : free_b / 2;
+  }
   const size_t max_q = kPinnedBytes / (sizeof(FilterQuery) + sizeof(JoinQuery) + sizeof(QCounters));
   uint32_t a = 0;
   while (a < nq) {

@@ -98,6 +98,12 @@ struct StepGroup {
   uint32_t query;        // index into the batch
   uint32_t core;
   uint32_t first, count; // steps [first, first+count) of the step array
+  // Labels of the query vertices whose slots the group's steps set or test on
+  // neighbours (one byte each, nlab of them; nlab = 0: too many, walk whole
+  // lists).  Only neighbours with these labels can change, so a candidate
+  // with a label run table walks just those runs.
+  uint32_t nlab;
+  uint8_t lab[4];
 };
 
 // Per-query device state (filter scratch and join inputs).
@@ -125,6 +131,8 @@ struct FilterQuery {
   uint32_t *vmask, *enc, *cand, *cand_cnt, *roots, *num_roots;
   uint64_t root_cap;             // entries `roots` can hold
   unsigned long long *stat;       // [0] sum over u of final |C(u)|, [1] walk list entries
+  uint32_t *cbits;               // the join's candidate bitmaps, written by collect (null: none)
+  uint64_t cwords;               // words per bitmap row, ceil(n / 32)
 };
 
 // Query-side constants the join reads.

@@ -179,6 +179,41 @@ __device__ __forceinline__ void walk_neighbors(const uint32_t *__restrict__ adj,
   }
 }
 
+// Walks neighbours [e0, e1) of candidate v in `arr` (the id-ordered lists,
+// or the label-ordered ones when from_l): the first kWalkChunk entries here,
+// the rest queued for the chunk pass, one warp per chunk.
+__device__ __forceinline__ void walk_span(const uint32_t *__restrict__ arr, bool from_l, uint32_t gi, uint32_t v,
+                                          uint32_t pass, uint32_t e0, uint32_t e1, const StepGroup &G,
+                                          const ClusterStep *__restrict__ steps, const uint32_t *__restrict__ aux,
+                                          const FilterQuery &Q, uint32_t kind, uint32_t lane,
+                                          const WalkOverflow &ov) {
+  uint32_t mine = e1;
+  if (e1 - e0 > kWalkChunk) {
+    const uint32_t extra = (e1 - e0 - 1) / kWalkChunk;
+    uint32_t base = kNone;
+    if (lane == 0) {
+      unsigned int old = *(volatile unsigned int *)ov.count;
+      while (old + extra <= ov.cap) {
+        const unsigned int seen = atomicCAS(ov.count, old, old + extra);
+        if (seen == old) {
+          base = old;
+          break;
+        }
+        old = seen;
+      }
+    }
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base != kNone) {
+      const uint32_t tag = gi | (from_l ? 0x80000000u : 0u);
+      for (uint32_t c = lane; c < extra; c += 32)
+        if (SMG_DCHECK(base + c < ov.cap, 205, base + c, ov.cap))
+          ov.items[base + c] = make_uint4(tag, v, pass, e0 + (c + 1) * kWalkChunk);
+      mine = e0 + kWalkChunk;
+    }
+  }
+  walk_neighbors(arr, G, steps, aux, Q, kind, pass, e0, mine, lane, ov.n);
+}
+
 __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict__ off,
                                                       const uint32_t *__restrict__ adj,
                                                       const StepGroup *__restrict__ groups, uint32_t group_base,
@@ -233,31 +268,20 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
     if (kind != 2 && pass == 0) continue;
     const uint32_t e0 = off[v], e1 = off[v + 1];
     if (!SMG_DCHECK(e0 <= e1 && e1 <= ov.m2, 204, e0, e1)) continue;
-    scanned += e1 - e0;
-    uint32_t mine = e1;
-    if (e1 - e0 > kWalkChunk) {
-      // hand the tail of a long list to the chunk pass, one warp per chunk
-      const uint32_t extra = (e1 - e0 - 1) / kWalkChunk;
-      uint32_t base = kNone;
-      if (lane == 0) {
-        unsigned int old = *(volatile unsigned int *)ov.count;
-        while (old + extra <= ov.cap) {
-          const unsigned int seen = atomicCAS(ov.count, old, old + extra);
-          if (seen == old) {
-            base = old;
-            break;
-          }
-          old = seen;
-        }
+    const uint32_t li = (G.nlab && ov.adjl) ? __ldg(ov.lab_of + v) : kNone;
+    if (li != kNone) {
+      // only neighbours with the group's labels can change: walk their runs
+      const uint32_t *t = ov.lab_off + static_cast<uint64_t>(li) * (ov.lab_buckets + 1);
+      for (uint32_t i = 0; i < G.nlab; ++i) {
+        const uint32_t b = min(static_cast<uint32_t>(G.lab[i]), ov.lab_buckets - 1);
+        const uint32_t r0 = e0 + __ldg(t + b), r1 = e0 + __ldg(t + b + 1);
+        scanned += r1 - r0;
+        walk_span(ov.adjl, true, gi, v, pass, r0, r1, G, steps, aux, Q, kind, lane, ov);
       }
-      base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      if (base != kNone) {
-        for (uint32_t c = lane; c < extra; c += 32)
-          if (SMG_DCHECK(base + c < ov.cap, 205, base + c, ov.cap)) ov.items[base + c] = make_uint4(gi, v, pass, e0 + (c + 1) * kWalkChunk);
-        mine = e0 + kWalkChunk;
-      }
+    } else {
+      scanned += e1 - e0;
+      walk_span(adj, false, gi, v, pass, e0, e1, G, steps, aux, Q, kind, lane, ov);
     }
-    walk_neighbors(adj, G, steps, aux, Q, kind, pass, e0, mine, lane, ov.n);
   }
   if (lane == 0 && scanned) atomicAdd(Q.stat + 1, scanned);
 }
@@ -274,12 +298,16 @@ __global__ void __launch_bounds__(256) k_walk_chunks(const uint32_t *__restrict_
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
     const uint4 it = ov.items[i];
-    if (!SMG_DCHECK(it.x < ov.num_groups && it.y < ov.n && it.w < ov.m2, 206, i, it.x)) continue;
-    const StepGroup G = groups[it.x];
+    const uint32_t gi = it.x & 0x7FFFFFFFu;
+    if (!SMG_DCHECK(gi < ov.num_groups && it.y < ov.n && it.w < ov.m2, 206, i, it.x)) continue;
+    const StepGroup G = groups[gi];
     const FilterQuery &Q = qs[G.query];
     const uint32_t kind = steps[G.first].kind;
+    // a chunk of a label run may run past the run's end into the vertex's
+    // next runs: those neighbours carry none of the group's labels, so their
+    // slots do not change
     const uint32_t e1 = min(it.w + kWalkChunk, off[it.y + 1]);
-    walk_neighbors(adj, G, steps, aux, Q, kind, it.z, it.w, e1, lane, ov.n);
+    walk_neighbors((it.x >> 31) ? ov.adjl : adj, G, steps, aux, Q, kind, it.z, it.w, e1, lane, ov.n);
   }
 }
 
@@ -310,6 +338,17 @@ __global__ void __launch_bounds__(256) k_collect(uint32_t n, const FilterQuery *
       }
       if (m0 != cm) vmask[v] = cm;
       ncand += __popc(cm);
+    }
+    // the join's candidate bitmaps: the warp's 32 consecutive vertices give
+    // one word of each query vertex's row
+    const uint32_t v0 = base + (threadIdx.x & ~31u);  // the warp's first vertex (uniform)
+    if (Q.cbits && v0 < n) {
+      uint32_t mine = 0;
+      for (uint32_t u = 0; u < Q.k; ++u) {
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, (cm >> u) & 1u);
+        if (lane == u) mine = b;
+      }
+      if (lane < Q.k) Q.cbits[lane * Q.cwords + v0 / 32] = mine;
     }
     const bool is_root = (cm >> root) & 1u;
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, is_root);
@@ -397,6 +436,33 @@ extern "C" int smg_debug_check_filter(unsigned long long *out) {
 }
 #endif
 
+// Adds the labels of cluster c's neighbour slots to a group's label set
+// (nlab = 0 once more than four distinct labels are needed).
+static void add_neighbor_labels(const Plan &P, uint32_t c, StepGroup &g, bool &overflow) {
+  for (uint32_t s = P.cl_off[c] + 1; s < P.cl_off[c + 1] && !overflow; ++s) {
+    const uint32_t l = P.label[P.slots[s]];
+    bool have = false;
+    for (uint32_t i = 0; i < g.nlab; ++i) have |= g.lab[i] == l;
+    if (have) continue;
+    if (g.nlab == 4 || l >= kMaxLabels) {
+      overflow = true;
+    } else {
+      g.lab[g.nlab++] = static_cast<uint8_t>(l);
+    }
+  }
+  if (overflow) g.nlab = 0;
+}
+
+static StepGroup make_group(uint32_t qi, uint32_t core, uint32_t first, uint32_t count) {
+  StepGroup g;
+  std::memset(&g, 0, sizeof(g));
+  g.query = qi;
+  g.core = core;
+  g.first = first;
+  g.count = count;
+  return g;
+}
+
 smg_status append_filter_steps(const Plan &P, uint32_t qi, FilterBatch &fb) {
   const uint32_t phases = 2 * P.num_layers - 1;
   if (fb.phases.size() < phases) fb.phases.resize(phases);
@@ -414,7 +480,10 @@ smg_status append_filter_steps(const Plan &P, uint32_t qi, FilterBatch &fb) {
   // phase 0: stars of layer 0, one group each
   for (uint32_t c = P.layer_begin[0]; c < P.layer_begin[1]; ++c) {
     ClusterStep st = base_step(c, 0);
-    fb.phases[0].push_back({qi, st.core, static_cast<uint32_t>(fb.steps.size()), 1});
+    StepGroup g = make_group(qi, st.core, static_cast<uint32_t>(fb.steps.size()), 1);
+    bool over = false;
+    add_neighbor_labels(P, c, g, over);
+    fb.phases[0].push_back(g);
     fb.steps.push_back(st);
   }
   for (uint32_t layer = 1; layer < P.num_layers; ++layer) {
@@ -428,8 +497,10 @@ smg_status append_filter_steps(const Plan &P, uint32_t qi, FilterBatch &fb) {
       by_core[core].push_back(c);
     }
     for (uint32_t core : cores) {
-      StepGroup gr{qi, core, static_cast<uint32_t>(fb.steps.size()), 0};
+      StepGroup gr = make_group(qi, core, static_cast<uint32_t>(fb.steps.size()), 0);
+      bool over = false;
       for (uint32_t c : by_core[core]) {
+        add_neighbor_labels(P, c, gr, over);
         const int64_t r = merge_of[c];
         if (r < 0) return fail(SMG_ERR_INTERNAL, "merge cluster without a merge record");
         ClusterStep st = base_step(c, 1);
@@ -465,7 +536,10 @@ smg_status append_filter_steps(const Plan &P, uint32_t qi, FilterBatch &fb) {
             }
         ++st.num_targets;
       }
-      fb.phases[2 * layer].push_back({qi, st.core, static_cast<uint32_t>(fb.steps.size()), 1});
+      StepGroup g = make_group(qi, st.core, static_cast<uint32_t>(fb.steps.size()), 1);
+      bool over = false;
+      add_neighbor_labels(P, rec.out, g, over);
+      fb.phases[2 * layer].push_back(g);
       fb.steps.push_back(st);
     }
   }
@@ -543,6 +617,10 @@ smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const Filter
     po.n = g.n;
     po.m2 = g.m2;
     po.num_groups = fd.phase_count[p];
+    po.adjl = g.adjl;
+    po.lab_of = g.lab_of;
+    po.lab_off = g.lab_off;
+    po.lab_buckets = g.lab_buckets;
     const uint32_t wx = std::max<uint32_t>(1, std::min<uint32_t>(2048, (num_sms * 16u + ng - 1) / ng));
     for (uint32_t y0 = 0; y0 < ng; y0 += 65535) {
       const uint32_t ny = std::min<uint32_t>(65535, ng - y0);

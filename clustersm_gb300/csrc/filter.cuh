@@ -15,13 +15,17 @@ constexpr uint32_t kWalkChunk = 2048;
 // Chunks of long neighbour lists queued by one walk phase for the chunk pass.
 // `count` points at this phase's counter (zeroed before the run; the walk
 // launcher gives each phase its own); items are (group, vertex, passed-step
-// mask, first adjacency index).
+// mask, first adjacency index).  Bit 31 of an item's group marks an index
+// into the label-ordered lists (adjl) rather than the id-ordered ones.
 struct WalkOverflow {
   unsigned int *count;
   uint32_t cap;
   uint4 *items;
   uint32_t n, num_groups;  // data vertices and the phase's step groups (bounds checks)
   uint64_t m2;             // adjacency entries
+  // the graph's label index (set by launch_walks; adjl null: none)
+  const uint32_t *adjl, *lab_of, *lab_off;
+  uint32_t lab_buckets;
 };
 
 // Steps of the cluster bitmap for a batch of queries, grouped into phases:

@@ -99,34 +99,50 @@ __device__ int wait_ticket(const JoinLaunch &p, unsigned long long ticket, uint6
   }
 }
 
-__global__ void k_seed(JoinLaunch p) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) p.qs->start_ns = now_ns();
+// One block per seeded query: thread 0 reserves the query's root tasks (one
+// per chunk of root candidates) at the queue's tail, then every thread writes
+// and publishes its share of them (a query may have tens of thousands).
+__global__ void __launch_bounds__(256) k_seed(JoinLaunch p) {
+  __shared__ unsigned long long s_first;
+  __shared__ uint32_t s_nt, s_chunk, s_nr;
+  if (blockIdx.y == 0 && threadIdx.x == 0) p.qs->start_ns = now_ns();
   const uint32_t nseed = p.seed_list ? p.seed_n : p.nq;
-  for (uint32_t si = blockIdx.x * blockDim.x + threadIdx.x; si < nseed; si += gridDim.x * blockDim.x) {
+  const uint32_t tw = 4 + p.kmax;
+  for (uint32_t si = blockIdx.y; si < nseed; si += gridDim.y) {
     const uint32_t q = p.seed_list ? p.seed_list[si] : si;
-    const uint32_t nr = *p.queries[q].num_roots;
-    if (nr == 0) continue;
-    const uint32_t rc = p.queries[q].root_chunk ? p.queries[q].root_chunk : p.root_chunk;
-    uint32_t chunk = rc ? rc : 1;
-    chunk = max(chunk, (nr + p.max_seed_tasks - 1) / p.max_seed_tasks);
-    const uint32_t nt = (nr + chunk - 1) / chunk;
-    const unsigned long long first = atomicAdd(&p.qs->tail.v, static_cast<unsigned long long>(nt));
-    const uint32_t tw = 4 + p.kmax;
-    if (first + nt > p.cap) {  // no room: the run fails (batches size the queue for every seed)
-      set_error(p.qs, JOIN_ERR_QUEUE_FULL);
-      continue;
+    if (threadIdx.x == 0) {
+      const uint32_t nr = *p.queries[q].num_roots;
+      const uint32_t rc = p.queries[q].root_chunk ? p.queries[q].root_chunk : p.root_chunk;
+      uint32_t chunk = rc ? rc : 1, nt = 0;
+      unsigned long long first = 0;
+      if (nr) {
+        chunk = max(chunk, (nr + p.max_seed_tasks - 1) / p.max_seed_tasks);
+        nt = (nr + chunk - 1) / chunk;
+        first = atomicAdd(&p.qs->tail.v, static_cast<unsigned long long>(nt));
+        if (first + nt > p.cap) {  // no room: the run fails (batches size the queue for every seed)
+          set_error(p.qs, JOIN_ERR_QUEUE_FULL);
+          nt = 0;
+        } else {
+          atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
+          atomicAdd(p.queries[q].pending, static_cast<unsigned long long>(nt));
+        }
+      }
+      s_first = first;
+      s_nt = nt;
+      s_chunk = chunk;
+      s_nr = nr;
     }
-    atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
-    atomicAdd(p.queries[q].pending, static_cast<unsigned long long>(nt));
-    for (uint32_t i = 0; i < nt; ++i) {
-      uint32_t *t = p.tasks + (first + i) * tw;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < s_nt; i += blockDim.x) {
+      uint32_t *t = p.tasks + (s_first + i) * tw;
       t[0] = q;
       t[1] = 0;
-      t[2] = i * chunk;
-      t[3] = min(nr, (i + 1) * chunk);
+      t[2] = i * s_chunk;
+      t[3] = min(s_nr, (i + 1) * s_chunk);
+      __threadfence();
+      p.ready[s_first + i] = 1;
     }
-    __threadfence();
-    for (uint32_t i = 0; i < nt; ++i) p.ready[first + i] = 1;
+    __syncthreads();  // the shared values are rewritten for the next query
   }
 }
 
@@ -152,32 +168,6 @@ struct CandView {
     return (__ldg(mask + w) >> u) & 1u;
   }
 };
-
-// Builds a query's candidate bitmaps from its final masks: a warp reads 32
-// consecutive masks (one coalesced line) and one ballot per query vertex is
-// that vertex's bitmap word.
-__global__ void __launch_bounds__(256) k_cand_bits(const JoinQuery *__restrict__ queries,
-                                                   const uint32_t *__restrict__ list, uint32_t nq, uint32_t n) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t qi = blockIdx.y; qi < nq; qi += gridDim.y) {
-    const JoinQuery &Q = queries[list ? list[qi] : qi];
-    if (!Q.cbits) continue;
-    const uint32_t k = Q.k;
-    const uint64_t words = Q.cwords;
-    for (uint64_t wi = warp; wi < words; wi += nwarps) {
-      const uint64_t v = wi * 32 + lane;
-      const uint32_t m = v < n ? __ldg(Q.candmask + v) : 0u;
-      uint32_t mine = 0;
-      for (uint32_t u = 0; u < k; ++u) {
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, (m >> u) & 1u);
-        if (lane == u) mine = b;
-      }
-      if (lane < k) Q.cbits[lane * words + wi] = mine;
-    }
-  }
-}
 
 // Last-level counts.  In a count-only run, when the last query vertex u_L
 // has a single edge back to the matched prefix (to level b), the last level
@@ -254,17 +244,34 @@ __global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict
   if (lane == 0 && read) atomicAdd(&qs->last_count_entries, read);
 }
 
-// Is w in the neighbour list (beg, deg) of a matched vertex?  `hub` selects
-// its bitmap when it has one.
-__device__ __forceinline__ bool is_neighbor(const JoinLaunch &p, uint32_t beg, uint32_t deg, uint32_t hub,
-                                            uint32_t w, uint32_t &probes) {
-  if (hub != kNone && SMG_DCHECK(hub < p.num_hubs, 102, hub, p.num_hubs) && SMG_DCHECK(w < p.n, 103, w, p.n)) {
+// Is w in the neighbour list of matched vertex x (id-ordered list at beg,
+// deg entries)?  `hub` selects x's bitmap when it has one.  With
+// p.probe_runs, a vertex with a label run table is searched in its run of
+// w's label bucket instead (bucket: that of the level w is a candidate for,
+// kNone when the query has no label index): a short sorted range that all
+// lanes of a warp search together, in place of a random bitmap word.
+__device__ __forceinline__ bool is_neighbor(const JoinLaunch &p, uint32_t x, uint32_t beg, uint32_t deg,
+                                            uint32_t hub, uint32_t bucket, uint32_t w, uint32_t &probes) {
+  const uint32_t *a = p.adj + beg;
+  uint32_t len = deg;
+  bool run = false;
+  if (p.probe_runs && bucket != kNone) {
+    const uint32_t li = __ldg(p.lab_of + x);
+    if (li != kNone) {
+      const uint32_t *t = p.lab_off + static_cast<uint64_t>(li) * (p.lab_buckets + 1) + bucket;
+      const uint32_t r0 = __ldg(t);
+      len = __ldg(t + 1) - r0;
+      a = p.adjl + beg + r0;
+      run = true;
+    }
+  }
+  if (!run && hub != kNone && SMG_DCHECK(hub < p.num_hubs, 102, hub, p.num_hubs) &&
+      SMG_DCHECK(w < p.n, 103, w, p.n)) {
     ++probes;
     return (__ldg(p.hub_bits + hub * p.hub_words + (w >> 5)) >> (w & 31)) & 1u;
   }
   if (!SMG_DCHECK(static_cast<uint64_t>(beg) + deg <= p.m2, 104, beg, deg)) return false;
-  const uint32_t *a = p.adj + beg;
-  uint32_t lo = 0, hi = deg;
+  uint32_t lo = 0, hi = len;
   while (lo < hi) {
     ++probes;
     const uint32_t mid = (lo + hi) >> 1;
@@ -273,7 +280,7 @@ __device__ __forceinline__ bool is_neighbor(const JoinLaunch &p, uint32_t beg, u
     else
       hi = mid;
   }
-  return lo < deg && __ldg(a + lo) == w;
+  return lo < len && __ldg(a + lo) == w;
 }
 
 // Per-warp shared state, K = largest query of the launch:
@@ -350,12 +357,35 @@ __device__ __forceinline__ const uint32_t *scan_list(const JoinLaunch &p, const 
   return p.adj + beg;
 }
 
-__device__ __forceinline__ uint32_t choose_pivot(const WarpView &S, uint32_t level) {
+// Length of the list scan_list would give: the run of the level's label
+// bucket when x has a run table, else its degree.
+__device__ __forceinline__ uint32_t run_len(const JoinLaunch &p, const WarpView &S, bool use_labels,
+                                            uint32_t level, uint32_t x, uint32_t deg) {
+  if (use_labels) {
+    const uint32_t li = __ldg(p.lab_of + x);
+    if (li != kNone) {
+      const uint32_t *t = p.lab_off + static_cast<uint64_t>(li) * (p.lab_buckets + 1) + S.lbk[level];
+      return __ldg(t + 1) - __ldg(t);
+    }
+  }
+  return deg;
+}
+
+// The pivot of `level`: the back neighbour whose list scan_list gives is
+// shortest (ties to the lower level).  cand_level / cand_v / cand_deg stand
+// in for the matched vertex of cand_level (the last level's candidate, not
+// yet in S.m); pass kNone otherwise.  Every path that picks a level's pivot
+// calls this, so donor and receiver of a task pick the same list.
+__device__ __forceinline__ uint32_t choose_pivot(const JoinLaunch &p, const WarpView &S, bool use_labels,
+                                                 uint32_t level, uint32_t cand_level = kNone, uint32_t cand_v = 0,
+                                                 uint32_t cand_deg = 0) {
   uint32_t best = 0, bd = 0xFFFFFFFFu;
   for (uint32_t b = S.bmask[level]; b; b &= b - 1) {
     const uint32_t j = __ffs(b) - 1;
-    if (S.deg[j] < bd) {
-      bd = S.deg[j];
+    const uint32_t d = j == cand_level ? run_len(p, S, use_labels, level, cand_v, cand_deg)
+                                       : run_len(p, S, use_labels, level, S.m[j], S.deg[j]);
+    if (d < bd) {
+      bd = d;
       best = j;
     }
   }
@@ -363,15 +393,16 @@ __device__ __forceinline__ uint32_t choose_pivot(const WarpView &S, uint32_t lev
 }
 
 // Candidate test for list entry w at `level` (>= 1, not the last level).
-__device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const CandView &cv, uint32_t level,
-                                       uint32_t w, uint32_t &probes) {
+__device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const CandView &cv, bool use_labels,
+                                       uint32_t level, uint32_t w, uint32_t &probes) {
   if (!SMG_DCHECK(w < p.n, 105, w, level)) return false;
+  const uint32_t bucket = use_labels ? S.lbk[level] : kNone;
   if (!cv.has(S.ord[level], w)) return false;
   for (uint32_t b = S.slab[level]; b; b &= b - 1)
     if (S.m[__ffs(b) - 1] == w) return false;
   for (uint32_t b = S.bmask[level] & ~(1u << S.piv[level]); b; b &= b - 1) {
     const uint32_t j = __ffs(b) - 1;
-    if (!is_neighbor(p, S.beg[j], S.deg[j], S.hub[j], w, probes)) return false;
+    if (!is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes)) return false;
   }
   return true;
 }
@@ -421,14 +452,8 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
                                                uint32_t hi, uint32_t lane, unsigned long long &scanned,
                                                uint32_t &probes) {
   const uint32_t L = P + 1;
-  uint32_t piv = 0, bd = 0xFFFFFFFFu;
-  for (uint32_t b = S.bmask[L]; b; b &= b - 1) {
-    const uint32_t j = __ffs(b) - 1;
-    if (S.deg[j] < bd) {
-      bd = S.deg[j];
-      piv = j;
-    }
-  }
+  const uint32_t bucket = Q.use_labels ? S.lbk[L] : kNone;
+  const uint32_t piv = choose_pivot(p, S, Q.use_labels, L);
   uint32_t len = 0;
   const uint32_t *base = scan_list(p, S, Q.use_labels, L, S.m[piv], S.beg[piv], S.deg[piv], len);
   hi = min(hi, len);
@@ -447,7 +472,7 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
       for (uint32_t b = same; b && good; b &= b - 1) good = S.m[__ffs(b) - 1] != w;
       for (uint32_t b = back; b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
-        good = is_neighbor(p, S.beg[j], S.deg[j], S.hub[j], w, probes);
+        good = is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes);
       }
     }
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
@@ -476,6 +501,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
                                          const CandView &cv, uint32_t P, uint32_t bc,
                                          uint32_t lane, unsigned long long &scanned, uint32_t &probes) {
   const uint32_t L = P + 1;
+  const uint32_t bucket = Q.use_labels ? S.lbk[L] : kNone;
   const uint32_t lt = (1u << lane) - 1;
   const bool fast_ok = Q.fast_last && !p.emit;  // k_last_counts ran only then
   uint32_t len = 0, fast = 0;
@@ -506,7 +532,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
           for (uint32_t b = S.slab[L]; b; b &= b - 1) {
             const uint32_t j = __ffs(b) - 1;
             const uint32_t x = j == P ? v : S.m[j];
-            if (x != a && cv.has(u, x) && is_neighbor(p, ab, ad, ah, x, probes)) ++corr;
+            if (x != a && cv.has(u, x) && is_neighbor(p, a, ab, ad, ah, bucket, x, probes)) ++corr;
           }
         }
         fast = c - corr;
@@ -515,17 +541,10 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
     }
     if (!counted) {
       const uint32_t vb = __ldg(p.off + v), vd = __ldg(p.off + v + 1) - vb;
-      uint32_t piv = 0, bd = 0xFFFFFFFFu;
-      for (uint32_t b = S.bmask[L]; b; b &= b - 1) {
-        const uint32_t j = __ffs(b) - 1;
-        const uint32_t d = j == P ? vd : S.deg[j];
-        if (d < bd) {
-          bd = d;
-          piv = j;
-        }
-      }
+      const uint32_t piv = choose_pivot(p, S, Q.use_labels, L, P, v, vd);
       const uint32_t pb = piv == P ? vb : S.beg[piv];
-      const uint32_t *lst = scan_list(p, S, Q.use_labels, L, piv == P ? v : S.m[piv], pb, bd, len);
+      const uint32_t *lst =
+          scan_list(p, S, Q.use_labels, L, piv == P ? v : S.m[piv], pb, piv == P ? vd : S.deg[piv], len);
       const bool from_l = lst != p.adj + pb;
       if (len > kSplitLen) len = split_last(S, p, Q, q, P, v, len);
       S.sv[lane] = v;
@@ -576,9 +595,9 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       for (uint32_t b = back & ~(1u << (sp & 31u)); b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
         if (j == P)
-          good = is_neighbor(p, S.sbeg[i], S.sdeg[i], S.shub[i], w, probes);
+          good = is_neighbor(p, vi, S.sbeg[i], S.sdeg[i], S.shub[i], bucket, w, probes);
         else
-          good = is_neighbor(p, S.beg[j], S.deg[j], S.hub[j], w, probes);
+          good = is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes);
       }
     }
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
@@ -821,7 +840,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         S.cur[L0] = lo;
         S.end[L0] = hi;
       } else {
-        const uint32_t pv = choose_pivot(S, L0);
+        const uint32_t pv = choose_pivot(p, S, Q.use_labels, L0);
         uint32_t len = 0;
         S.piv[L0] = pv;
         S.lbase[L0] = scan_list(p, S, Q.use_labels, L0, S.m[pv], S.beg[pv], S.deg[pv], len);
@@ -930,7 +949,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
           __syncwarp();
           const uint32_t nl = level + 1;
           if (lane == 0) {
-            const uint32_t pv = choose_pivot(S, nl);
+            const uint32_t pv = choose_pivot(p, S, Q.use_labels, nl);
             uint32_t len = 0;
             S.piv[nl] = pv;
             S.lbase[nl] = scan_list(p, S, Q.use_labels, nl, S.m[pv], S.beg[pv], S.deg[pv], len);
@@ -958,7 +977,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
                                                 : in_lists(p, base + c + lane),
                                    114, c + lane, level)) {
           w = __ldg(base + c + lane);
-          good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, cv, level, w, probes));
+          good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, cv, Q.use_labels, level, w, probes));
         }
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
         if (good) S.batch[level * 32 + __popc(bal & lt)] = w;
@@ -1115,7 +1134,19 @@ JoinKernel join_kernel(size_t smem_per_block) {
   return k_join4;
 }
 
-smg_status launch_persistent(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
+// Membership probes: hub bitmaps and id-ordered lists (default), or, with
+// SMG_PROBE=runs, binary searches of label runs where a vertex has them.
+bool probe_runs() {
+  static const bool v = [] {
+    const char *e = std::getenv("SMG_PROBE");
+    return e && std::string(e) == "runs";
+  }();
+  return v;
+}
+
+smg_status launch_persistent(const JoinLaunch &jl_in, cudaStream_t s, int num_sms) {
+  JoinLaunch jl = jl_in;
+  jl.probe_runs = probe_runs() && jl.adjl != nullptr;
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
   const JoinKernel kern = join_kernel(smem);
   if (smem > 48 * 1024)
@@ -1132,11 +1163,11 @@ smg_status launch_persistent(const JoinLaunch &jl, cudaStream_t s, int num_sms) 
 
 smg_status launch_join(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   if (jl.nq == 0) return SMG_OK;
-  const uint32_t seed_threads = 128;
+  const uint32_t seed_threads = 256;
   const uint32_t nseed = jl.seed_list ? jl.seed_n : jl.nq;
   smg_status rc = launch_join_prep(jl, s, num_sms);
   if (rc) return rc;
-  k_seed<<<(nseed + seed_threads - 1) / seed_threads, seed_threads, 0, s>>>(jl);
+  k_seed<<<dim3(1, std::min<uint32_t>(nseed, 65535)), seed_threads, 0, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
   return launch_persistent(jl, s, num_sms);
 }
@@ -1147,14 +1178,8 @@ smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
 
 smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   const uint32_t nq = jl.seed_list ? jl.seed_n : jl.nq;
-  if (!nq || !jl.n) return SMG_OK;
-  const uint64_t words = (static_cast<uint64_t>(jl.n) + 31) / 32;
+  if (!nq || !jl.n || jl.emit) return SMG_OK;
   const uint32_t want = std::max<uint32_t>(1, static_cast<uint32_t>(std::max(num_sms, 1)) * 16 / nq);
-  const uint32_t span_bits = static_cast<uint32_t>((words + 7) / 8);  // 8 warps per block, a word each
-  const dim3 g1(std::min(span_bits, want), std::min<uint32_t>(nq, 65535));
-  k_cand_bits<<<g1, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.n);
-  SMG_CUDA(cudaGetLastError());
-  if (jl.emit) return SMG_OK;
   const uint32_t span = static_cast<uint32_t>((static_cast<uint64_t>(jl.n) + 255) / 256);  // 32 vertices a warp
   const dim3 g2(std::min(span, want), std::min<uint32_t>(nq, 65535));
   k_last_counts<<<g2, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.off, jl.adj, jl.adjl, jl.lab_of, jl.lab_off,
@@ -1166,7 +1191,7 @@ smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
 smg_status launch_seed(const JoinLaunch &jl, cudaStream_t s) {
   const uint32_t n = jl.seed_list ? jl.seed_n : jl.nq;
   if (!n) return SMG_OK;
-  k_seed<<<(n + 127) / 128, 128, 0, s>>>(jl);
+  k_seed<<<dim3(1, std::min<uint32_t>(n, 65535)), 256, 0, s>>>(jl);
   SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }

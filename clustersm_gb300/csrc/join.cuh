@@ -42,6 +42,7 @@ struct JoinLaunch {
   const uint32_t *adjl;      // label index (DevGraph::adjl, lab_of, lab_off)
   const uint32_t *lab_of, *lab_off;
   uint32_t lab_buckets;
+  uint32_t probe_runs;       // membership probes search label runs (SMG_PROBE=runs)
   uint32_t n;                // data vertices (bounds of the self-checking build)
   uint64_t m2;               // adjacency entries
   uint32_t num_hubs;
@@ -91,12 +92,11 @@ smg_status launch_join_only(const JoinLaunch &jl, cudaStream_t s, int num_sms);
 smg_status launch_compact(const uint32_t *tasks_old, const uint32_t *ready_old, uint32_t cap, uint32_t tw,
                           uint32_t *tasks_new, uint32_t *ready_new, unsigned int *new_count, QueueState *qs,
                           cudaStream_t s, int num_sms);
-// Join inputs built after the filter for the queries jl.seed_list names (all
-// jl.nq when it is null): each query's candidate bitmaps (cbits) from its
-// final masks, then, unless the run emits embeddings, its last-level counts
-// (fast_last queries): for every candidate v of the last vertex's back
-// neighbour, how many neighbours of v are candidates of the last vertex.
-// launch_join runs it itself.
+// Join inputs built after the filter (which leaves the candidate bitmaps)
+// for the queries jl.seed_list names (all jl.nq when it is null): unless the
+// run emits embeddings, each fast_last query's last-level counts: for every
+// candidate v of the last vertex's back neighbour, how many neighbours of v
+// are candidates of the last vertex.  launch_join runs it itself.
 smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms);
 // Label index of a resident graph (DevGraph::adjl, lab_of, lab_off) from the
 // host's id-ordered lists: vertices of degree >= min_degree get a run table,

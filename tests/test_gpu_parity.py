@@ -203,3 +203,26 @@ def test_reference_edge_order_gives_same_counts(ctx):
     r = subprocess.run([sys.executable, "-c", PLAN_ORDER_SCRIPT, str(root)], env=env, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("min_degree,enabled", [("1", "1"), ("64", "0")])
+def test_label_index_every_vertex_or_none(ctx, monkeypatch, min_degree, enabled):
+    """The label index (neighbour lists ordered by label, with per-label run
+    tables) given to every vertex, and left out: cluster bitmaps stay
+    bit-exact and counts equal the oracle's either way.  The settings are read
+    when a graph is uploaded."""
+    monkeypatch.setenv("SMG_LABEL_INDEX_MIN_DEGREE", min_degree)
+    monkeypatch.setenv("SMG_LABEL_INDEX", enabled)
+    host = HostGraph.rmat(12, 16, 8, seed=7)
+    dev = DeviceGraph(ctx, host)
+    checked = 0
+    for q in small_queries(host, shapes=RMAT_SHAPES, ks=(4, 5, 6, 8), seeds=range(2)):
+        plan, _ = check_filter(ctx, host, dev, q)
+        want = budgeted(host, q)
+        if want is None:
+            continue
+        res, _ = native.match(ctx, dev, plan)
+        assert res.count == want, (q.to_dict(), res.count, want)
+        checked += 1
+    assert checked >= 8
+    dev.free()
