@@ -335,7 +335,11 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "k_join", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                          "traffic": traffic,
-                         "algorithmic_bytes_per_step": jbytes / args.steps},
+                         "algorithmic_bytes_per_step": jbytes / args.steps,
+                         # DRAM traffic of the same kernel (one ncu capture) over its event-timed duration
+                         "traffic_gbs": traffic / (join_ms / args.steps / 1e3) / 1e9 if traffic and join_ms else None,
+                         "traffic_frac": traffic / (join_ms / args.steps / 1e3) / 1e9 / peak if traffic and join_ms
+                         else None},
             "clocks": clocks,
             "serving": serve,
         }

@@ -224,17 +224,18 @@ smg_status smg_graph_upload(smg_ctx *c, const smg_csr *in, smg_graph **out) {
   if (n) SMG_CUDA(cudaMemcpyAsync(g.label, in->labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
   smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
   if (st) return st;
+  if (label_index_enabled()) {
+    // the id-ordered lists the device got (the caller's, or their sorted copy);
+    // built first: the hub bitmaps take its label layout
+    st = build_label_index(g, in->offsets, adj_src, in->labels, label_index_min_degree(), 1ull << 30, c->stream);
+    if (st) return st;
+  }
   {
     std::vector<uint32_t> deg(n);
 #pragma omp parallel for schedule(static)
     for (int64_t v = 0; v < static_cast<int64_t>(n); ++v)
       deg[v] = static_cast<uint32_t>(in->offsets[v + 1] - in->offsets[v]);
     st = build_hub_bitmaps(g, hub_min_degree(), hub_max_bytes(), c->stream, deg);
-    if (st) return st;
-  }
-  if (label_index_enabled()) {
-    // the id-ordered lists the device got (the caller's, or their sorted copy)
-    st = build_label_index(g, in->offsets, adj_src, in->labels, label_index_min_degree(), 1ull << 30, c->stream);
     if (st) return st;
   }
   SMG_CUDA(cudaStreamSynchronize(c->stream));
@@ -256,6 +257,8 @@ void smg_graph_free(smg_graph *G) {
   if (g.adjl) cudaFree(g.adjl);
   if (g.lab_of) cudaFree(g.lab_of);
   if (g.lab_off) cudaFree(g.lab_off);
+  if (g.lab_rank) cudaFree(g.lab_rank);
+  if (g.bucket_word_off) cudaFree(g.bucket_word_off);
   delete G;
 }
 
@@ -582,18 +585,7 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
   const uint32_t nq = ch.b - ch.a;
   JoinLaunch jl;
   std::memset(&jl, 0, sizeof(jl));
-  jl.off = g.off;
-  jl.adj = g.adj;
-  jl.hub_of = g.hub_of;
-  jl.hub_bits = g.hub_bits;
-  jl.hub_words = g.hub_words;
-  jl.adjl = g.adjl;
-  jl.lab_of = g.lab_of;
-  jl.lab_off = g.lab_off;
-  jl.lab_buckets = g.lab_buckets;
-  jl.n = g.n;
-  jl.m2 = g.m2;
-  jl.num_hubs = g.num_hubs;
+  set_graph(jl, g);
   jl.queries = ch.jq;
   jl.nq = nq;
   jl.kmax = ch.kmax;

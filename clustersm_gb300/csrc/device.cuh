@@ -60,6 +60,17 @@ struct DevGraph {
   uint32_t *lab_of = nullptr;   // [n] row of the vertex's run table, or kNone
   uint32_t *lab_off = nullptr;  // [indexed][lab_buckets + 1]
   uint32_t lab_buckets = 0, lab_indexed = 0;
+  // Optional hub bitmap layout by label bucket (SMG_HUB_LAYOUT=label, with
+  // the label index): the bit of neighbour w sits at word
+  // bucket_word_off[bucket(w)] + lab_rank[w] / 32 of the hub's row, where
+  // lab_rank[w] is w's index among the vertices of its bucket (in id order).
+  // A probe for a candidate of one label then touches that label's
+  // n_label / 8 bytes of the row instead of all n / 8, at the price of one
+  // more dependent load.
+  uint32_t *lab_rank = nullptr;         // [n]
+  uint32_t *bucket_word_off = nullptr;  // [lab_buckets + 1]
+  uint64_t hub_row_words = 0;           // bucket_word_off[lab_buckets]
+  bool hub_by_label = false;            // hub rows use the layout above (else by id)
   std::vector<uint64_t> label_count;  // vertices per label (host copy)
   uint64_t bytes = 0;
 };

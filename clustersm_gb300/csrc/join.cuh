@@ -42,6 +42,8 @@ struct JoinLaunch {
   const uint32_t *adjl;      // label index (DevGraph::adjl, lab_of, lab_off)
   const uint32_t *lab_of, *lab_off;
   uint32_t lab_buckets;
+  const uint32_t *label;     // vertex labels (bucket of a probed vertex without a level bucket)
+  const uint32_t *lab_rank, *bucket_word_off;  // hub bitmap layout by label (null: by id)
   uint32_t probe_runs;       // membership probes search label runs (SMG_PROBE=runs)
   uint32_t n;                // data vertices (bounds of the self-checking build)
   uint64_t m2;               // adjacency entries
@@ -72,6 +74,9 @@ struct JoinLaunch {
   uint32_t seed_n;
 };
 
+// The resident graph's arrays in a launch record (every launch site uses
+// this, so the hub bitmap layout and the label index always travel together).
+void set_graph(JoinLaunch &jl, const DevGraph &g);
 // Bytes of queue storage for `cap` tasks of a batch whose largest query has
 // kmax vertices.
 size_t join_queue_bytes(uint32_t cap, uint32_t kmax);

@@ -105,14 +105,7 @@ extern "C" smg_status smg_join_noalloc(smg_ctx *c, const smg_graph *G, const smg
   SMG_CUDA(cudaMemcpyAsync(&sc.cnt->num_roots, hroots, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
   JoinLaunch jl;
   std::memset(&jl, 0, sizeof(jl));
-  jl.off = G->g.off;
-  jl.adj = G->g.adj;
-  jl.hub_of = G->g.hub_of;
-  jl.hub_bits = G->g.hub_bits;
-  jl.hub_words = G->g.hub_words;
-  jl.n = G->g.n;
-  jl.m2 = G->g.m2;
-  jl.num_hubs = G->g.num_hubs;
+  set_graph(jl, G->g);
   jl.queries = sc.jq;
   jl.nq = 1;
   jl.kmax = kMaxK;

@@ -184,18 +184,7 @@ smg::JoinLaunch join_launch(smg_server *s) {
   const smg::DevGraph &g = s->graph->g;
   smg::JoinLaunch jl;
   std::memset(&jl, 0, sizeof(jl));
-  jl.off = g.off;
-  jl.adj = g.adj;
-  jl.hub_of = g.hub_of;
-  jl.hub_bits = g.hub_bits;
-  jl.hub_words = g.hub_words;
-  jl.adjl = g.adjl;
-  jl.lab_of = g.lab_of;
-  jl.lab_off = g.lab_off;
-  jl.lab_buckets = g.lab_buckets;
-  jl.n = g.n;
-  jl.m2 = g.m2;
-  jl.num_hubs = g.num_hubs;
+  smg::set_graph(jl, g);
   jl.queries = s->d_jq;
   jl.nq = s->cfg.max_inflight;
   jl.kmax = kServerK;

@@ -226,3 +226,24 @@ def test_label_index_every_vertex_or_none(ctx, monkeypatch, min_degree, enabled)
         checked += 1
     assert checked >= 8
     dev.free()
+
+
+@pytest.mark.parametrize("layout", ["label", "id"])
+def test_hub_bitmap_layouts(ctx, monkeypatch, layout):
+    """Hub neighbour bitmaps laid out by (label, rank) and by id, with every
+    vertex of degree >= 16 a hub: counts equal the oracle's either way (the
+    settings are read when a graph is uploaded)."""
+    monkeypatch.setenv("SMG_HUB_MIN_DEGREE", "16")
+    monkeypatch.setenv("SMG_HUB_LAYOUT", layout)
+    host = HostGraph.rmat(12, 16, 8, seed=7)
+    dev = DeviceGraph(ctx, host)
+    checked = 0
+    for q in small_queries(host, shapes=RMAT_SHAPES, ks=(4, 5, 6), seeds=range(3)):
+        want = budgeted(host, q)
+        if want is None:
+            continue
+        res, _ = native.match(ctx, dev, Plan(q))
+        assert res.count == want, (layout, q.to_dict(), res.count, want)
+        checked += 1
+    assert checked >= 10
+    dev.free()
