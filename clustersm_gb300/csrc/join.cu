@@ -310,11 +310,18 @@ __device__ __forceinline__ bool is_neighbor(const JoinLaunch &p, uint32_t x, uin
 //   seg*          per-candidate segments of the segmented last level; bit 31
 //                 of spiv marks a segment read from the label-ordered lists
 __host__ __device__ inline uint32_t scalar_words(uint32_t K) { return (13 * K + 1) & ~1u; }
-__host__ __device__ inline uint32_t warp_words(uint32_t K) { return scalar_words(K) + 2 * K + 32 * K + 7 * 32; }
+//   xs, xlen      the hoisted last-level set of the current prefix (see
+//                 last_level): sorted, at most kHoistCap entries
+constexpr uint32_t kHoistCap = 256;
+constexpr uint32_t kHoistInvalid = 0xFFFFFFFFu;  // xlen: not built for this prefix
+constexpr uint32_t kHoistTooBig = 0xFFFFFFFEu;   // xlen: larger than kHoistCap
+__host__ __device__ inline uint32_t warp_words(uint32_t K) {
+  return scalar_words(K) + 2 * K + 32 * K + 7 * 32 + kHoistCap + 2;
+}
 
 struct WarpView {
   uint32_t *m, *beg, *deg, *hub, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *lbk, *batch;
-  uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv;
+  uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv, *xs, *xlen;
   const uint32_t **lbase;
   __device__ WarpView(uint32_t *W, uint32_t K) {
     m = W;
@@ -340,10 +347,14 @@ struct WarpView {
     sbase = shub + 32;
     spre = sbase + 32;
     spiv = spre + 32;
+    xs = spiv + 32;
+    xlen = xs + kHoistCap;
   }
 };
 
 constexpr uint32_t kFromLabelIndex = 1u << 31;  // spiv flag: segment in adjl
+constexpr uint32_t kHoistScan = 1u << 30;       // spiv flag: keep entries found in the hoisted set
+constexpr uint32_t kHoistSet = 1u << 29;        // spiv flag: the segment is the hoisted set itself
 
 // Self-checking build: does `e` point into adj or adjl?
 __device__ __forceinline__ bool in_lists(const JoinLaunch &p, const uint32_t *e) {
@@ -507,6 +518,72 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
   return cnt;
 }
 
+// Is w in the hoisted set (sorted, n entries)?
+__device__ __forceinline__ bool in_hoisted(const WarpView &S, uint32_t n, uint32_t w) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (S.xs[mid] < w)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo < n && S.xs[lo] == w;
+}
+
+// The hoisted last-level set of the prefix m[0..P-1]: the candidates w of the
+// last vertex u_L adjacent to every back neighbour of u_L matched before level
+// P (`fixed`), other than the matched vertices of u_L's label before P.  It
+// does not depend on the level-P vertex, so a warp builds it once per prefix
+// and every batch of level-P candidates reuses it.  It is the shortest fixed
+// back neighbour's run filtered by the others, so it comes out sorted by id.
+// Sets *S.xlen to its size, or kHoistTooBig past kHoistCap entries.
+__device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery &Q, const CandView &cv,
+                              uint32_t P, uint32_t fixed, uint32_t lane, unsigned long long &scanned,
+                              uint32_t &probes) {
+  const uint32_t L = P + 1;
+  const uint32_t bucket = Q.use_labels ? S.lbk[L] : kNone;
+  uint32_t a = 0, best = 0xFFFFFFFFu;
+  for (uint32_t b = fixed; b; b &= b - 1) {
+    const uint32_t j = __ffs(b) - 1;
+    const uint32_t d = run_len(p, S, Q.use_labels, L, S.m[j], S.deg[j]);
+    if (d < best) {
+      best = d;
+      a = j;
+    }
+  }
+  uint32_t len = 0;
+  const uint32_t *lst = scan_list(p, S, Q.use_labels, L, S.m[a], S.beg[a], S.deg[a], len);
+  const uint32_t u = S.ord[L], same = S.slab[L] & ((1u << P) - 1), others = fixed & ~(1u << a);
+  const uint32_t lt = (1u << lane) - 1;
+  uint32_t n = 0;
+  scanned += len;
+  for (uint32_t t0 = 0; t0 < len; t0 += 32) {
+    const uint32_t t = t0 + lane;
+    bool good = false;
+    uint32_t w = 0;
+    if (t < len) {
+      w = __ldg(lst + t);
+      good = SMG_DCHECK(w < p.n, 116, w, t) && cv.has(u, w);
+      for (uint32_t b = same; b && good; b &= b - 1) good = S.m[__ffs(b) - 1] != w;
+      for (uint32_t b = others; b && good; b &= b - 1) {
+        const uint32_t j = __ffs(b) - 1;
+        good = is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes);
+      }
+    }
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
+    if (n + __popc(bal) > kHoistCap) {
+      n = kHoistTooBig;
+      break;
+    }
+    if (good) S.xs[n + __popc(bal & lt)] = w;
+    n += __popc(bal);
+  }
+  __syncwarp();
+  if (lane == 0) *S.xlen = n;
+  __syncwarp();
+}
+
 // Counts (and optionally emits) the last level for every candidate of the
 // batch of level P = k-2: the candidates' last-level lists are concatenated
 // and walked 32 entries at a time, each lane finding its candidate by binary
@@ -518,12 +595,49 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   const uint32_t bucket = Q.use_labels ? S.lbk[L] : kNone;
   const uint32_t lt = (1u << lane) - 1;
   const bool fast_ok = Q.fast_last && !p.emit;  // k_last_counts ran only then
+  // several back edges, some to levels before P: the hoisted set of the prefix
+  const uint32_t fixed = S.bmask[L] & ((1u << P) - 1);
+  uint32_t xn = kHoistTooBig;
+  if (p.hoist && !p.emit && !Q.fast_last && fixed) {
+    if (*S.xlen == kHoistInvalid) build_hoisted(S, p, Q, cv, P, fixed, lane, scanned, probes);
+    xn = *S.xlen;
+  }
+  const bool use_x = xn != kHoistTooBig;
   uint32_t len = 0, fast = 0;
   if (lane < bc) {
     uint32_t v = S.batch[P * 32 + lane];
     if (!SMG_DCHECK(v < p.n, 106, v, P)) v = 0;
     bool counted = false;
-    if (fast_ok) {
+    if (use_x) {
+      const uint32_t vb = __ldg(p.off + v), vd = __ldg(p.off + v + 1) - vb;
+      if (!((S.bmask[L] >> P) & 1u)) {
+        // u_L is not adjacent to level P: every candidate sees the whole set,
+        // less itself when it has u_L's label
+        fast = xn - (((S.slab[L] >> P) & 1u) && in_hoisted(S, xn, v) ? 1u : 0u);
+        counted = true;
+      } else {
+        // |X & N(v)|: walk v's run keeping members of X, or walk X probing
+        // N(v), whichever is shorter
+        const uint32_t rv = run_len(p, S, Q.use_labels, L, v, vd);
+        uint32_t mode = kHoistSet, base = 0;
+        if (rv <= xn) {
+          const uint32_t *lst = scan_list(p, S, Q.use_labels, L, v, vb, vd, len);
+          const bool from_l = lst != p.adj + vb;
+          base = static_cast<uint32_t>(lst - (from_l ? p.adjl : p.adj));
+          mode = kHoistScan | (from_l ? kFromLabelIndex : 0u);
+        } else {
+          len = xn;
+        }
+        S.sv[lane] = v;
+        S.sbeg[lane] = vb;
+        S.sdeg[lane] = vd;
+        S.shub[lane] = __ldg(p.hub_of + v);
+        S.sbase[lane] = base;
+        S.spiv[lane] = P | mode;
+        counted = true;
+      }
+    }
+    if (!counted && fast_ok) {
       // one back edge, to level fb: the stored neighbour count of its vertex
       // a, less the matched vertices of the last vertex's label adjacent to a
       const uint32_t fb = Q.fast_last - 1;
@@ -578,7 +692,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   S.spre[lane] = incl - len;
   __syncwarp();
   scanned += total;
-  unsigned long long cnt = fast_ok ? __reduce_add_sync(0xFFFFFFFFu, fast) : 0u;
+  unsigned long long cnt = (fast_ok || use_x) ? __reduce_add_sync(0xFFFFFFFFu, fast) : 0u;
   const uint32_t u = S.ord[L];
   const uint32_t back = S.bmask[L], same = S.slab[L];
   for (uint32_t t0 = 0; t0 < total; t0 += 32) {
@@ -596,22 +710,31 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       }
       i = lo;
       const uint32_t vi = S.sv[i];
-      const uint64_t ai = static_cast<uint64_t>(S.sbase[i]) + (t - S.spre[i]);
-      const bool in_adj = SMG_DCHECK(ai < p.m2, 107, ai, i);
       const uint32_t sp = S.spiv[i];
-      w = in_adj ? __ldg(((sp & kFromLabelIndex) ? p.adjl : p.adj) + ai) : 0u;
-      good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) && cv.has(u, w);
-      for (uint32_t b = same; b && good; b &= b - 1) {
-        const uint32_t j = __ffs(b) - 1;
-        good = (j == P ? vi : S.m[j]) != w;
-      }
-      // back edges other than the pivot's (whose list w comes from)
-      for (uint32_t b = back & ~(1u << (sp & 31u)); b && good; b &= b - 1) {
-        const uint32_t j = __ffs(b) - 1;
-        if (j == P)
-          good = is_neighbor(p, vi, S.sbeg[i], S.sdeg[i], S.shub[i], bucket, w, probes);
-        else
-          good = is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes);
+      if (sp & kHoistSet) {  // a member of the hoisted set: is it a neighbour of v?
+        w = S.xs[t - S.spre[i]];
+        good = is_neighbor(p, vi, S.sbeg[i], S.sdeg[i], S.shub[i], bucket, w, probes);
+      } else {
+        const uint64_t ai = static_cast<uint64_t>(S.sbase[i]) + (t - S.spre[i]);
+        const bool in_adj = SMG_DCHECK(ai < p.m2, 107, ai, i);
+        w = in_adj ? __ldg(((sp & kFromLabelIndex) ? p.adjl : p.adj) + ai) : 0u;
+        if (sp & kHoistScan) {  // a neighbour of v: is it in the hoisted set?
+          good = in_adj && in_hoisted(S, xn, w);
+        } else {
+          good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) && cv.has(u, w);
+          for (uint32_t b = same; b && good; b &= b - 1) {
+            const uint32_t j = __ffs(b) - 1;
+            good = (j == P ? vi : S.m[j]) != w;
+          }
+          // back edges other than the pivot's (whose list w comes from)
+          for (uint32_t b = back & ~(1u << (sp & 31u)); b && good; b &= b - 1) {
+            const uint32_t j = __ffs(b) - 1;
+            if (j == P)
+              good = is_neighbor(p, vi, S.sbeg[i], S.sdeg[i], S.shub[i], bucket, w, probes);
+            else
+              good = is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes);
+          }
+        }
       }
     }
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
@@ -863,6 +986,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       }
       S.bcnt[L0] = 0;
       S.bidx[L0] = 0;
+      *S.xlen = kHoistInvalid;  // a new prefix
     }
     __syncwarp();
 
@@ -971,6 +1095,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
             S.end[nl] = len;
             S.bcnt[nl] = 0;
             S.bidx[nl] = 0;
+            if (nl == P) *S.xlen = kHoistInvalid;  // the prefix m[0..P-1] changed
           }
           __syncwarp();
           ++descents;
@@ -1176,9 +1301,19 @@ bool probe_runs() {
   return v;
 }
 
+// The hoisted last-level set (SMG_HOIST=0 turns it off).
+bool hoist_enabled() {
+  static const bool v = [] {
+    const char *e = std::getenv("SMG_HOIST");
+    return !(e && std::string(e) == "0");
+  }();
+  return v;
+}
+
 smg_status launch_persistent(const JoinLaunch &jl_in, cudaStream_t s, int num_sms) {
   JoinLaunch jl = jl_in;
   jl.probe_runs = probe_runs() && jl.adjl != nullptr;
+  jl.hoist = hoist_enabled();
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
   const JoinKernel kern = join_kernel(smem);
   if (smem > 48 * 1024)

@@ -45,6 +45,7 @@ struct JoinLaunch {
   const uint32_t *label;     // vertex labels (bucket of a probed vertex without a level bucket)
   const uint32_t *lab_rank, *bucket_word_off;  // hub bitmap layout by label (null: by id)
   uint32_t probe_runs;       // membership probes search label runs (SMG_PROBE=runs)
+  uint32_t hoist;            // hoisted last-level sets (count-only runs; SMG_HOIST=0: off)
   uint32_t n;                // data vertices (bounds of the self-checking build)
   uint64_t m2;               // adjacency entries
   uint32_t num_hubs;
