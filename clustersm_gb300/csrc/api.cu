@@ -210,6 +210,19 @@ smg_status smg_graph_upload(smg_ctx *c, const smg_csr *in, smg_graph **out) {
   g.label_count.assign(std::min<uint32_t>(g.num_labels, kMaxLabels), 0);
   for (uint32_t v = 0; v < n; ++v)
     if (in->labels[v] < kMaxLabels) ++g.label_count[in->labels[v]];
+  // vertex ids grouped by label (labels >= kMaxLabels, which no query has, at the end)
+  std::vector<uint32_t> lverts(std::max<uint32_t>(n, 1));
+  {
+    const size_t nl = g.label_count.size();
+    g.lvert_start.assign(nl + 1, 0);
+    for (size_t l = 0; l < nl; ++l) g.lvert_start[l + 1] = g.lvert_start[l] + static_cast<uint32_t>(g.label_count[l]);
+    std::vector<uint32_t> at(g.lvert_start.begin(), g.lvert_start.end() - 1);
+    uint32_t tail = g.lvert_start[nl];
+    for (uint32_t v = 0; v < n; ++v) {
+      const uint32_t l = in->labels[v];
+      lverts[l < nl ? at[l]++ : tail++] = v;
+    }
+  }
   const uint32_t ncols = std::min<uint32_t>(g.num_labels, kMaxLabels);
   g.nlc_stride = std::max<uint32_t>(16, (ncols + 15) & ~15u);
   const size_t b_off = (static_cast<size_t>(n) + 1) * 4, b_adj = std::max<uint64_t>(m2, 1) * 4,
@@ -218,10 +231,12 @@ smg_status smg_graph_upload(smg_ctx *c, const smg_csr *in, smg_graph **out) {
   SMG_CUDA(cudaMalloc(&g.adj, b_adj));
   SMG_CUDA(cudaMalloc(&g.label, b_lab));
   SMG_CUDA(cudaMalloc(&g.nlc, b_nlc));
-  g.bytes = b_off + b_adj + b_lab + b_nlc;
+  SMG_CUDA(cudaMalloc(&g.lverts, b_lab));
+  g.bytes = b_off + b_adj + 2 * b_lab + b_nlc;
   SMG_CUDA(cudaMemcpyAsync(g.off, off32.data(), b_off, cudaMemcpyHostToDevice, c->stream));
   if (m2) SMG_CUDA(cudaMemcpyAsync(g.adj, adj_src, m2 * 4, cudaMemcpyHostToDevice, c->stream));
   if (n) SMG_CUDA(cudaMemcpyAsync(g.label, in->labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
+  if (n) SMG_CUDA(cudaMemcpyAsync(g.lverts, lverts.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
   smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
   if (st) return st;
   if (label_index_enabled()) {
@@ -252,6 +267,7 @@ void smg_graph_free(smg_graph *G) {
   if (g.adj) cudaFree(g.adj);
   if (g.label) cudaFree(g.label);
   if (g.nlc) cudaFree(g.nlc);
+  if (g.lverts) cudaFree(g.lverts);
   if (g.hub_of) cudaFree(g.hub_of);
   if (g.hub_bits) cudaFree(g.hub_bits);
   if (g.adjl) cudaFree(g.adjl);
@@ -425,7 +441,14 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
     j.cwords = (g.n + 31ull) / 32;
     j.lastcnt = b.vmask;
     const uint32_t last_back = j.back_mask[P.k - 1];
-    if (last_back && !(last_back & (last_back - 1))) j.fast_last = static_cast<uint32_t>(__builtin_ctz(last_back)) + 1;
+    if (last_back && !(last_back & (last_back - 1))) {
+      j.fast_last = static_cast<uint32_t>(__builtin_ctz(last_back)) + 1;
+      const uint32_t l = P.label[j.order[j.fast_last - 1]];  // its candidates all carry this label
+      if (l + 1 < g.lvert_start.size()) {
+        j.lc_lo = g.lvert_start[l];
+        j.lc_hi = g.lvert_start[l + 1];
+      }
+    }
   }
   j.roots = b.roots;
   j.num_roots = &b.counters->num_roots;
@@ -483,23 +506,25 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   const size_t o_wcnt = off;
   off += al(kMaxWalkPhases * 2 * sizeof(unsigned int));
   std::vector<size_t> o_enc(nq), o_vm(nq), o_cand(nq), o_root(nq), o_cb(nq);
+  // the filter writes masks and candidate bitmaps only for vertices of the
+  // query's labels: they start at zero with the cluster bitmaps
   for (uint32_t i = 0; i < nq; ++i) {
     o_enc[i] = off;
     off += al(static_cast<size_t>(g.n) * plans[ch.a + i]->num_words * 4);
+    o_vm[i] = off;
+    off += al(static_cast<size_t>(g.n) * 4);
+    o_cb[i] = off;
+    off += al(cbits_bytes(g, plans[ch.a + i]->k));
   }
   ch.zero_bytes = off;
   for (uint32_t i = 0; i < nq; ++i) {
     const Plan &P = *plans[ch.a + i];
     query_bytes(g, P, ch.cand_total[i]);
-    o_vm[i] = off;
-    off += al(static_cast<size_t>(g.n) * 4);
     o_cand[i] = off;
     off += al(ch.cand_total[i] * 4);
     o_root[i] = off;
     const uint64_t rc = label_cands(g, P.label[join_root(P, g)]);
     off += al(std::max<uint64_t>(rc, 1) * 4);
-    o_cb[i] = off;
-    off += al(cbits_bytes(g, P.k));
   }
   const size_t o_tasks = off;
   off += al(static_cast<size_t>(ch.cap) * (4 + ch.kmax) * 4);
@@ -699,8 +724,11 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
         seen[P.label[u]] = 1;
         lab += g.label_count[P.label[u]];
       }
-    st->filter_bytes += 12ull * g.n + lab * (8 + 32) + 8ull * q.initial_cands + 8ull * q.walk_entries +
-                        4ull * q.num_roots;
+    // masks cleared (4 B a vertex); per vertex of the query's labels: group
+    // entry, offsets, NLC sector, mask write, then group entry and mask read
+    // in collect; per candidate appended, per walked entry, per root
+    st->filter_bytes += 4ull * g.n + lab * (4 + 8 + 32 + 4 + 4 + 4) + 8ull * q.initial_cands +
+                        8ull * q.walk_entries + 4ull * q.num_roots;
     st->filter_bytes += cbits_bytes(g, P.k);  // candidate bitmap rows written by collect
   }
   st->tasks += hq->tasks_done;

@@ -72,6 +72,11 @@ struct DevGraph {
   uint64_t hub_row_words = 0;           // bucket_word_off[lab_buckets]
   bool hub_by_label = false;            // hub rows use the layout above (else by id)
   std::vector<uint64_t> label_count;  // vertices per label (host copy)
+  // Vertex ids grouped by label (ascending within a label) for labels below
+  // kMaxLabels, and where each label's group starts (host and device copies):
+  // the per-query filter sweeps visit only the vertices of the query's labels.
+  uint32_t *lverts = nullptr;              // [n]
+  std::vector<uint32_t> lvert_start;       // [min(num_labels, kMaxLabels) + 1]
   uint64_t bytes = 0;
 };
 
@@ -144,6 +149,10 @@ struct FilterQuery {
   unsigned long long *stat;       // [0] sum over u of final |C(u)|, [1] walk list entries
   uint32_t *cbits;               // the join's candidate bitmaps, written by collect (null: none)
   uint64_t cwords;               // words per bitmap row, ceil(n / 32)
+  // the query's distinct labels present in the graph: their vertex groups in
+  // DevGraph::lverts ([grp_lo, grp_hi)) and the query vertices carrying them
+  uint32_t ngrp;
+  uint32_t grp_lo[kMaxK], grp_hi[kMaxK], grp_mask[kMaxK];
 };
 
 // Query-side constants the join reads.
@@ -186,6 +195,9 @@ struct JoinQuery {
   // when use_labels is set; otherwise the join scans whole lists).
   uint32_t level_bucket[kMaxK];
   uint32_t use_labels;
+  // the vertex group (DevGraph::lverts range) of the label of the fast_last
+  // back neighbour's query vertex: its candidates all lie there
+  uint32_t lc_lo, lc_hi;
   // 1 + the level of the last vertex's only back neighbour when the last
   // level can be counted from per-vertex neighbour counts (one back edge and
   // cbits present); 0: the last level is always scanned.

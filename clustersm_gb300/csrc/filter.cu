@@ -75,10 +75,30 @@ __global__ void k_build_nlc(uint32_t n, const uint32_t *__restrict__ off, const 
 }
 
 // ------------------------------------------------------------ initial filter
-// Thread per data vertex (coalesced over labels and masks).  Candidates are
-// appended to per-u lists with one atomic per warp and query vertex.
-__global__ void __launch_bounds__(256) k_nlc_filter(uint32_t n, const uint32_t *__restrict__ off,
-                                                    const uint32_t *__restrict__ label,
+// A query's vertices to visit: its label groups laid end to end.  Returns the
+// vertex at position t (< total) and the query vertices carrying its label.
+__device__ __forceinline__ uint32_t group_vertex(const FilterQuery &Q, const uint32_t *__restrict__ lverts, uint32_t t,
+                                                 uint32_t &same) {
+  uint32_t i = 0;
+  while (t >= Q.grp_hi[i] - Q.grp_lo[i]) {
+    t -= Q.grp_hi[i] - Q.grp_lo[i];
+    ++i;
+  }
+  same = Q.grp_mask[i];
+  return lverts[Q.grp_lo[i] + t];
+}
+
+__device__ __forceinline__ uint32_t group_total(const FilterQuery &Q) {
+  uint32_t total = 0;
+  for (uint32_t i = 0; i < Q.ngrp; ++i) total += Q.grp_hi[i] - Q.grp_lo[i];
+  return total;
+}
+
+// Thread per data vertex of the query's labels (the masks start at zero, so
+// other vertices are never touched).  Candidates are appended to per-u lists
+// with one atomic per warp and query vertex.
+__global__ void __launch_bounds__(256) k_nlc_filter(const uint32_t *__restrict__ lverts,
+                                                    const uint32_t *__restrict__ off,
                                                     const uint8_t *__restrict__ nlc, uint32_t stride,
                                                     const FilterQuery *__restrict__ qs) {
   __shared__ FilterQuery Q;
@@ -87,27 +107,24 @@ __global__ void __launch_bounds__(256) k_nlc_filter(uint32_t n, const uint32_t *
     reinterpret_cast<uint32_t *>(&Q)[i] = reinterpret_cast<const uint32_t *>(src)[i];
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  const uint32_t k = Q.k;
-  const uint32_t total = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += total) {
-    const uint32_t v = base + threadIdx.x;
-    uint32_t mask = 0;
-    if (v < n) {
-      const uint32_t lv = label[v];
+  const uint32_t total = group_total(Q);
+  const uint32_t step = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += step) {
+    const uint32_t t = base + threadIdx.x;
+    uint32_t mask = 0, v = 0;
+    if (t < total) {
       uint32_t same = 0;
-      for (uint32_t u = 0; u < k; ++u) same |= (Q.label[u] == lv) ? (1u << u) : 0u;
-      if (same) {
-        const uint32_t dv = off[v + 1] - off[v];
-        const uint8_t *row = nlc + static_cast<size_t>(v) * stride;
-        for (uint32_t b = same; b; b &= b - 1) {
-          const uint32_t u = __ffs(b) - 1;
-          if (Q.deg[u] > dv) continue;
-          bool ok = true;
-          for (uint32_t i = 0; i < Q.nnlc[u] && ok; ++i) ok = row[Q.nlc_label[u][i]] >= Q.nlc_count[u][i];
-          if (ok) mask |= 1u << u;
-        }
+      v = group_vertex(Q, lverts, t, same);
+      const uint32_t dv = off[v + 1] - off[v];
+      const uint8_t *row = nlc + static_cast<size_t>(v) * stride;
+      for (uint32_t b = same; b; b &= b - 1) {
+        const uint32_t u = __ffs(b) - 1;
+        if (Q.deg[u] > dv) continue;
+        bool ok = true;
+        for (uint32_t i = 0; i < Q.nnlc[u] && ok; ++i) ok = row[Q.nlc_label[u][i]] >= Q.nlc_count[u][i];
+        if (ok) mask |= 1u << u;
       }
-      Q.vmask[v] = mask;
+      if (mask) Q.vmask[v] = mask;
     }
     // warp-aggregated appends, one atomic per query vertex present in the warp
     uint32_t any = __reduce_or_sync(0xFFFFFFFFu, mask);
@@ -312,11 +329,12 @@ __global__ void __launch_bounds__(256) k_walk_chunks(const uint32_t *__restrict_
 }
 
 // --------------------------------------------------------------- collect
-// Thread per vertex: bit u of the final mask is the bit of u's last slot.
-// Vertices with no initial candidate bit are skipped (the bitmap can only
-// hold bits the initial filter allowed).  Root candidates are appended with
+// Thread per vertex of the query's labels: bit u of the final mask is the
+// bit of u's last slot.  Vertices with no initial candidate bit are skipped
+// (the bitmap can only hold bits the initial filter allowed).  Root candidates are appended with
 // a warp-aggregated atomic.
-__global__ void __launch_bounds__(256) k_collect(uint32_t n, const FilterQuery *__restrict__ qs) {
+__global__ void __launch_bounds__(256) k_collect(const uint32_t *__restrict__ lverts,
+                                                 const FilterQuery *__restrict__ qs) {
   __shared__ uint32_t last_slot[kMaxK];
   const FilterQuery &Q = qs[blockIdx.y];
   if (threadIdx.x < kMaxK) last_slot[threadIdx.x] = Q.last_slot[threadIdx.x];
@@ -326,11 +344,14 @@ __global__ void __launch_bounds__(256) k_collect(uint32_t n, const FilterQuery *
   uint32_t *const vmask = Q.vmask;
   const uint32_t *const enc = Q.enc;
   unsigned long long ncand = 0;
-  const uint32_t total = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += total) {
-    const uint32_t v = base + threadIdx.x;
-    uint32_t cm = 0;
-    if (v < n) {
+  const uint32_t total = group_total(Q);
+  const uint32_t step = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += step) {
+    const uint32_t t = base + threadIdx.x;
+    uint32_t cm = 0, v = 0;
+    if (t < total) {
+      uint32_t same = 0;
+      v = group_vertex(Q, lverts, t, same);
       const uint32_t m0 = vmask[v];
       for (uint32_t b = m0; b; b &= b - 1) {
         const uint32_t u = __ffs(b) - 1;
@@ -338,17 +359,10 @@ __global__ void __launch_bounds__(256) k_collect(uint32_t n, const FilterQuery *
       }
       if (m0 != cm) vmask[v] = cm;
       ncand += __popc(cm);
-    }
-    // the join's candidate bitmaps: the warp's 32 consecutive vertices give
-    // one word of each query vertex's row
-    const uint32_t v0 = base + (threadIdx.x & ~31u);  // the warp's first vertex (uniform)
-    if (Q.cbits && v0 < n) {
-      uint32_t mine = 0;
-      for (uint32_t u = 0; u < Q.k; ++u) {
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, (cm >> u) & 1u);
-        if (lane == u) mine = b;
-      }
-      if (lane < Q.k) Q.cbits[lane * Q.cwords + v0 / 32] = mine;
+      // the join's candidate bitmaps (zero on entry): one bit per (u, v)
+      if (Q.cbits)
+        for (uint32_t b = cm; b; b &= b - 1)
+          atomicOr(Q.cbits + (__ffs(b) - 1) * Q.cwords + (v >> 5), 1u << (v & 31));
     }
     const bool is_root = (cm >> root) & 1u;
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, is_root);
@@ -404,6 +418,23 @@ smg_status fill_filter_query(const Plan &P, const DevGraph &g, FilterQuery &fq) 
       ++c;
     }
     fq.nnlc[u] = c;
+  }
+  // the vertex groups of the query's labels (a label the graph lacks, or
+  // carries on no vertex, has none)
+  uint32_t grp_label[kMaxK];
+  for (uint32_t u = 0; u < P.k; ++u) {
+    const uint32_t l = P.label[u];
+    if (l + 1 >= g.lvert_start.size() || g.lvert_start[l] == g.lvert_start[l + 1]) continue;
+    uint32_t i = 0;
+    while (i < fq.ngrp && grp_label[i] != l) ++i;
+    if (i == fq.ngrp) {
+      grp_label[i] = l;
+      fq.grp_lo[i] = g.lvert_start[l];
+      fq.grp_hi[i] = g.lvert_start[l + 1];
+      fq.grp_mask[i] = 0;
+      ++fq.ngrp;
+    }
+    fq.grp_mask[i] |= 1u << u;
   }
   return SMG_OK;
 }
@@ -600,7 +631,7 @@ smg_status launch_nlc_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_
   if (!nq || !g.n) return SMG_OK;
   for (uint32_t y0 = 0; y0 < nq; y0 += 65535) {
     const uint32_t ny = std::min<uint32_t>(65535, nq - y0);
-    k_nlc_filter<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.n, g.off, g.label, g.nlc, g.nlc_stride,
+    k_nlc_filter<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.lverts, g.off, g.nlc, g.nlc_stride,
                                                                          d_qs + y0);
     SMG_CUDA(cudaGetLastError());
   }
@@ -639,7 +670,7 @@ smg_status launch_collect(const DevGraph &g, const FilterQuery *d_qs, uint32_t n
   if (!nq || !g.n) return SMG_OK;
   for (uint32_t y0 = 0; y0 < nq; y0 += 65535) {
     const uint32_t ny = std::min<uint32_t>(65535, nq - y0);
-    k_collect<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.n, d_qs + y0);
+    k_collect<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.lverts, d_qs + y0);
     SMG_CUDA(cudaGetLastError());
   }
   return SMG_OK;

@@ -193,6 +193,7 @@ constexpr uint32_t kLastCountMaxDeg = 8192;
 // (four independent list entries per lane per step).
 __global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict__ queries,
                                                      const uint32_t *__restrict__ list, uint32_t nq,
+                                                     const uint32_t *__restrict__ lverts,
                                                      const uint32_t *__restrict__ off,
                                                      const uint32_t *__restrict__ adj,
                                                      const uint32_t *__restrict__ adjl,
@@ -210,12 +211,14 @@ __global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict
     const uint32_t *row = Q.cbits + ul * Q.cwords;
     const uint32_t bk = Q.level_bucket[Q.k - 1];
     uint32_t *cnt = Q.lastcnt;
-    for (uint64_t v0 = static_cast<uint64_t>(warp) * 32; v0 < n; v0 += static_cast<uint64_t>(nwarps) * 32) {
-      const uint64_t v = v0 + lane;
-      const uint32_t mine = v < n ? cnt[v] : 0u;  // the final mask, until overwritten below
+    // the candidates of order[b] all carry its label: walk that label's group
+    for (uint32_t t0 = Q.lc_lo + warp * 32; t0 < Q.lc_hi; t0 += nwarps * 32) {
+      const uint32_t t = t0 + lane;
+      const uint32_t v = t < Q.lc_hi ? __ldg(lverts + t) : 0u;
+      const uint32_t mine = t < Q.lc_hi ? cnt[v] : 0u;  // the final mask, until overwritten below
       for (uint32_t bal = __ballot_sync(0xFFFFFFFFu, (mine >> ub) & 1u); bal; bal &= bal - 1) {
         const uint32_t src = __ffs(bal) - 1;
-        const uint64_t x = v0 + src;
+        const uint32_t x = __shfl_sync(0xFFFFFFFFu, v, src);
         // the neighbours of x with the last vertex's label bucket (its run
         // when x has a run table, else the whole list)
         uint32_t beg = __ldg(off + x), end = __ldg(off + x + 1);
@@ -1257,6 +1260,7 @@ void set_graph(JoinLaunch &jl, const DevGraph &g) {
   jl.lab_off = g.lab_off;
   jl.lab_buckets = g.lab_buckets;
   jl.label = g.label;
+  jl.lverts = g.lverts;
   jl.lab_rank = g.hub_by_label ? g.lab_rank : nullptr;
   jl.bucket_word_off = g.hub_by_label ? g.bucket_word_off : nullptr;
   jl.n = g.n;
@@ -1349,8 +1353,8 @@ smg_status launch_join_prep(const JoinLaunch &jl, cudaStream_t s, int num_sms) {
   const uint32_t want = std::max<uint32_t>(1, static_cast<uint32_t>(std::max(num_sms, 1)) * 16 / nq);
   const uint32_t span = static_cast<uint32_t>((static_cast<uint64_t>(jl.n) + 255) / 256);  // 32 vertices a warp
   const dim3 g2(std::min(span, want), std::min<uint32_t>(nq, 65535));
-  k_last_counts<<<g2, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.off, jl.adj, jl.adjl, jl.lab_of, jl.lab_off,
-                                    jl.lab_buckets, jl.n, jl.qs);
+  k_last_counts<<<g2, 256, 0, s>>>(jl.queries, jl.seed_list, nq, jl.lverts, jl.off, jl.adj, jl.adjl, jl.lab_of,
+                                    jl.lab_off, jl.lab_buckets, jl.n, jl.qs);
   SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }

@@ -43,6 +43,7 @@ struct JoinLaunch {
   const uint32_t *lab_of, *lab_off;
   uint32_t lab_buckets;
   const uint32_t *label;     // vertex labels (bucket of a probed vertex without a level bucket)
+  const uint32_t *lverts;    // vertex ids grouped by label (DevGraph::lverts)
   const uint32_t *lab_rank, *bucket_word_off;  // hub bitmap layout by label (null: by id)
   uint32_t probe_runs;       // membership probes search label runs (SMG_PROBE=runs)
   uint32_t hoist;            // hoisted last-level sets (count-only runs; SMG_HOIST=0: off)

@@ -329,7 +329,9 @@ smg_status admit(smg_server *s) {
     rc = smg::append_filter_steps(*sl.plan, i, fb);
     if (rc) return rc;
     hseed[i] = idx;
+    SMG_CUDA(cudaMemsetAsync(b.vmask, 0, fps[i].vmask, st));  // the filter writes candidates only
     SMG_CUDA(cudaMemsetAsync(b.enc, 0, fps[i].enc, st));
+    SMG_CUDA(cudaMemsetAsync(b.cbits, 0, fps[i].cbits, st));
     SMG_CUDA(cudaMemsetAsync(b.counters, 0, sizeof(smg::QCounters), st));
     SMG_CUDA(cudaMemcpyAsync(s->d_jq + idx, hj + i, sizeof(smg::JoinQuery), cudaMemcpyHostToDevice, st));
   }
