@@ -327,61 +327,132 @@ namespace {
 
 uint64_t label_cands(const DevGraph &g, uint32_t l) { return l < g.label_count.size() ? g.label_count[l] : 0; }
 
-bool use_plan_order() {
-  static const bool v = [] {
+uint32_t order_mode() {  // 0 cost-based with counted endings, 1 greedy only, 2 the reference's
+  static const uint32_t v = [] {
     const char *e = std::getenv("SMG_JOIN_ORDER");
-    return e && std::strcmp(e, "plan") == 0;
+    if (e && std::strcmp(e, "plan") == 0) return 2u;
+    if (e && std::strcmp(e, "greedy") == 0) return 1u;
+    return 0u;
   }();
   return v;
 }
 
-}  // namespace
-
-// First vertex of the join's matching order: the fewest candidates (data
-// vertices with its label) per query edge; ties go to the lower index.
-uint32_t join_root(const Plan &P, const DevGraph &g) {
-  if (use_plan_order()) return P.root;
-  uint32_t root = 0;
-  for (uint32_t u = 1; u < P.k; ++u)
-    if (label_cands(g, P.label[u]) * P.deg[root] < label_cands(g, P.label[root]) * P.deg[u]) root = u;
-  return root;
+// Greedy order of the query vertices in `allowed` (a connected set): first
+// the one with the fewest label candidates per query edge, then repeatedly
+// the one with the most edges back to those placed, then the fewest
+// candidates, then the highest degree.  Writes order[at ..] and returns the
+// next position.
+uint32_t greedy_order(const Plan &P, const DevGraph &g, uint32_t allowed, uint32_t *order, uint32_t at) {
+  const uint32_t k = P.k;
+  uint32_t root = kNone;
+  for (uint32_t u = 0; u < k; ++u)
+    if ((allowed >> u) & 1u)
+      if (root == kNone || label_cands(g, P.label[u]) * P.deg[root] < label_cands(g, P.label[root]) * P.deg[u])
+        root = u;
+  uint32_t placed = 1u << root;
+  order[at++] = root;
+  while (placed != allowed) {
+    uint32_t best = kNone, best_back = 0;
+    for (uint32_t u = 0; u < k; ++u) {
+      if (!((allowed >> u) & 1u) || ((placed >> u) & 1u)) continue;
+      uint32_t nb = 0;
+      for (uint32_t e = P.q_off[u]; e < P.q_off[u + 1]; ++e) nb += (placed >> P.q_nbr[e]) & 1u;
+      if (!nb) continue;
+      bool better = best == kNone || nb > best_back;
+      if (!better && nb == best_back) {
+        const uint64_t cu = label_cands(g, P.label[u]), cb = label_cands(g, P.label[best]);
+        better = cu < cb || (cu == cb && P.deg[u] > P.deg[best]);
+      }
+      if (better) {
+        best = u;
+        best_back = nb;
+      }
+    }
+    order[at++] = best;  // `allowed` is connected, so one is adjacent
+    placed |= 1u << best;
+  }
+  return at;
 }
 
-// The join's matching order.  Every connected order yields the same
-// embeddings, so the join takes one chosen for the resident graph instead of
-// the order the reference's edge order (order.cpp getBFSEdgeOrder) reaches
-// the vertices in: after join_root, each next vertex has the most edges back
-// to the vertices already placed, then the fewest candidates, then the
-// highest degree.  SMG_JOIN_ORDER=plan selects the reference-derived order.
+uint32_t nbr_mask(const Plan &P, uint32_t u) {
+  uint32_t m = 0;
+  for (uint32_t e = P.q_off[u]; e < P.q_off[u + 1]; ++e) m |= 1u << P.q_nbr[e];
+  return m;
+}
+
+bool connected(const Plan &P, uint32_t set) {
+  if (!set) return false;
+  uint32_t seen = set & (~set + 1), frontier = seen;
+  while (frontier) {
+    uint32_t next = 0;
+    for (uint32_t f = frontier; f; f &= f - 1) next |= nbr_mask(P, __builtin_ctz(f)) & set;
+    frontier = next & ~seen;
+    seen |= next;
+  }
+  return seen == set;
+}
+
+// The join's matching order (every connected order yields the same
+// embeddings).  It ends, where the query allows, so that the last level is
+// counted rather than enumerated: with a leaf (one back edge: per-vertex
+// neighbour counts), else with two non-adjacent vertices (the last vertex
+// does not depend on the level before it: one hoisted set per prefix);
+// among several, the ending vertex with the most candidates.  The rest, and
+// queries with neither, take the greedy order.  SMG_JOIN_ORDER=greedy keeps
+// the greedy order throughout, =plan the order the reference's edge order
+// (order.cpp getBFSEdgeOrder) reaches the vertices in.
+void compute_order(const Plan &P, const DevGraph &g, uint32_t *order) {
+  const uint32_t k = P.k, all = k >= 32 ? 0xFFFFFFFFu : (1u << k) - 1;
+  if (order_mode() == 2) {
+    for (uint32_t l = 0; l < k; ++l) order[l] = P.order[l];
+    return;
+  }
+  if (order_mode() == 0 && k >= 3) {
+    uint32_t leaf = kNone;
+    for (uint32_t u = 0; u < k; ++u)
+      if (P.deg[u] == 1 && (leaf == kNone || label_cands(g, P.label[u]) > label_cands(g, P.label[leaf]))) leaf = u;
+    if (leaf != kNone) {
+      greedy_order(P, g, all & ~(1u << leaf), order, 0);
+      order[k - 1] = leaf;
+      return;
+    }
+    if (k >= 4) {
+      uint32_t bx = kNone, by = kNone;
+      for (uint32_t y = 0; y < k; ++y)
+        for (uint32_t x = 0; x < k; ++x) {
+          if (x == y || ((nbr_mask(P, y) >> x) & 1u)) continue;
+          if (!connected(P, all & ~(1u << x) & ~(1u << y))) continue;
+          const uint64_t cy = label_cands(g, P.label[y]), cx = label_cands(g, P.label[x]);
+          if (by == kNone || cy > label_cands(g, P.label[by]) ||
+              (cy == label_cands(g, P.label[by]) && cx > label_cands(g, P.label[bx]))) {
+            bx = x;
+            by = y;
+          }
+        }
+      if (by != kNone) {
+        greedy_order(P, g, all & ~(1u << bx) & ~(1u << by), order, 0);
+        order[k - 2] = bx;
+        order[k - 1] = by;
+        return;
+      }
+    }
+  }
+  greedy_order(P, g, all, order, 0);
+}
+
+}  // namespace
+
+// The first vertex of the join's matching order (its candidates are the root list).
+uint32_t join_root(const Plan &P, const DevGraph &g) {
+  uint32_t order[kMaxK];
+  compute_order(P, g, order);
+  return order[0];
+}
+
 void join_order(const Plan &P, const DevGraph &g, uint32_t *order, uint32_t *back, uint32_t *same) {
   const uint32_t k = P.k;
   std::vector<uint32_t> level(k, kNone);
-  if (use_plan_order()) {
-    for (uint32_t l = 0; l < k; ++l) order[l] = P.order[l];
-  } else {
-    order[0] = join_root(P, g);
-    level[order[0]] = 0;
-    for (uint32_t l = 1; l < k; ++l) {
-      uint32_t best = kNone, best_back = 0;
-      for (uint32_t u = 0; u < k; ++u) {
-        if (level[u] != kNone) continue;
-        uint32_t nb = 0;
-        for (uint32_t e = P.q_off[u]; e < P.q_off[u + 1]; ++e) nb += level[P.q_nbr[e]] != kNone;
-        if (!nb) continue;
-        bool better = best == kNone || nb > best_back;
-        if (!better && nb == best_back) {
-          const uint64_t cu = label_cands(g, P.label[u]), cb = label_cands(g, P.label[best]);
-          better = cu < cb || (cu == cb && P.deg[u] > P.deg[best]);
-        }
-        if (better) {
-          best = u;
-          best_back = nb;
-        }
-      }
-      order[l] = best;  // a connected query always has one
-      level[best] = l;
-    }
-  }
+  compute_order(P, g, order);
   for (uint32_t l = 0; l < k; ++l) level[order[l]] = l;
   for (uint32_t l = 0; l < k; ++l) {
     const uint32_t u = order[l];

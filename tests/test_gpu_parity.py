@@ -190,16 +190,18 @@ sys.exit(1 if bad else 0)
 """
 
 
-def test_reference_edge_order_gives_same_counts(ctx):
+@pytest.mark.parametrize("mode", ["plan", "greedy"])
+def test_other_join_orders_give_same_counts(ctx, mode):
     """SMG_JOIN_ORDER=plan matches vertices in the order the reference's edge
-    order (order.cpp getBFSEdgeOrder) reaches them instead of the cost-based
-    order; the counts are the same (the setting is read once per process)."""
+    order (order.cpp getBFSEdgeOrder) reaches them, =greedy in the cost-based
+    order without the counted ending; the counts are the same (the setting is
+    read once per process)."""
     import os
     import subprocess
     import sys
     from pathlib import Path
     root = Path(__file__).resolve().parents[1]
-    env = dict(os.environ, SMG_JOIN_ORDER="plan")
+    env = dict(os.environ, SMG_JOIN_ORDER=mode)
     r = subprocess.run([sys.executable, "-c", PLAN_ORDER_SCRIPT, str(root)], env=env, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
