@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-rates", default="100,1000,5000")
+    ap.add_argument("--tune", action="store_true",
+                    help="run the library's per-shape-class autotuner on the workload before timing (untimed)")
     return ap.parse_args()
 
 
@@ -145,7 +147,8 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=512):
     for rate in rates:
         rng = random.Random(f"serve-{rate}")
         n = max(64, min(max_requests, int(rate * seconds)))
-        srv = Server(ctx, dev, max_inflight=512, memory_budget_bytes=64 << 30)
+        srv = Server(ctx, dev, max_inflight=512, memory_budget_bytes=64 << 30,
+                     max_query_vertices=max(p.view.k for p in plans))
         tickets = []
         t_next = time.perf_counter()
         while len(tickets) < n:
@@ -241,6 +244,11 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    tuning = None
+    if args.tune:  # setup, outside the timed region
+        tuning = [{"shape_class": e.shape_class, "root_chunk": e.root_chunk, "donate_min": e.donate_min,
+                   "best_ms": e.best_ms, "default_ms": e.default_ms}
+                  for e in native.autotune(ctx, dev, plans) if e.samples]
     # correctness against the committed counts before timing
     counts, _ = native.match_batch(ctx, dev, plans)
     want = [expected[i] for i in mine]
@@ -341,6 +349,7 @@ def main():
                          "traffic_frac": traffic / (join_ms / args.steps / 1e3) / 1e9 / peak if traffic and join_ms
                          else None},
             "clocks": clocks,
+            "tuning": tuning,
             "serving": serve,
         }
         if not args.no_cpu_baseline:

@@ -845,6 +845,12 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     budget += free_b > kHeadroomBytes ? free_b - kHeadroomBytes : free_b / 2;
   }
+  // SMG_MAX_BATCH_BYTES caps what one chunk may use (a chunk holds at least
+  // one query whatever the cap)
+  if (const char *cap = std::getenv("SMG_MAX_BATCH_BYTES")) {
+    const unsigned long long v = std::strtoull(cap, nullptr, 10);
+    if (v) budget = std::min<size_t>(budget, v);
+  }
   const size_t max_q = kPinnedBytes / (sizeof(FilterQuery) + sizeof(JoinQuery) + sizeof(QCounters));
   uint32_t a = 0;
   while (a < nq) {

@@ -1166,10 +1166,12 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
 // registers for resident warps.  On the 2^22 R-MAT workload (scanning whole
 // lists), 8 blocks of 8 warps per SM (32 registers, a 476-byte spill)
 // measured 501 queries/s, 6 blocks (40 registers) 426 and 4 blocks (64
-// registers) 357; the compiler's own choice, 80 registers, fits 3.  With the
-// label index, 6 and 8 blocks run at the same speed and 6 spills less (its
-// local-memory traffic reaches DRAM), so 6 is the default.  A launch takes
-// the most blocks its shared memory allows; SMG_JOIN_OCCUPANCY=4|6|8 caps it.
+// registers) 357; the compiler's own choice, 80 registers, fits 3.  Once the
+// label index, counted and hoisted last levels removed most of the list
+// scanning, the spills cost more than the extra warps gain: 4 blocks (64
+// registers, no spill to speak of) measured 3,647 queries/s, 6 blocks 3,453
+// and 8 blocks 3,477, so 4 is the default.  A launch takes the most blocks
+// its shared memory allows; SMG_JOIN_OCCUPANCY=4|6|8 caps it.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 8) k_join(JoinLaunch p) { join_body(p); }
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_join6(JoinLaunch p) { join_body(p); }
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 4) k_join4(JoinLaunch p) { join_body(p); }
@@ -1279,7 +1281,7 @@ using JoinKernel = void (*)(JoinLaunch);
 uint32_t occupancy_cap() {
   static const uint32_t cap = [] {
     const char *e = std::getenv("SMG_JOIN_OCCUPANCY");
-    const int v = e ? std::atoi(e) : 6;
+    const int v = e ? std::atoi(e) : 4;
     return static_cast<uint32_t>(v >= 8 ? 8 : v >= 6 ? 6 : 4);
   }();
   return cap;

@@ -40,7 +40,6 @@ double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-constexpr uint32_t kServerK = smg::kMaxK;  // task width covers any query
 
 struct Request {
   uint64_t ticket;
@@ -133,6 +132,7 @@ struct smg_server {
   unsigned int *walk_count = nullptr;
   uint4 *walk_items = nullptr;
   uint32_t cap = 0, cur = 0;
+  uint32_t kmax = smg::kMaxK;  // task width: the largest query accepted
   uint64_t slice_ns = 0, slice_min_ns = 0;
   cudaEvent_t ev = nullptr;
   bool inflight = false, bell_rung = false;
@@ -170,7 +170,7 @@ namespace {
 
 using smg::fail;
 
-uint32_t task_words() { return 4 + kServerK; }
+uint32_t task_words(const smg_server *s) { return 4 + s->kmax; }
 
 smg::WalkOverflow walk_overflow(smg_server *s) {
   smg::WalkOverflow w;
@@ -187,7 +187,7 @@ smg::JoinLaunch join_launch(smg_server *s) {
   smg::set_graph(jl, g);
   jl.queries = s->d_jq;
   jl.nq = s->cfg.max_inflight;
-  jl.kmax = kServerK;
+  jl.kmax = s->kmax;
   jl.qs = s->qs;
   jl.tasks = s->tasks[s->cur];
   jl.ready = s->ready[s->cur];
@@ -260,7 +260,7 @@ void maybe_ring(smg_server *s) {
 smg_status end_slice(smg_server *s) {
   cudaStream_t st = s->ctx->stream;
   const uint32_t other = 1 - s->cur;
-  smg_status rc = smg::launch_compact(s->tasks[s->cur], s->ready[s->cur], s->cap, task_words(), s->tasks[other],
+  smg_status rc = smg::launch_compact(s->tasks[s->cur], s->ready[s->cur], s->cap, task_words(s), s->tasks[other],
                                       s->ready[other], s->next_count, s->qs, st, s->ctx->num_sms);
   if (rc) return rc;
   SMG_CUDA(cudaMemsetAsync(s->ready[s->cur], 0, static_cast<size_t>(s->cap) * 4, st));
@@ -438,6 +438,11 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   s->graph = g;
   if (cfg) s->cfg = *cfg;
   if (!s->cfg.max_inflight) s->cfg.max_inflight = 64;
+  if (s->cfg.max_query_vertices) {
+    if (s->cfg.max_query_vertices < 2 || s->cfg.max_query_vertices > smg::kMaxK)
+      return fail(SMG_ERR_INVALID, "max_query_vertices must be 2..32 (0: 32)");
+    s->kmax = s->cfg.max_query_vertices;
+  }
   const size_t per_rec = sizeof(smg::FilterQuery) + sizeof(smg::JoinQuery) + 4;
   if (s->cfg.max_inflight * per_rec > smg::kPinnedBytes) return fail(SMG_ERR_LIMIT, "max_inflight too large");
   size_t free_b = 0, total_b = 0;
@@ -446,7 +451,7 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   s->slice_ns = static_cast<uint64_t>(env_ms("SMG_SLICE_MS", 250.0) * 1e6);
   s->slice_min_ns = std::min(s->slice_ns, static_cast<uint64_t>(env_ms("SMG_SLICE_MIN_MS", 2.0) * 1e6));
   s->cap = 2u << 20;
-  const size_t tw = task_words();
+  const size_t tw = task_words(s.get());
   const uint32_t m = s->cfg.max_inflight;
   SMG_CUDA(cudaMalloc(&s->pool_mem, s->cfg.memory_budget_bytes));
   s->pool.init(s->pool_mem, s->cfg.memory_budget_bytes);
@@ -483,6 +488,7 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
 
 smg_status smg_server_submit(smg_server *s, const smg_plan *p, uint64_t *ticket) {
   if (!s || !p || !ticket) return fail(SMG_ERR_INVALID, "null argument");
+  if (p->p.k > s->kmax) return fail(SMG_ERR_LIMIT, "query larger than the server's max_query_vertices");
   const uint64_t bytes = smg::query_footprint(s->graph->g, p->p).total();
   if (bytes > s->cfg.memory_budget_bytes) return fail(SMG_ERR_BUDGET, "query exceeds the server memory budget");
   for (uint32_t u = 0; u < p->p.k; ++u)

@@ -94,7 +94,8 @@ class GraphStats(C.Structure):
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_inflight", C.c_uint32), ("reserved", C.c_uint32)]
+    _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_inflight", C.c_uint32),
+                ("max_query_vertices", C.c_uint32)]
 
 
 class ServerStats(C.Structure):
@@ -464,9 +465,10 @@ class Server:
     """Continuous-batching request loop (smg_server_*).  Plans must outlive
     their requests; this wrapper keeps a reference until the result is read."""
 
-    def __init__(self, ctx: Context, graph: DeviceGraph, memory_budget_bytes: int = 0, max_inflight: int = 0):
+    def __init__(self, ctx: Context, graph: DeviceGraph, memory_budget_bytes: int = 0, max_inflight: int = 0,
+                 max_query_vertices: int = 0):
         self.ctx, self.graph = ctx, graph
-        cfg = ServerConfig(memory_budget_bytes, max_inflight, 0)
+        cfg = ServerConfig(memory_budget_bytes, max_inflight, max_query_vertices)
         self._h = C.c_void_p()
         check(lib.smg_server_create(ctx.handle, graph.handle, C.byref(cfg), C.byref(self._h)), "smg_server_create")
         self._plans = {}

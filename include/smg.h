@@ -335,7 +335,9 @@ typedef struct smg_server smg_server;
 typedef struct smg_server_config {
   uint64_t memory_budget_bytes; /* HBM for per-request state; 0 = auto      */
   uint32_t max_inflight;        /* queries resident at once; 0 = auto        */
-  uint32_t reserved;
+  uint32_t max_query_vertices;  /* largest query accepted (2..32); 0 = 32.
+                                   Smaller values give the join smaller task
+                                   records and more resident warps.          */
 } smg_server_config;
 typedef struct smg_request_result {
   smg_status status;

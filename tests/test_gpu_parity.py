@@ -249,3 +249,19 @@ def test_hub_bitmap_layouts(ctx, monkeypatch, layout):
         checked += 1
     assert checked >= 10
     dev.free()
+
+
+def test_memory_bounded_chunks(ctx, monkeypatch):
+    """A batch whose state does not fit the memory cap runs as several
+    chunks (each its own filter pass and join launch) with the same counts."""
+    host = HostGraph.rmat(12, 16, 8, seed=7)
+    dev = DeviceGraph(ctx, host)
+    plans = [Plan(q) for q in small_queries(host, shapes=RMAT_SHAPES, ks=(4, 5), seeds=range(3))]
+    whole, st1 = native.match_batch(ctx, dev, plans, use_graph=False)
+    assert st1.chunks == 1
+    # the fixed queue bound (256 MB) plus room for a few queries per chunk
+    monkeypatch.setenv("SMG_MAX_BATCH_BYTES", str((256 << 20) + (256 << 10)))
+    parts, st2 = native.match_batch(ctx, dev, plans, use_graph=False)
+    assert st2.chunks > 1
+    assert parts.tolist() == whole.tolist()
+    dev.free()

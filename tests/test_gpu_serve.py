@@ -102,3 +102,18 @@ def test_cancel_and_budget(ctx, er):
     with pytest.raises(native.SmgError) as e:
         small.submit(plans[0])
     assert e.value.status == 10  # SMG_ERR_BUDGET
+
+
+def test_query_size_limit(ctx, er):
+    """A server built for queries of at most 4 vertices (smaller task records,
+    more resident warps) serves them exactly and rejects larger ones."""
+    dev, plans, want = er
+    srv = Server(ctx, dev, max_inflight=16, max_query_vertices=4)
+    tickets = [srv.submit(p) for p in plans[:12]]
+    big = Plan(native.Query([0, 1, 2, 3, 0], [0, 1, 1, 2, 2, 3, 3, 4]))
+    with pytest.raises(native.SmgError) as e:
+        srv.submit(big)
+    assert e.value.status == 5  # SMG_ERR_LIMIT
+    srv.drain()
+    assert [int(srv.poll(t).count) for t in tickets] == [int(w) for w in want[:12]]
+    srv.close()
