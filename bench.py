@@ -135,7 +135,7 @@ def cpu_baseline(host, queries, seconds):
                       f"{os.cpu_count()} OpenMP threads, {dt:.1f} s", "embeddings_per_s": emb / dt}
 
 
-def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=512):
+def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
     """Poisson arrivals into the continuous-batching server (smg_server_*).
     Per rate, requests cycle through the workload's queries with seeded
     exponential gaps; between arrivals the loop calls the non-blocking

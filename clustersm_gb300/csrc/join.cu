@@ -359,10 +359,12 @@ constexpr uint32_t kFromLabelIndex = 1u << 31;  // spiv flag: segment in adjl
 constexpr uint32_t kHoistScan = 1u << 30;       // spiv flag: keep entries found in the hoisted set
 constexpr uint32_t kHoistSet = 1u << 29;        // spiv flag: the segment is the hoisted set itself
 
+#ifdef SMG_CHECKED
 // Self-checking build: does `e` point into adj or adjl?
 __device__ __forceinline__ bool in_lists(const JoinLaunch &p, const uint32_t *e) {
   return (e >= p.adj && e < p.adj + p.m2) || (p.adjl && e >= p.adjl && e < p.adjl + p.m2);
 }
+#endif
 
 // The list that level `level` scans: the neighbours of matched vertex x (its
 // id-ordered list starts at beg and holds deg entries), narrowed to the run
