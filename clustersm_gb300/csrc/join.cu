@@ -542,9 +542,11 @@ __device__ __forceinline__ bool in_hoisted(const WarpView &S, uint32_t n, uint32
 // does not depend on the level-P vertex, so a warp builds it once per prefix
 // and every batch of level-P candidates reuses it.  It is the shortest fixed
 // back neighbour's run filtered by the others, so it comes out sorted by id.
-// Sets *S.xlen to its size, or kHoistTooBig past kHoistCap entries.
+// Sets *S.xlen to its size, or kHoistTooBig past kHoistCap entries.  With
+// store false only its size is needed (the last vertex does not depend on
+// level P) and there is no cap.
 __device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery &Q, const CandView &cv,
-                              uint32_t P, uint32_t fixed, uint32_t lane, unsigned long long &scanned,
+                              uint32_t P, uint32_t fixed, bool store, uint32_t lane, unsigned long long &scanned,
                               uint32_t &probes) {
   const uint32_t L = P + 1;
   const uint32_t bucket = Q.use_labels ? S.lbk[L] : kNone;
@@ -577,11 +579,13 @@ __device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery 
       }
     }
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
-    if (n + __popc(bal) > kHoistCap) {
-      n = kHoistTooBig;
-      break;
+    if (store) {
+      if (n + __popc(bal) > kHoistCap) {
+        n = kHoistTooBig;
+        break;
+      }
+      if (good) S.xs[n + __popc(bal & lt)] = w;
     }
-    if (good) S.xs[n + __popc(bal & lt)] = w;
     n += __popc(bal);
   }
   __syncwarp();
@@ -602,9 +606,10 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
   const bool fast_ok = Q.fast_last && !p.emit;  // k_last_counts ran only then
   // several back edges, some to levels before P: the hoisted set of the prefix
   const uint32_t fixed = S.bmask[L] & ((1u << P) - 1);
+  const bool p_indep = !((S.bmask[L] >> P) & 1u);  // u_L not adjacent to level P: only |X| matters
   uint32_t xn = kHoistTooBig;
   if (p.hoist && !p.emit && !Q.fast_last && fixed) {
-    if (*S.xlen == kHoistInvalid) build_hoisted(S, p, Q, cv, P, fixed, lane, scanned, probes);
+    if (*S.xlen == kHoistInvalid) build_hoisted(S, p, Q, cv, P, fixed, !p_indep, lane, scanned, probes);
     xn = *S.xlen;
   }
   const bool use_x = xn != kHoistTooBig;
@@ -615,10 +620,21 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
     bool counted = false;
     if (use_x) {
       const uint32_t vb = __ldg(p.off + v), vd = __ldg(p.off + v + 1) - vb;
-      if (!((S.bmask[L] >> P) & 1u)) {
+      if (p_indep) {
         // u_L is not adjacent to level P: every candidate sees the whole set,
-        // less itself when it has u_L's label
-        fast = xn - (((S.slab[L] >> P) & 1u) && in_hoisted(S, xn, v) ? 1u : 0u);
+        // less itself when it has u_L's label and belongs to the set (tested
+        // directly: the set may be counted rather than stored)
+        bool member = false;
+        if ((S.slab[L] >> P) & 1u) {
+          const uint32_t u = S.ord[L];
+          member = cv.has(u, v);
+          for (uint32_t b = S.slab[L] & ((1u << P) - 1); b && member; b &= b - 1) member = S.m[__ffs(b) - 1] != v;
+          for (uint32_t b = fixed; b && member; b &= b - 1) {
+            const uint32_t j = __ffs(b) - 1;
+            member = is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, v, probes);
+          }
+        }
+        fast = xn - (member ? 1u : 0u);
         counted = true;
       } else {
         // |X & N(v)|: walk v's run keeping members of X, or walk X probing
