@@ -302,7 +302,7 @@ struct Chunk {
   uint32_t a = 0, b = 0, kmax = 0, cap = 0;
   size_t zero_bytes = 0, total = 0;
   QueueState *qs = nullptr;
-  uint32_t *ready = nullptr, *tasks = nullptr, *emb = nullptr;
+  uint32_t *ready = nullptr, *tasks = nullptr, *emb = nullptr, *xbuf = nullptr;
   QCounters *counters = nullptr;
   unsigned int *walk_count = nullptr;  // one zeroed counter pair per walk phase
   uint4 *walk_items = nullptr;
@@ -599,6 +599,8 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   }
   const size_t o_tasks = off;
   off += al(static_cast<size_t>(ch.cap) * (4 + ch.kmax) * 4);
+  const size_t o_xbuf = off;  // the join warps' hoisted-set buffers
+  off += al(hoist_buffer_bytes(c->num_sms));
   ch.walk_cap = kWalkCap;
   const size_t o_witems = off;
   off += al(static_cast<size_t>(ch.walk_cap) * sizeof(uint4));
@@ -618,6 +620,7 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   ch.walk_count = reinterpret_cast<unsigned int *>(B + o_wcnt);
   ch.walk_items = reinterpret_cast<uint4 *>(B + o_witems);
   ch.tasks = reinterpret_cast<uint32_t *>(B + o_tasks);
+  ch.xbuf = reinterpret_cast<uint32_t *>(B + o_xbuf);
   ch.fq = reinterpret_cast<FilterQuery *>(B + o_fq);
   ch.jq = reinterpret_cast<JoinQuery *>(B + o_jq);
   ch.emb = (o.emb_host && o.emb_cap) ? reinterpret_cast<uint32_t *>(B + o_emb) : nullptr;
@@ -694,6 +697,8 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
   jl.donate_min = 2;
   jl.time_limit_ns = time_limit_ns();
   jl.emit = ch.emb != nullptr;
+  jl.xbuf = ch.xbuf;
+  jl.xcap = kHoistGlobalCap;
   return jl;
 }
 
@@ -831,7 +836,8 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
                        QueryOut *out, RunStats *st) {
   SMG_CUDA(cudaSetDevice(c->device));
   if (o.emb_host && nq != 1) return fail(SMG_ERR_INVALID, "embeddings are returned by the plain path only");
-  const size_t per_chunk_fixed = (64ull << 20) * 4;  // queue storage of a chunk (bound)
+  // queue storage of a chunk (bound) and the join warps' hoisted-set buffers
+  const size_t per_chunk_fixed = (64ull << 20) * 4 + hoist_buffer_bytes(c->num_sms);
   // device memory is asked for only when the batch may not fit the arena
   // (cudaMemGetInfo is a driver round trip, too slow for every plain call)
   size_t need = per_chunk_fixed;

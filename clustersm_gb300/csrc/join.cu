@@ -325,6 +325,7 @@ __host__ __device__ inline uint32_t warp_words(uint32_t K) {
 struct WarpView {
   uint32_t *m, *beg, *deg, *hub, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *lbk, *batch;
   uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv, *xs, *xlen;
+  uint32_t xcap = kHoistCap;  // entries xs holds (xs may be moved to a global buffer)
   const uint32_t **lbase;
   __device__ WarpView(uint32_t *W, uint32_t K) {
     m = W;
@@ -542,7 +543,7 @@ __device__ __forceinline__ bool in_hoisted(const WarpView &S, uint32_t n, uint32
 // does not depend on the level-P vertex, so a warp builds it once per prefix
 // and every batch of level-P candidates reuses it.  It is the shortest fixed
 // back neighbour's run filtered by the others, so it comes out sorted by id.
-// Sets *S.xlen to its size, or kHoistTooBig past kHoistCap entries.  With
+// Sets *S.xlen to its size, or kHoistTooBig past the warp's S.xcap entries.  With
 // store false only its size is needed (the last vertex does not depend on
 // level P) and there is no cap.
 __device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery &Q, const CandView &cv,
@@ -580,7 +581,7 @@ __device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery 
     }
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
     if (store) {
-      if (n + __popc(bal) > kHoistCap) {
+      if (n + __popc(bal) > S.xcap) {
         n = kHoistTooBig;
         break;
       }
@@ -923,6 +924,10 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint32_t K = p.kmax, tw = 4 + K;
   WarpView S(smem + wib * warp_words(K), K);
+  if (p.xbuf) {  // a larger hoisted-set buffer of this warp's own in global memory
+    S.xs = p.xbuf + (static_cast<uint64_t>(blockIdx.x) * kWarpsPerBlock + wib) * p.xcap;
+    S.xcap = p.xcap;
+  }
   const uint32_t lt = (1u << lane) - 1;
   QueueState *qs = p.qs;
   volatile int *vabort = &qs->abort;
@@ -1286,6 +1291,11 @@ void set_graph(JoinLaunch &jl, const DevGraph &g) {
   jl.n = g.n;
   jl.m2 = g.m2;
   jl.num_hubs = g.num_hubs;
+}
+
+size_t hoist_buffer_bytes(int num_sms) {
+  // at most 8 resident blocks of kWarpsPerBlock warps per SM
+  return static_cast<size_t>(std::max(num_sms, 1)) * 8 * kWarpsPerBlock * kHoistGlobalCap * sizeof(uint32_t);
 }
 
 size_t join_queue_bytes(uint32_t cap, uint32_t kmax) {

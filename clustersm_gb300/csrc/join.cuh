@@ -47,6 +47,11 @@ struct JoinLaunch {
   const uint32_t *lab_rank, *bucket_word_off;  // hub bitmap layout by label (null: by id)
   uint32_t probe_runs;       // membership probes search label runs (SMG_PROBE=runs)
   uint32_t hoist;            // hoisted last-level sets (count-only runs; SMG_HOIST=0: off)
+  // per resident warp, room for a stored hoisted set of xcap entries (global
+  // memory, [blocks x warps per block][xcap]); null: the warp's shared
+  // memory, 256 entries
+  uint32_t *xbuf;
+  uint32_t xcap;
   uint32_t n;                // data vertices (bounds of the self-checking build)
   uint64_t m2;               // adjacency entries
   uint32_t num_hubs;
@@ -79,6 +84,10 @@ struct JoinLaunch {
 // The resident graph's arrays in a launch record (every launch site uses
 // this, so the hub bitmap layout and the label index always travel together).
 void set_graph(JoinLaunch &jl, const DevGraph &g);
+// Entries of a warp's hoisted-set buffer in global memory, and the bytes of
+// such buffers for every warp a join launch on num_sms SMs can have.
+constexpr uint32_t kHoistGlobalCap = 4096;
+size_t hoist_buffer_bytes(int num_sms);
 // Bytes of queue storage for `cap` tasks of a batch whose largest query has
 // kmax vertices.
 size_t join_queue_bytes(uint32_t cap, uint32_t kmax);

@@ -128,6 +128,7 @@ struct smg_server {
   uint32_t *tasks[2] = {nullptr, nullptr};
   uint32_t *ready[2] = {nullptr, nullptr};
   unsigned int *next_count = nullptr;    // tasks preempted into the other queue
+  uint32_t *xbuf = nullptr;              // the join warps' hoisted-set buffers
   smg::QueueState *qs = nullptr;
   unsigned int *walk_count = nullptr;
   uint4 *walk_items = nullptr;
@@ -157,7 +158,7 @@ struct smg_server {
                     static_cast<void *>(d_cnt), static_cast<void *>(d_seed), static_cast<void *>(tasks[0]),
                     static_cast<void *>(tasks[1]), static_cast<void *>(ready[0]), static_cast<void *>(ready[1]),
                     static_cast<void *>(next_count), static_cast<void *>(qs), static_cast<void *>(walk_count),
-                    static_cast<void *>(walk_items)})
+                    static_cast<void *>(walk_items), static_cast<void *>(xbuf)})
       if (p) cudaFree(p);
     for (void *p : {static_cast<void *>(h_cnt), static_cast<void *>(h_qs), static_cast<void *>(h_bell),
                     static_cast<void *>(h_done)})
@@ -201,6 +202,8 @@ smg::JoinLaunch join_launch(smg_server *s) {
   jl.next_tasks = s->tasks[1 - s->cur];
   jl.next_ready = s->ready[1 - s->cur];
   jl.next_count = s->next_count;
+  jl.xbuf = s->xbuf;
+  jl.xcap = smg::kHoistGlobalCap;
   return jl;
 }
 
@@ -464,6 +467,7 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
     SMG_CUDA(cudaMalloc(&s->ready[i], static_cast<size_t>(s->cap) * 4));
   }
   SMG_CUDA(cudaMalloc(&s->next_count, sizeof(unsigned int)));
+  SMG_CUDA(cudaMalloc(&s->xbuf, smg::hoist_buffer_bytes(c->num_sms)));
   SMG_CUDA(cudaMalloc(&s->qs, sizeof(smg::QueueState)));
   SMG_CUDA(cudaMalloc(&s->walk_count, smg::kMaxWalkPhases * 2 * sizeof(unsigned int)));
   SMG_CUDA(cudaMalloc(&s->walk_items, static_cast<size_t>(smg::kWalkCap) * sizeof(uint4)));

@@ -259,8 +259,8 @@ def test_memory_bounded_chunks(ctx, monkeypatch):
     plans = [Plan(q) for q in small_queries(host, shapes=RMAT_SHAPES, ks=(4, 5), seeds=range(3))]
     whole, st1 = native.match_batch(ctx, dev, plans, use_graph=False)
     assert st1.chunks == 1
-    # the fixed queue bound (256 MB) plus room for a few queries per chunk
-    monkeypatch.setenv("SMG_MAX_BATCH_BYTES", str((256 << 20) + (256 << 10)))
+    # below a chunk's fixed part (queue bound and join buffers): one query per chunk
+    monkeypatch.setenv("SMG_MAX_BATCH_BYTES", str(256 << 20))
     parts, st2 = native.match_batch(ctx, dev, plans, use_graph=False)
     assert st2.chunks > 1
     assert parts.tolist() == whole.tolist()
