@@ -698,7 +698,7 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
   jl.time_limit_ns = time_limit_ns();
   jl.emit = ch.emb != nullptr;
   jl.xbuf = ch.xbuf;
-  jl.xcap = kHoistGlobalCap;
+  jl.xcap = hoist_global_cap();
   return jl;
 }
 

@@ -1293,9 +1293,18 @@ void set_graph(JoinLaunch &jl, const DevGraph &g) {
   jl.num_hubs = g.num_hubs;
 }
 
+uint32_t hoist_global_cap() {
+  static const uint32_t v = [] {
+    const char *e = std::getenv("SMG_HOIST_CAP");
+    const long x = e ? std::atol(e) : 4096;
+    return static_cast<uint32_t>(std::min<long>(std::max<long>(x, 256), 1 << 20));
+  }();
+  return v;
+}
+
 size_t hoist_buffer_bytes(int num_sms) {
   // at most 8 resident blocks of kWarpsPerBlock warps per SM
-  return static_cast<size_t>(std::max(num_sms, 1)) * 8 * kWarpsPerBlock * kHoistGlobalCap * sizeof(uint32_t);
+  return static_cast<size_t>(std::max(num_sms, 1)) * 8 * kWarpsPerBlock * hoist_global_cap() * sizeof(uint32_t);
 }
 
 size_t join_queue_bytes(uint32_t cap, uint32_t kmax) {

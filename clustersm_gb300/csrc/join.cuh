@@ -84,9 +84,10 @@ struct JoinLaunch {
 // The resident graph's arrays in a launch record (every launch site uses
 // this, so the hub bitmap layout and the label index always travel together).
 void set_graph(JoinLaunch &jl, const DevGraph &g);
-// Entries of a warp's hoisted-set buffer in global memory, and the bytes of
-// such buffers for every warp a join launch on num_sms SMs can have.
-constexpr uint32_t kHoistGlobalCap = 4096;
+// Entries of a warp's hoisted-set buffer in global memory (SMG_HOIST_CAP,
+// default 4,096), and the bytes of such buffers for every warp a join launch
+// on num_sms SMs can have.
+uint32_t hoist_global_cap();
 size_t hoist_buffer_bytes(int num_sms);
 // Bytes of queue storage for `cap` tasks of a batch whose largest query has
 // kmax vertices.

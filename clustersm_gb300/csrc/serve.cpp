@@ -203,7 +203,7 @@ smg::JoinLaunch join_launch(smg_server *s) {
   jl.next_ready = s->ready[1 - s->cur];
   jl.next_count = s->next_count;
   jl.xbuf = s->xbuf;
-  jl.xcap = smg::kHoistGlobalCap;
+  jl.xcap = smg::hoist_global_cap();
   return jl;
 }
 
