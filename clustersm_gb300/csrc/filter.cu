@@ -160,77 +160,76 @@ __device__ __forceinline__ void spread_slots(const ClusterStep &st, uint32_t xm,
   }
 }
 
-// Neighbour part of a step group for candidate v over adj[e0, e1): set the
-// neighbour slots of every step v passed (star / merge), or apply the
-// combine rule (AND of the other clusters' slots) to each neighbour.
+// One neighbour w of a candidate that passed steps `pass` of its group: set
+// the neighbour slots of those steps (star / merge), or apply the combine
+// rule (AND of the other clusters' slots) to w.
+__device__ __forceinline__ void walk_entry(uint32_t w, const StepGroup &G, const ClusterStep *__restrict__ steps,
+                                           const uint32_t *__restrict__ aux, const FilterQuery &Q, uint32_t kind,
+                                           uint32_t pass) {
+  const uint32_t W = Q.words;
+  uint32_t *const enc = Q.enc;
+  if (kind != 2) {
+    const uint32_t xm = Q.vmask[w];
+    if (!xm) return;
+    for (uint32_t p = pass; p; p &= p - 1) spread_slots(steps[G.first + __ffs(p) - 1], xm, enc, W, w);
+  } else {
+    const ClusterStep &st = steps[G.first];
+    uint32_t t = st.targets_off;
+    for (uint32_t ti = 0; ti < st.num_targets; ++ti) {
+      const uint32_t slot = aux[t], nsrc = aux[t + 1];
+      bool fin = true;
+      for (uint32_t s = 0; s < nsrc && fin; ++s) fin = enc_bit(enc, W, w, aux[t + 2 + s]);
+      t += 2 + nsrc;
+      if (st.type == 0) {
+        if (fin) enc_set(enc, W, w, slot >> 5, 1u << (slot & 31));
+      } else if (!fin) {
+        enc_clear(enc, W, w, slot);
+      }
+    }
+  }
+}
+
+// Neighbour part of a step group for candidate v over adj[e0, e1), one
+// entry per lane.
 __device__ __forceinline__ void walk_neighbors(const uint32_t *__restrict__ adj, const StepGroup &G,
                                                const ClusterStep *__restrict__ steps,
                                                const uint32_t *__restrict__ aux, const FilterQuery &Q,
                                                uint32_t kind, uint32_t pass, uint32_t e0, uint32_t e1,
                                                uint32_t lane, uint32_t n) {
-  const uint32_t W = Q.words;
-  uint32_t *const enc = Q.enc;
-  const uint32_t *const vmask = Q.vmask;
   for (uint32_t e = e0 + lane; e < e1; e += 32) {
     const uint32_t w = adj[e];
     if (!SMG_DCHECK(w < n, 207, w, e)) continue;
-    if (kind != 2) {
-      const uint32_t xm = vmask[w];
-      if (!xm) continue;
-      for (uint32_t p = pass; p; p &= p - 1) spread_slots(steps[G.first + __ffs(p) - 1], xm, enc, W, w);
-    } else {
-      const ClusterStep &st = steps[G.first];
-      uint32_t t = st.targets_off;
-      for (uint32_t ti = 0; ti < st.num_targets; ++ti) {
-        const uint32_t slot = aux[t], nsrc = aux[t + 1];
-        bool fin = true;
-        for (uint32_t s = 0; s < nsrc && fin; ++s) fin = enc_bit(enc, W, w, aux[t + 2 + s]);
-        t += 2 + nsrc;
-        if (st.type == 0) {
-          if (fin) enc_set(enc, W, w, slot >> 5, 1u << (slot & 31));
-        } else if (!fin) {
-          enc_clear(enc, W, w, slot);
-        }
-      }
-    }
+    walk_entry(w, G, steps, aux, Q, kind, pass);
   }
 }
 
-// Walks neighbours [e0, e1) of candidate v in `arr` (the id-ordered lists,
-// or the label-ordered ones when from_l): the first kWalkChunk entries here,
-// the rest queued for the chunk pass, one warp per chunk.
-__device__ __forceinline__ void walk_span(const uint32_t *__restrict__ arr, bool from_l, uint32_t gi, uint32_t v,
-                                          uint32_t pass, uint32_t e0, uint32_t e1, const StepGroup &G,
-                                          const ClusterStep *__restrict__ steps, const uint32_t *__restrict__ aux,
-                                          const FilterQuery &Q, uint32_t kind, uint32_t lane,
-                                          const WalkOverflow &ov) {
-  uint32_t mine = e1;
-  if (e1 - e0 > kWalkChunk) {
-    const uint32_t extra = (e1 - e0 - 1) / kWalkChunk;
-    uint32_t base = kNone;
-    if (lane == 0) {
-      unsigned int old = *(volatile unsigned int *)ov.count;
-      while (old + extra <= ov.cap) {
-        const unsigned int seen = atomicCAS(ov.count, old, old + extra);
-        if (seen == old) {
-          base = old;
-          break;
-        }
-        old = seen;
-      }
+// Queues entries [e0 + kWalkChunk, e1) of candidate v for the chunk pass,
+// one item per kWalkChunk entries; returns the end the caller keeps (e1 when
+// the queue has no room).  Called by single lanes.
+__device__ __forceinline__ uint32_t queue_tail_chunks(uint32_t tag, uint32_t v, uint32_t pass, uint32_t e0,
+                                                      uint32_t e1, const WalkOverflow &ov) {
+  if (e1 - e0 <= kWalkChunk) return e1;
+  const uint32_t extra = (e1 - e0 - 1) / kWalkChunk;
+  unsigned int old = *(volatile unsigned int *)ov.count;
+  while (old + extra <= ov.cap) {
+    const unsigned int seen = atomicCAS(ov.count, old, old + extra);
+    if (seen == old) {
+      for (uint32_t c = 0; c < extra; ++c)
+        if (SMG_DCHECK(old + c < ov.cap, 205, old + c, ov.cap))
+          ov.items[old + c] = make_uint4(tag, v, pass, e0 + (c + 1) * kWalkChunk);
+      return e0 + kWalkChunk;
     }
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base != kNone) {
-      const uint32_t tag = gi | (from_l ? 0x80000000u : 0u);
-      for (uint32_t c = lane; c < extra; c += 32)
-        if (SMG_DCHECK(base + c < ov.cap, 205, base + c, ov.cap))
-          ov.items[base + c] = make_uint4(tag, v, pass, e0 + (c + 1) * kWalkChunk);
-      mine = e0 + kWalkChunk;
-    }
+    old = seen;
   }
-  walk_neighbors(arr, G, steps, aux, Q, kind, pass, e0, mine, lane, ov.n);
+  return e1;
 }
 
+// A warp takes 32 candidates of the group's core, one per lane: each lane
+// applies the group's steps to its own candidate (core slot, merge tests,
+// combine rule), then the warp walks the neighbour runs of all 32 as one
+// segmented stream (an entry finds its candidate by a binary search over the
+// lanes' run offsets), so short runs still fill the warp.  Runs longer than
+// kWalkChunk hand their tail to the chunk pass.
 __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict__ off,
                                                       const uint32_t *__restrict__ adj,
                                                       const StepGroup *__restrict__ groups, uint32_t group_base,
@@ -247,59 +246,101 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
   uint32_t cnt = *(volatile const uint32_t *)(Q.cand_cnt + G.core);
   if (!SMG_DCHECK(Q.cand_off[G.core] + cnt <= Q.cand_off[G.core + 1], 202, cnt, G.core)) cnt = 0;
   const uint32_t kind = steps[G.first].kind;
-  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  const bool by_label = G.nlab && ov.adjl;
+  const uint32_t nruns = by_label ? G.nlab : 1;
+  const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
   unsigned long long scanned = 0;
-  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < cnt; i += warps) {
-    const uint32_t v = list[i];
-    if (v == kNone) continue;  // removed by an earlier merge
-    if (!SMG_DCHECK(v < ov.n, 203, v, i)) continue;
-    uint32_t pass = 0;         // steps of the group that v passed
-    if (kind == 0) {
-      const ClusterStep &st = steps[G.first];
-      if (lane == 0) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
-      pass = 1;
-    } else if (kind == 1) {
-      bool alive = true;
-      for (uint32_t j = 0; j < G.count && alive; ++j) {
-        const ClusterStep &st = steps[G.first + j];
-        if (enc_bit(enc, W, v, st.left_pos) && enc_bit(enc, W, v, st.right_pos)) {
-          pass |= 1u << j;
-          if (lane == 0) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+  for (uint64_t i0 = (static_cast<uint64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; i0 < cnt;
+       i0 += warps * 32) {
+    const uint64_t i = i0 + lane;
+    uint32_t v = 0, pass = 0;
+    bool act = false;
+    if (i < cnt) {
+      v = list[i];
+      if (v != kNone && SMG_DCHECK(v < ov.n, 203, v, i)) {
+        if (kind == 0) {
+          const ClusterStep &st = steps[G.first];
+          enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+          pass = 1;
+          act = true;
+        } else if (kind == 1) {
+          bool alive = true;
+          for (uint32_t j = 0; j < G.count && alive; ++j) {
+            const ClusterStep &st = steps[G.first + j];
+            if (enc_bit(enc, W, v, st.left_pos) && enc_bit(enc, W, v, st.right_pos)) {
+              pass |= 1u << j;
+              enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+            } else {
+              alive = false;
+            }
+          }
+          if (!alive) list[i] = kNone;  // removed by this merge group
+          act = pass != 0;
         } else {
-          alive = false;
-        }
-      }
-      if (!alive && lane == 0) list[i] = kNone;
-    } else {
-      const ClusterStep &st = steps[G.first];
-      bool all = true;
-      for (uint32_t o = 0; o < st.num_others && all; ++o) all = enc_bit(enc, W, v, aux[st.others_off + o]);
-      if (lane == 0) {
-        if (st.type == 0) {
-          if (all) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
-        } else if (!all) {
-          enc_clear(enc, W, v, st.core_slot);
+          const ClusterStep &st = steps[G.first];
+          bool all = true;
+          for (uint32_t o = 0; o < st.num_others && all; ++o) all = enc_bit(enc, W, v, aux[st.others_off + o]);
+          if (st.type == 0) {
+            if (all) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+          } else if (!all) {
+            enc_clear(enc, W, v, st.core_slot);
+          }
+          act = true;
         }
       }
     }
-    if (kind != 2 && pass == 0) continue;
-    const uint32_t e0 = off[v], e1 = off[v + 1];
-    if (!SMG_DCHECK(e0 <= e1 && e1 <= ov.m2, 204, e0, e1)) continue;
-    const uint32_t li = (G.nlab && ov.adjl) ? __ldg(ov.lab_of + v) : kNone;
-    if (li != kNone) {
-      // only neighbours with the group's labels can change: walk their runs
-      const uint32_t *t = ov.lab_off + static_cast<uint64_t>(li) * (ov.lab_buckets + 1);
-      for (uint32_t i = 0; i < G.nlab; ++i) {
-        const uint32_t b = min(static_cast<uint32_t>(G.lab[i]), ov.lab_buckets - 1);
-        const uint32_t r0 = e0 + __ldg(t + b), r1 = e0 + __ldg(t + b + 1);
-        scanned += r1 - r0;
-        walk_span(ov.adjl, true, gi, v, pass, r0, r1, G, steps, aux, Q, kind, lane, ov);
+    uint32_t e0 = 0, e1 = 0, li = kNone;
+    if (act) {
+      e0 = off[v];
+      e1 = off[v + 1];
+      if (!SMG_DCHECK(e0 <= e1 && e1 <= ov.m2, 204, e0, e1)) act = false;
+      else if (by_label) li = __ldg(ov.lab_of + v);
+    }
+    for (uint32_t r = 0; r < nruns; ++r) {
+      // this lane's segment: the run of the group's r-th label when its
+      // candidate has a run table (only those neighbours can change), else
+      // (r = 0 only) its whole list
+      uint32_t s0 = 0, s1 = 0;
+      bool from_l = false;
+      if (act) {
+        if (li != kNone) {
+          const uint32_t *t = ov.lab_off + static_cast<uint64_t>(li) * (ov.lab_buckets + 1) +
+                              min(static_cast<uint32_t>(G.lab[r]), ov.lab_buckets - 1);
+          s0 = e0 + __ldg(t);
+          s1 = e0 + __ldg(t + 1);
+          from_l = true;
+        } else if (r == 0) {
+          s0 = e0;
+          s1 = e1;
+        }
       }
-    } else {
-      scanned += e1 - e0;
-      walk_span(adj, false, gi, v, pass, e0, e1, G, steps, aux, Q, kind, lane, ov);
+      scanned += s1 - s0;
+      if (s1 - s0 > kWalkChunk) s1 = queue_tail_chunks(gi | (from_l ? 0x80000000u : 0u), v, pass, s0, s1, ov);
+      const uint32_t len = s1 - s0;
+      uint32_t incl = len;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += x;
+      }
+      const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31), pre = incl - len;
+      const uint32_t fl = from_l ? 1u : 0u;
+      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        uint32_t src = 0;  // the last lane whose segment starts at or before t
+        for (uint32_t step = 16; step; step >>= 1) {
+          const uint32_t c = src + step;
+          if (__shfl_sync(0xFFFFFFFFu, pre, c) <= t) src = c;
+        }
+        const uint32_t sb = __shfl_sync(0xFFFFFFFFu, s0, src), sp = __shfl_sync(0xFFFFFFFFu, pre, src);
+        const uint32_t spass = __shfl_sync(0xFFFFFFFFu, pass, src), sfl = __shfl_sync(0xFFFFFFFFu, fl, src);
+        if (t < total) {
+          const uint32_t w = (sfl ? ov.adjl : adj)[sb + (t - sp)];
+          if (SMG_DCHECK(w < ov.n, 207, w, sb)) walk_entry(w, G, steps, aux, Q, kind, spass);
+        }
+      }
     }
   }
+  for (int o = 16; o; o >>= 1) scanned += __shfl_down_sync(0xFFFFFFFFu, scanned, o);
   if (lane == 0 && scanned) atomicAdd(Q.stat + 1, scanned);
 }
 
