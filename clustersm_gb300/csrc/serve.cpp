@@ -31,6 +31,7 @@
 #include <map>
 #include <memory>
 #include <thread>
+#include <unordered_set>
 
 #include "api_internal.cuh"
 
@@ -117,7 +118,8 @@ struct smg_server {
   std::deque<Request> waiting;
   std::vector<Slot> slots;
   uint32_t free_slots = 0;
-  std::map<uint64_t, smg_request_result> done;
+  std::map<uint64_t, smg_request_result> done;  // finished, not yet collected by smg_server_poll
+  std::unordered_set<uint64_t> outstanding;     // submitted, not yet finished
   Pool pool;
   // device allocations
   char *pool_mem = nullptr;
@@ -228,6 +230,7 @@ void retire(smg_server *s, Slot &sl, smg_status status, uint64_t count) {
   r.start_s = sl.start_s;
   r.finish_s = now_s();
   s->done[sl.ticket] = r;
+  s->outstanding.erase(sl.ticket);
   s->pool.release(sl.off, sl.size);
   sl = Slot();
   ++s->free_slots;
@@ -499,6 +502,7 @@ smg_status smg_server_submit(smg_server *s, const smg_plan *p, uint64_t *ticket)
     if (p->p.label[u] >= smg::kMaxLabels) return fail(SMG_ERR_LIMIT, "query labels must be below 256");
   *ticket = s->next_ticket++;
   s->waiting.push_back({*ticket, &p->p, now_s(), bytes});
+  s->outstanding.insert(*ticket);
   return SMG_OK;
 }
 
@@ -511,10 +515,11 @@ smg_status smg_server_poll(smg_server *s, uint64_t ticket, smg_request_result *o
   if (!s || !out) return fail(SMG_ERR_INVALID, "null argument");
   auto it = s->done.find(ticket);
   if (it == s->done.end()) {
-    if (ticket == 0 || ticket >= s->next_ticket) return fail(SMG_ERR_INVALID, "unknown ticket");
-    return SMG_ERR_NOT_READY;
+    if (s->outstanding.count(ticket)) return SMG_ERR_NOT_READY;
+    return fail(SMG_ERR_INVALID, "unknown ticket, or its result was already collected");
   }
   *out = it->second;
+  s->done.erase(it);  // a result is handed out once, so a long-running server keeps no history
   return SMG_OK;
 }
 
@@ -527,6 +532,7 @@ smg_status smg_server_cancel(smg_server *s, uint64_t ticket) {
       res.submit_s = it->submit_s;
       res.finish_s = now_s();
       s->done[ticket] = res;
+      s->outstanding.erase(ticket);
       s->waiting.erase(it);
       return SMG_OK;
     }

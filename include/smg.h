@@ -350,7 +350,9 @@ typedef struct smg_request_result {
 smg_status smg_server_create(smg_ctx *ctx, const smg_graph *g,
                              const smg_server_config *cfg, smg_server **out);
 smg_status smg_server_submit(smg_server *s, const smg_plan *p, uint64_t *ticket);
-/* SMG_ERR_NOT_READY while the request is queued or running. */
+/* SMG_ERR_NOT_READY while the request is queued or running.  A finished
+ * request's result is returned once: the server then forgets it, and a later
+ * poll of the same ticket fails with SMG_ERR_INVALID. */
 smg_status smg_server_poll(smg_server *s, uint64_t ticket, smg_request_result *out);
 smg_status smg_server_cancel(smg_server *s, uint64_t ticket);
 /* Drive the server until every submitted request has finished. */

@@ -116,4 +116,7 @@ def test_query_size_limit(ctx, er):
     assert e.value.status == 5  # SMG_ERR_LIMIT
     srv.drain()
     assert [int(srv.poll(t).count) for t in tickets] == [int(w) for w in want[:12]]
+    with pytest.raises(native.SmgError) as e:  # a result is collected once
+        srv.poll(tickets[0])
+    assert e.value.status == 1  # SMG_ERR_INVALID
     srv.close()
