@@ -147,7 +147,7 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
     for rate in rates:
         rng = random.Random(f"serve-{rate}")
         n = max(64, min(max_requests, int(rate * seconds)))
-        srv = Server(ctx, dev, max_inflight=512, memory_budget_bytes=64 << 30,
+        srv = Server(ctx, dev, max_inflight=1024, memory_budget_bytes=96 << 30,
                      max_query_vertices=max(p.view.k for p in plans))
         tickets = []
         t_next = time.perf_counter()

@@ -319,12 +319,12 @@ constexpr uint32_t kHoistCap = 256;
 constexpr uint32_t kHoistInvalid = 0xFFFFFFFFu;  // xlen: not built for this prefix
 constexpr uint32_t kHoistTooBig = 0xFFFFFFFEu;   // xlen: larger than kHoistCap
 __host__ __device__ inline uint32_t warp_words(uint32_t K) {
-  return scalar_words(K) + 2 * K + 32 * K + 7 * 32 + kHoistCap + 2;
+  return scalar_words(K) + 2 * K + 32 * K + 7 * 32 + kHoistCap + 2 + 32 * K;
 }
 
 struct WarpView {
   uint32_t *m, *beg, *deg, *hub, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *lbk, *batch;
-  uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv, *xs, *xlen;
+  uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv, *xs, *xlen, *bpos;
   uint32_t xcap = kHoistCap;  // entries xs holds (xs may be moved to a global buffer)
   const uint32_t **lbase;
   __device__ WarpView(uint32_t *W, uint32_t K) {
@@ -353,6 +353,7 @@ struct WarpView {
     spiv = spre + 32;
     xs = spiv + 32;
     xlen = xs + kHoistCap;
+    bpos = xlen + 2;  // [K][32] list position of each batch entry
   }
 };
 
@@ -853,10 +854,15 @@ __device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned l
                         uint32_t level, uint32_t P, uint32_t lane) {
   int ok = 0;
   if (lane == 0) {
+    // per level at most two tasks: the untried part of its batch, as the list
+    // range from the first untried entry to just past the last one still in
+    // the batch (entries in between that failed their tests fail again;
+    // entries a donation took from the batch's end lie beyond it), and the
+    // unscanned rest of the list
     uint32_t n = 0;
     for (uint32_t l = L0; l <= level; ++l) {
       if (S.cur[l] < S.end[l]) ++n;
-      if (l < P) n += S.bcnt[l] - S.bidx[l];
+      if (l < P && S.bidx[l] < S.bcnt[l]) ++n;
     }
     if (n == 0) {
       ok = 1;
@@ -885,17 +891,15 @@ __device__ bool preempt(WarpView &S, const JoinLaunch &p, uint32_t q, unsigned l
             for (uint32_t j = 0; j < l; ++j) T[4 + j] = S.m[j];
             p.next_ready[idx++] = 1;
           }
-          if (l < P)
-            for (uint32_t b = S.bidx[l]; b < S.bcnt[l]; ++b) {
-              uint32_t *T = p.next_tasks + static_cast<uint64_t>(idx) * tw;
-              T[0] = q;
-              T[1] = l + 1;
-              T[2] = 0;
-              T[3] = kNone;
-              for (uint32_t j = 0; j < l; ++j) T[4 + j] = S.m[j];
-              T[4 + l] = S.batch[l * 32 + b];
-              p.next_ready[idx++] = 1;
-            }
+          if (l < P && S.bidx[l] < S.bcnt[l]) {
+            uint32_t *T = p.next_tasks + static_cast<uint64_t>(idx) * tw;
+            T[0] = q;
+            T[1] = l;
+            T[2] = S.bpos[l * 32 + S.bidx[l]];
+            T[3] = S.bpos[l * 32 + S.bcnt[l] - 1] + 1;
+            for (uint32_t j = 0; j < l; ++j) T[4 + j] = S.m[j];
+            p.next_ready[idx++] = 1;
+          }
         }
         atomicAdd(qpending, static_cast<unsigned long long>(n));
         ok = 1;
@@ -1145,7 +1149,10 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
           good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, cv, Q.use_labels, level, w, probes));
         }
         const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
-        if (good) S.batch[level * 32 + __popc(bal & lt)] = w;
+        if (good) {
+          S.batch[level * 32 + __popc(bal & lt)] = w;
+          S.bpos[level * 32 + __popc(bal & lt)] = c + lane;
+        }
         __syncwarp();
         if (lane == 0) {
           S.bcnt[level] = __popc(bal);
