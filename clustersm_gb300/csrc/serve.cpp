@@ -136,6 +136,7 @@ struct smg_server {
   uint4 *walk_items = nullptr;
   uint32_t cap = 0, cur = 0;
   uint32_t kmax = smg::kMaxK;  // task width: the largest query accepted
+  uint32_t admit_batch = 1;    // free slots that ring the doorbell (SMG_ADMIT_BATCH; default an eighth)
   uint64_t slice_ns = 0, slice_min_ns = 0;
   cudaEvent_t ev = nullptr;
   bool inflight = false, bell_rung = false;
@@ -248,12 +249,13 @@ void poll_done(smg_server *s) {
 }
 
 // While a slice runs: ring the doorbell once requests wait and enough slots
-// are free to admit them in a batch (an eighth of the slots), or any slot is
+// are free to admit them in a batch (SMG_ADMIT_BATCH, default an eighth of
+// the slots), or any slot is
 // free and the slice has run 10 ms, so that the slice closes and the next one
 // admits them.  (The device closes a slice no earlier than SMG_SLICE_MIN_MS.)
 void maybe_ring(smg_server *s) {
   if (s->bell_rung || s->waiting.empty() || s->free_slots == 0) return;
-  const uint32_t want = std::max<uint32_t>(1, static_cast<uint32_t>(s->slots.size()) / 8);
+  const uint32_t want = s->admit_batch;
   if (s->free_slots >= want || now_s() - s->slice_start_s > 0.010) {
     __atomic_store_n(s->h_bell, 1u, __ATOMIC_RELEASE);
     s->bell_rung = true;
@@ -457,6 +459,7 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   s->slice_ns = static_cast<uint64_t>(env_ms("SMG_SLICE_MS", 250.0) * 1e6);
   s->slice_min_ns = std::min(s->slice_ns, static_cast<uint64_t>(env_ms("SMG_SLICE_MIN_MS", 2.0) * 1e6));
   s->cap = 2u << 20;
+  s->admit_batch = std::max<uint32_t>(1, static_cast<uint32_t>(env_ms("SMG_ADMIT_BATCH", s->cfg.max_inflight / 8.0)));
   const size_t tw = task_words(s.get());
   const uint32_t m = s->cfg.max_inflight;
   SMG_CUDA(cudaMalloc(&s->pool_mem, s->cfg.memory_budget_bytes));
