@@ -2,12 +2,37 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "smg.h"
 
 namespace smg {
+
+// Allocator whose resize() leaves new elements uninitialised, so that large
+// host arrays are first touched by the parallel loops that fill them instead
+// of by one thread writing zeros.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+  template <class U>
+  void construct(U *p) noexcept {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <class U, class... A>
+  void construct(U *p, A &&...a) {
+    ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+  }
+};
+using RawU32 = std::vector<uint32_t, NoInitAlloc<uint32_t>>;
 
 // Records `msg` as the calling thread's last error detail and returns `s`.
 smg_status fail(smg_status s, const std::string &msg);
@@ -18,7 +43,7 @@ struct HostGraph {
   uint32_t n = 0;
   uint64_t m = 0;  // undirected edges
   std::vector<uint64_t> off;
-  std::vector<uint32_t> adj;
+  RawU32 adj;
   std::vector<uint32_t> label;
   smg_csr view() const {
     smg_csr c;
@@ -89,10 +114,15 @@ smg_status build_plan(const smg_query_desc &q, Plan &out);
 
 // .in parsing (io.cu:24-108 dialect)
 smg_status read_in_file(const char *path, uint32_t &n, std::vector<uint32_t> &label,
-                        std::vector<uint32_t> &deg, std::vector<uint32_t> &edges);
+                        std::vector<uint32_t> &deg, RawU32 &edges);
 
-smg_status csr_from_edges(uint32_t n, const std::vector<uint32_t> &edges, bool sort_lists,
-                          HostGraph &g);
+// Degree of every vertex in a flat (a, b) edge-pair list, counted in parallel.
+std::vector<uint32_t> count_degrees(uint32_t n, const RawU32 &edges);
+
+// CSR from an edge-pair list; each list keeps file order unless sort_lists.
+// `degrees`, when given, must be the counts count_degrees would return.
+smg_status csr_from_edges(uint32_t n, const RawU32 &edges, bool sort_lists,
+                          HostGraph &g, const std::vector<uint32_t> *degrees = nullptr);
 
 }  // namespace smg
 
