@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--subset", type=int, default=0, help="use only the first N queries (profiling runs)")
+    ap.add_argument("--shape", default="", choices=["", "tree", "sparse", "dense"],
+                    help="use only the queries of one shape class (profiling runs)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
@@ -228,6 +230,9 @@ def main():
     from clustersm_gb300.workloads import load, shard
     wl = load(args.workload)
     queries_all, expected, meta = wl.queries()
+    if args.shape:
+        keep = [i for i, q in enumerate(meta["queries"]) if q.get("shape") == args.shape]
+        queries_all, expected = [queries_all[i] for i in keep], [expected[i] for i in keep]
     if args.subset:
         queries_all, expected = queries_all[: args.subset], expected[: args.subset]
     mine = shard(len(queries_all), rank, world)
@@ -270,6 +275,7 @@ def main():
         native.match_batch(ctx, dev, plans, profile=True)
 
     step_ms, join_ms, filt_ms, jbytes, fbytes, launches = [], 0.0, 0.0, 0, 0, 0
+    work = {"scanned": 0, "descents": 0, "probes": 0, "last_count_entries": 0, "donations": 0, "tasks": 0}
     h2d = d2h = 0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -286,6 +292,8 @@ def main():
             jbytes += st.join_bytes
             fbytes += st.filter_bytes
             launches += st.kernel_launches
+            for key in work:
+                work[key] += getattr(st, key)
             h2d, d2h = st.h2d_bytes, st.d2h_bytes
     clocks = clk.summary()
     total_ms = sum(step_ms)
@@ -342,13 +350,15 @@ def main():
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": wl.name, "description": wl.description, "queries": nq_all,
                        "graph_vertices": host.n, "graph_edges": host.m, "l2": "flushed (256 MB write) between steps",
-                       "parallelism": f"replicas{world}" if world > 1 else "single"},
+                       "parallelism": f"replicas{world}" if world > 1 else "single",
+                       **({"shape": args.shape} if args.shape else {})},
             "embeddings_per_s": embeddings * world * args.steps / (total_ms / 1e3),
             "embeddings_per_step": embeddings,
             "counts_checked": len(want), "count_mismatches": mismatches,
             "plain_queries_per_s": plain_qps, "batched_over_plain": value / plain_qps if plain_qps else None,
             "plain_sample": None if args.no_plain else min(args.plain_sample, len(plans)),
             "filter_ms_per_step": filt_ms / args.steps, "join_ms_per_step": join_ms / args.steps,
+            "join_work_per_step": {key: val // args.steps for key, val in work.items()},
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": "k_join", "achieved": achieved, "peak": peak, "unit": "GB/s",
