@@ -369,6 +369,13 @@ def main():
                          "traffic_gbs": traffic / (join_ms / args.steps / 1e3) / 1e9 if traffic and join_ms else None,
                          "traffic_frac": traffic / (join_ms / args.steps / 1e3) / 1e9 / peak if traffic and join_ms
                          else None},
+            # the filter kernels of the same passes (k_nlc_filter, k_cluster_walk, k_walk_chunks,
+            # k_collect): their algorithmic bytes over their event-timed duration
+            "roofline_filter": {"bound": "hbm", "kernels": "k_nlc_filter+k_cluster_walk+k_walk_chunks+k_collect",
+                                "achieved": fbytes / (filt_ms / 1e3) / 1e9 if filt_ms > 0 else 0.0,
+                                "peak": peak, "unit": "GB/s",
+                                "frac": (fbytes / (filt_ms / 1e3) / 1e9 / peak) if filt_ms > 0 else 0.0,
+                                "algorithmic_bytes_per_step": fbytes / args.steps},
             "clocks": clocks,
             "tuning": tuning,
             "serving": serve,

@@ -1460,19 +1460,23 @@ smg_status build_label_index(DevGraph &g, const uint64_t *offsets, const uint32_
     for (uint32_t j = 0; j < B; ++j) t[j + 1] += t[j];  // t[j] = start of bucket j, t[B] = degree
   }
   // rank of each vertex within its bucket, and where each bucket's words
-  // start in a hub bitmap row
-  std::vector<uint32_t> rank(n), bwo(B + 1, 0);
-  {
+  // start in a hub bitmap row: only the label layout of the hub bitmaps
+  // (SMG_HUB_LAYOUT=label) reads them
+  std::vector<uint32_t> rank, bwo;
+  const char *layout = std::getenv("SMG_HUB_LAYOUT");
+  if (layout && std::string(layout) == "label") {
+    rank.resize(n);
+    bwo.assign(B + 1, 0);
     std::vector<uint32_t> cnt(B, 0);
     for (uint32_t v = 0; v < n; ++v) rank[v] = cnt[std::min(labels[v], B - 1)]++;
     for (uint32_t b = 0; b < B; ++b) bwo[b + 1] = bwo[b] + (cnt[b] + 31) / 32;
+    g.hub_row_words = bwo[B];
+    SMG_CUDA(cudaMalloc(&g.lab_rank, static_cast<size_t>(n) * 4));
+    SMG_CUDA(cudaMalloc(&g.bucket_word_off, (B + 1) * 4));
+    SMG_CUDA(cudaMemcpyAsync(g.lab_rank, rank.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, s));
+    SMG_CUDA(cudaMemcpyAsync(g.bucket_word_off, bwo.data(), (B + 1) * 4, cudaMemcpyHostToDevice, s));
+    g.bytes += static_cast<size_t>(n) * 4 + (B + 1) * 4;
   }
-  g.hub_row_words = bwo[B];
-  SMG_CUDA(cudaMalloc(&g.lab_rank, static_cast<size_t>(n) * 4));
-  SMG_CUDA(cudaMalloc(&g.bucket_word_off, (B + 1) * 4));
-  SMG_CUDA(cudaMemcpyAsync(g.lab_rank, rank.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, s));
-  SMG_CUDA(cudaMemcpyAsync(g.bucket_word_off, bwo.data(), (B + 1) * 4, cudaMemcpyHostToDevice, s));
-  g.bytes += static_cast<size_t>(n) * 4 + (B + 1) * 4;
   SMG_CUDA(cudaMalloc(&g.adjl, g.m2 * 4));
   SMG_CUDA(cudaMalloc(&g.lab_of, static_cast<size_t>(n) * 4));
   SMG_CUDA(cudaMalloc(&g.lab_off, lab_off.size() * 4));
