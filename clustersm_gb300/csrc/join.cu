@@ -595,6 +595,15 @@ __device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery 
   __syncwarp();
 }
 
+// Which way |X & N(v)| is counted for a stored hoisted set X (xn entries,
+// sorted) and a level-P candidate v whose run has rv entries: true scans v's
+// run, testing each entry by a binary search of X; false walks X, probing
+// N(v) for each member (a hub bitmap word or a binary search of v's list).
+// The run is scanned while it is at most hoist_scan_x8 / 8 times as long as X.
+__device__ __forceinline__ bool hoist_scan_run(const JoinLaunch &p, uint32_t rv, uint32_t xn) {
+  return 8ull * rv <= static_cast<uint64_t>(p.hoist_scan_x8) * xn;
+}
+
 // Counts (and optionally emits) the last level for every candidate of the
 // batch of level P = k-2: the candidates' last-level lists are concatenated
 // and walked 32 entries at a time, each lane finding its candidate by binary
@@ -642,8 +651,9 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
         // |X & N(v)|: walk v's run keeping members of X, or walk X probing
         // N(v), whichever is shorter
         const uint32_t rv = run_len(p, S, Q.use_labels, L, v, vd);
+        const uint32_t hv = __ldg(p.hub_of + v);
         uint32_t mode = kHoistSet, base = 0;
-        if (rv <= xn) {
+        if (hoist_scan_run(p, rv, xn)) {
           const uint32_t *lst = scan_list(p, S, Q.use_labels, L, v, vb, vd, len);
           const bool from_l = lst != p.adj + vb;
           base = static_cast<uint32_t>(lst - (from_l ? p.adjl : p.adj));
@@ -654,7 +664,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
         S.sv[lane] = v;
         S.sbeg[lane] = vb;
         S.sdeg[lane] = vd;
-        S.shub[lane] = __ldg(p.hub_of + v);
+        S.shub[lane] = hv;
         S.sbase[lane] = base;
         S.spiv[lane] = P | mode;
         counted = true;
@@ -1360,10 +1370,23 @@ bool hoist_enabled() {
   return v;
 }
 
+// How much longer than a hoisted set X a candidate's run may be and still be
+// scanned against X rather than X walked against the candidate's list, in
+// eighths (SMG_HOIST_SCAN_RATIO; default 8: the shorter side is walked).
+uint32_t hoist_scan_x8() {
+  static const uint32_t v = [] {
+    const char *e = std::getenv("SMG_HOIST_SCAN_RATIO");
+    const long c = e ? std::strtol(e, nullptr, 10) : 8;
+    return static_cast<uint32_t>(std::min(std::max(c, 1L), 1024L));
+  }();
+  return v;
+}
+
 smg_status launch_persistent(const JoinLaunch &jl_in, cudaStream_t s, int num_sms) {
   JoinLaunch jl = jl_in;
   jl.probe_runs = probe_runs() && jl.adjl != nullptr;
   jl.hoist = hoist_enabled();
+  jl.hoist_scan_x8 = hoist_scan_x8();
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
   const JoinKernel kern = join_kernel(smem);
   if (smem > 48 * 1024)

@@ -47,6 +47,10 @@ struct JoinLaunch {
   const uint32_t *lab_rank, *bucket_word_off;  // hub bitmap layout by label (null: by id)
   uint32_t probe_runs;       // membership probes search label runs (SMG_PROBE=runs)
   uint32_t hoist;            // hoisted last-level sets (count-only runs; SMG_HOIST=0: off)
+  // how |X & N(v)| is counted for a stored hoisted set X: v's run is
+  // scanned when 8 x its length <= hoist_scan_x8 x |X|, else X is walked
+  // (SMG_HOIST_SCAN_RATIO, in eighths; 8 walks the shorter side)
+  uint32_t hoist_scan_x8;
   // per resident warp, room for a stored hoisted set of xcap entries (global
   // memory, [blocks x warps per block][xcap]); null: the warp's shared
   // memory, 256 entries
