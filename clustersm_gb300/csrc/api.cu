@@ -791,7 +791,8 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
     for (uint32_t u = 0; u < plans[ch.a + i]->k; ++u) q.initial_cands += hc[i].cand_cnt[u];
     q.emb_written = ch.emb ? std::min<uint64_t>(hc[i].emb_count, o.emb_cap) : 0;
     q.overflow = ch.emb ? (hc[i].emb_count > o.emb_cap) : 0;
-    // algorithmic bytes of the filter (model in the design doc)
+    // algorithmic bytes of the filter: each array touched once, 4 B per id or
+    // word (the per-kernel units are itemised below)
     const Plan &P = *plans[ch.a + i];
     uint64_t lab = 0;
     std::vector<char> seen(kMaxLabels, 0);

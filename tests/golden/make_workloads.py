@@ -1,7 +1,8 @@
 """Generate the committed query sets of the benchmark workloads, with exact
 embedding counts checked by two independent implementations.
 
-    # on a GPU host: draw and screen queries (writes gpurun_out/workload_<name>.json)
+    # on a GPU host: draw and screen queries (writes $WORKLOAD_DIR/workload_<name>.json,
+    # default screened/ at the repository root)
     python tests/golden/make_workloads.py gpu rmat22 rmat20
     # on any host: recount every kept query with the CPU oracle and commit
     python tests/golden/make_workloads.py verify rmat22 rmat20
@@ -35,6 +36,8 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parents[2]
+# where screening writes its draws and verification reads them
+SCREEN_DIR = Path(os.environ.get("WORKLOAD_DIR", str(ROOT / "screened")))
 sys.path.insert(0, str(ROOT))
 
 from clustersm_gb300.workloads import load  # noqa: E402
@@ -116,8 +119,8 @@ def gen_gpu(name, seconds=None, resume=None, per_round=16):
         for s in range(nq):
             nxt[s] = int(old.get("next_attempt", {}).get(str(s), first if old.get("complete") else 0))
         tried = old.get("draws_total", 0)
-    path = ROOT / "gpurun_out" / f"workload_{name}.json"
-    path.parent.mkdir(exist_ok=True)
+    path = SCREEN_DIR / f"workload_{name}.json"
+    path.parent.mkdir(parents=True, exist_ok=True)
 
     def save(complete):
         out = [kept[s] for s in sorted(kept)]
@@ -186,7 +189,7 @@ def gen_gpu(name, seconds=None, resume=None, per_round=16):
 def verify(name, src=None):
     import oracle
     wl = load(name)
-    src = Path(src) if src else ROOT / "gpurun_out" / f"workload_{name}.json"
+    src = Path(src) if src else SCREEN_DIR / f"workload_{name}.json"
     data = json.loads(src.read_text())
     host = wl.graph()
     t0 = time.time()
