@@ -118,3 +118,18 @@ def test_record_split_across_lines_reads_as_one(tmp_path):
     g = HostGraph.read(p)
     assert g.offsets().tolist() == [0, 1, 3, 4]
     assert g.neighbors().tolist() == [1, 0, 2, 1]
+
+
+def test_split_records_and_no_final_newline_in_large_file(big):
+    # every 'e' record spans two lines, so pieces may only start at lines
+    # that begin with a letter; the file also ends without a newline
+    n, a, b, lab, d = big
+    deg = np.bincount(np.concatenate([a, b]), minlength=n)
+    vs = [f"v {i} {lab[i]}\n{deg[i]}" for i in range(n)]
+    es = [f"e {x}\n{y}" for x, y in zip(a.tolist(), b.tolist())]
+    p = d / "split_big.in"
+    p.write_text("\n".join([f"t {n} {len(a)}", *vs, *es]))
+    g = HostGraph.read(p)
+    off, adj = _file_order_csr(n, a, b)
+    assert np.array_equal(g.offsets(), off) and np.array_equal(g.neighbors(), adj)
+    assert np.array_equal(g.labels(), lab)
