@@ -11,6 +11,7 @@
 // reference would write out of bounds or build a multigraph on them.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -133,7 +134,12 @@ bool is_letter(char c) { return (c >= 'a' && c <= 'z') || (c >= 'A' && c <= 'Z')
 std::vector<Piece> split_body(const char *b, const char *e, size_t want) {
   std::vector<Piece> pieces;
   const size_t len = static_cast<size_t>(e - b);
-  const size_t min_piece = 1 << 20;
+  // smallest piece worth a thread (SMG_IO_PIECE_BYTES, default 1 MiB)
+  size_t min_piece = 1 << 20;
+  if (const char *env = std::getenv("SMG_IO_PIECE_BYTES")) {
+    const long long v = std::atoll(env);
+    if (v > 0) min_piece = static_cast<size_t>(v);
+  }
   size_t np = std::max<size_t>(1, std::min(want, len / min_piece));
   const char *at = b;
   for (size_t i = 1; i <= np; ++i) {
