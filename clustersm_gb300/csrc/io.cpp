@@ -281,7 +281,11 @@ smg_status csr_from_edges(uint32_t n, const RawU32 &edges, bool sort_lists,
   const int T = num_threads();
   const size_t R = static_cast<size_t>(std::max(1, std::min(T * 2, 250)));
   const size_t P = static_cast<size_t>(std::max(1, T * 2));
-  if (m2 < (1u << 20) || R == 1) {
+  // lists shorter in total than SMG_IO_SCATTER_MIN entries (default 2^20)
+  // are filled by one thread
+  uint64_t scatter_min = 1u << 20;
+  if (const char *env = std::getenv("SMG_IO_SCATTER_MIN")) scatter_min = std::strtoull(env, nullptr, 10);
+  if (m2 < scatter_min || R == 1) {
     std::vector<uint64_t> cur(g.off.begin(), g.off.end() - 1);
     for (uint64_t i = 0; i < pairs; ++i) {
       uint32_t a = edges[2 * i], b = edges[2 * i + 1];

@@ -1,4 +1,5 @@
-"""Piecewise parsing of .in files gives the same result as one pass.
+"""Piecewise parsing of .in files, and the parallel CSR fill, give the same
+result as one pass.
 
 SMG_IO_PIECE_BYTES shrinks the loader's pieces to a few bytes, so small
 random files, with any whitespace between tokens, records split across
@@ -17,21 +18,27 @@ given, settings = hyp.given, hyp.settings
 
 
 def _read(path, piece):
-    old = os.environ.get("SMG_IO_PIECE_BYTES")
+    """Read with pieces of `piece` bytes and the parallel CSR fill forced on
+    (piece 0: one piece, one-thread fill)."""
+    keys = ("SMG_IO_PIECE_BYTES", "SMG_IO_SCATTER_MIN")
+    old = {k: os.environ.get(k) for k in keys}
     if piece:
         os.environ["SMG_IO_PIECE_BYTES"] = str(piece)
+        os.environ["SMG_IO_SCATTER_MIN"] = "0"
     else:
-        os.environ.pop("SMG_IO_PIECE_BYTES", None)
+        for k in keys:
+            os.environ.pop(k, None)
     try:
         g = HostGraph.read(path)
         return 0, (g.offsets().tolist(), g.neighbors().tolist(), g.labels().tolist())
     except SmgError as e:
         return e.status, None
     finally:
-        if old is None:
-            os.environ.pop("SMG_IO_PIECE_BYTES", None)
-        else:
-            os.environ["SMG_IO_PIECE_BYTES"] = old
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
 @st.composite
