@@ -1,0 +1,34 @@
+"""Host-side parts of bench.py that run without a GPU: the argument defaults
+the timing rules depend on, and the CPU-baseline leg's record."""
+import sys
+
+import pytest
+
+import bench
+from clustersm_gb300.native import HostGraph, Query
+
+
+def test_defaults_meet_timing_rules(monkeypatch):
+    monkeypatch.setattr(sys, "argv", ["bench.py"])
+    a = bench.parse()
+    assert a.gpus == 1 and a.warmup >= 3 and a.steps >= 1
+    assert a.workload == "rmat22" and a.impl == "gb300" and a.shape == ""
+
+
+def test_shape_choices(monkeypatch):
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--shape", "dense", "--subset", "8"])
+    a = bench.parse()
+    assert a.shape == "dense" and a.subset == 8
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--shape", "cyclic"])
+    with pytest.raises(SystemExit):
+        bench.parse()
+
+
+def test_cpu_baseline_record():
+    g = HostGraph.er(300, 1200, 3, seed=2)
+    qs = [Query.generate(g, 4, "sparse", seed=s) for s in range(6)]
+    r = bench.cpu_baseline(g, qs, 0.5)
+    assert r["kind"] == "port" and r["unit"] == "queries/s" and r["value"] > 0 and r["cores"] >= 1
+    assert r["embeddings_per_s"] > 0
+    one = r["single_core"]
+    assert one["value"] > 0 and one["embeddings_per_s"] > 0 and "1 thread" in one["sample"]
