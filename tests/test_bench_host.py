@@ -32,3 +32,20 @@ def test_cpu_baseline_record():
     assert r["embeddings_per_s"] > 0
     one = r["single_core"]
     assert one["value"] > 0 and one["embeddings_per_s"] > 0 and "1 thread" in one["sample"]
+
+
+def test_reference_arm_line():
+    # the reference arm runs only on host cores: its JSON line is checked here
+    import json
+    import subprocess
+    from pathlib import Path
+    root = Path(bench.__file__).resolve().parent
+    out = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--workload", "er1k",
+                          "--steps", "1", "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["steps"] == 1
+    assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["workload"] == "er1k"
