@@ -20,9 +20,14 @@ the device-resident data graph.  Prints one JSON line (rank 0).
              server (smg_server_*) under seeded Poisson arrivals of the same
              queries at 100, 1,000 and 5,000 queries/s offered
 
+  reference_binary  the reference's own filter and join (compiled from its
+             sources for sm_103a, oracle/_ref/ref_match) against the plain
+             path on the same 2^20-vertex R-MAT queries (those the reference
+             can run in bounds, tests/golden/ref_screen_rmat20.json): per-query
+             hot-path wall time, graph resident, counts compared
+
 --impl reference times the reference's algorithm on the host cores instead:
-the reference has no CPU implementation of its path and its GPU binary cannot
-be rebuilt on the GPU host (its sources are not there), so the arm runs the
+the reference has no CPU implementation of its path, so the arm runs the
 oracle port, the CPU restatement of the same semantics.
 
 For N > 1 (torchrun) the queries are dealt round-robin to ranks: each rank
@@ -62,6 +67,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-rates", default="100,1000,5000")
+    ap.add_argument("--no-reference-binary", action="store_true",
+                    help="skip the leg that runs the reference's own GPU filter and join")
     ap.add_argument("--tune", action="store_true",
                     help="run the library's per-shape-class autotuner on the workload before timing (untimed)")
     return ap.parse_args()
@@ -186,6 +193,69 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
                     "sustained_qps": n / (last - first), "counts_ok": ok, "slices": ss.slices, "bells": ss.bells,
                     "retired_in_slice": ss.retired_in_slice, "slice_s": ss.slice_s, "between_s": ss.between_s})
     return out
+
+
+def reference_binary_leg(ctx, repeats=3):
+    """The reference's filter and join (oracle/_ref/ref_match) and the plain
+    path (smg_match, one call per query) on the screened queries of the
+    2^20-vertex workload.  Per query, the reference's time is the wall time of
+    its per-query work (candidate buffers, clusterFilter, edge order, join,
+    with their allocations, memsets and copies); the plain path's is the wall
+    time of one smg_match call, best of `repeats`.  Both with the data graph
+    already on the device."""
+    import os as _os
+    from clustersm_gb300 import native
+    from clustersm_gb300.native import DeviceGraph, Plan
+    from clustersm_gb300.workloads import load
+    harness = ROOT / "oracle" / "_ref" / "ref_match"
+    if not _os.access(harness, _os.X_OK):
+        return {"unavailable": "oracle/_ref/ref_match not built (the reference's sources were not available)"}
+    screen = json.loads((ROOT / "tests" / "golden" / "ref_screen_rmat20.json").read_text())
+    rows = [r for r in screen["screen"] if r["run"]]
+    wl = load("rmat20")
+    host = wl.graph()
+    qs, counts, _ = wl.queries()
+    with tempfile.TemporaryDirectory() as td:
+        gpath = Path(td) / "g.in"
+        host.write(gpath)
+        qpaths = []
+        for r in rows:
+            qpaths.append(str(Path(td) / f"q{r['index']}.in"))
+            qs[r["index"]].write(qpaths[-1])
+        p = subprocess.run([str(harness), str(ctx.device), str(gpath), *qpaths], capture_output=True, text=True,
+                           timeout=1800)
+    if p.returncode != 0:
+        return {"unavailable": f"ref_match exited {p.returncode}: {p.stderr[-300:]}"}
+    out = [json.loads(line) for line in p.stdout.splitlines() if line.startswith("{")]
+    load_s = out[0].get("load_s")
+    res = [o for o in out if "query" in o]
+    dev = DeviceGraph(ctx, host)
+    plans = [Plan(qs[r["index"]]) for r in rows]
+    for pl in plans:  # warm-up
+        native.match(ctx, dev, pl)
+    plain_ms, lib_counts = [], []
+    for pl in plans:
+        best = None
+        for _ in range(repeats):
+            t = time.perf_counter()
+            r, _ = native.match(ctx, dev, pl)
+            dt = (time.perf_counter() - t) * 1e3
+            best = dt if best is None else min(best, dt)
+        plain_ms.append(best)
+        lib_counts.append(int(r.count))
+    dev.free()
+    ref_ms = [o["ms"] for o in res]
+    ref_counts = [int(o["num_res"]) for o in res]
+    want = [counts[r["index"]] for r in rows]
+    return {"workload": "rmat20", "queries": len(rows), "screened_from": screen["queries"],
+            "reference_queries_per_s": len(rows) / (sum(ref_ms) / 1e3),
+            "plain_queries_per_s": len(rows) / (sum(plain_ms) / 1e3),
+            "plain_over_reference": sum(ref_ms) / sum(plain_ms),
+            "reference_ms_median": statistics.median(ref_ms), "plain_ms_median": statistics.median(plain_ms),
+            "reference_filter_ms_median": statistics.median([o["filter_ms"] for o in res]),
+            "reference_load_s": load_s,
+            "counts_equal": ref_counts == want == lib_counts,
+            "count_mismatches": sum(1 for a, b, c in zip(ref_counts, want, lib_counts) if not a == b == c)}
 
 
 def run_reference(args, wl, host, queries, rank):
@@ -328,6 +398,10 @@ def main():
             native.match(ctx, dev, p)
         plain_qps = ns / (time.perf_counter() - t)
 
+    ref_bin = None
+    if not args.no_reference_binary and world == 1:
+        ref_bin = reference_binary_leg(ctx)
+
     serve = None
     if not args.no_serve and world == 1:
         serve = serving(ctx, dev, plans, want, [float(r) for r in args.serve_rates.split(",") if r])
@@ -378,6 +452,7 @@ def main():
                                 "algorithmic_bytes_per_step": fbytes / args.steps},
             "clocks": clocks,
             "tuning": tuning,
+            "reference_binary": ref_bin,
             "serving": serve,
         }
         if not args.no_cpu_baseline:

@@ -358,6 +358,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()
+        self.device = device
         check(lib.smg_open(device, C.byref(self._h)), "smg_open")
 
     @property

@@ -32,7 +32,9 @@ def _load():
     lib.oracle_encode.argtypes = [C.POINTER(Csr), C.POINTER(PlanView), u32p, u32p, u32p]
     lib.oracle_count_budget.argtypes = [C.POINTER(Csr), C.POINTER(QueryDesc), u32p, C.c_int, C.c_uint64, u64p,
                                         u64p]
-    for f in ("oracle_count_budget", "oracle_count", "oracle_embeddings", "oracle_count_roots", "oracle_nlc_filter", "oracle_encode"):
+    lib.oracle_ref_rows.argtypes = [C.POINTER(Csr), C.c_uint32, C.c_uint32, u32p, u32p, u32p, C.c_int, C.c_uint64,
+                                    u64p]
+    for f in ("oracle_ref_rows", "oracle_count_budget", "oracle_count", "oracle_embeddings", "oracle_count_roots", "oracle_nlc_filter", "oracle_encode"):
         getattr(lib, f).restype = C.c_int
     return lib
 
@@ -104,3 +106,20 @@ def encode(graph, plan, vmask0):
                           enc.ctypes.data_as(u32p), cm.ctypes.data_as(u32p)):
         raise ValueError("oracle_encode failed")
     return enc, cm
+
+
+def ref_rows(graph, plan, candmask, limit: int = (1 << 64) - 2, threads: int = 0):
+    """Rows of the reference's breadth-first join tables after each step of
+    its edge order (the plan's edge_order_first/second): a list of
+    num_edges + 1 ints, None from the first level holding more than `limit`."""
+    v = plan.view
+    E = v.num_edges
+    first = np.ctypeslib.as_array(v.edge_order_first, shape=(E,)).astype(np.uint32)
+    second = np.ctypeslib.as_array(v.edge_order_second, shape=(E,)).astype(np.uint32)
+    candmask = np.ascontiguousarray(candmask, dtype=np.uint32)
+    rows = np.zeros(E + 1, dtype=np.uint64)
+    rc = _lib.oracle_ref_rows(C.byref(graph.csr), v.k, E, first.ctypes.data_as(u32p), second.ctypes.data_as(u32p),
+                              candmask.ctypes.data_as(u32p), threads, limit, rows.ctypes.data_as(u64p))
+    if rc:
+        raise ValueError("oracle_ref_rows rejected the input")
+    return [None if int(r) == (1 << 64) - 1 else int(r) for r in rows.tolist()]

@@ -254,6 +254,124 @@ int oracle_embeddings(const smg_csr *g, const smg_query_desc *q, uint64_t max_ro
   return 0;
 }
 
+// Rows of the reference's breadth-first join tables, level by level
+// (join.cu:290-435): rows[0] = |C(first vertex of the edge order)|
+// (firstJoinKernel join.cu:71-97), then after each edge (a -> b) of the
+// order: b unmapped, every row r and neighbour w of r[a] with bit b of
+// candmask[w] set and w not yet in r gives a row (joinOneEdgeKernel
+// join.cu:100-177); b mapped, r is kept when r[b] is a neighbour of r[a]
+// (selectPartialMatchingsKernel join.cu:16-68).  Depth-first over the same
+// rows.  Gives up once a level holds more than `limit` rows: that level and
+// the later ones then read UINT64_MAX.
+int oracle_ref_rows(const smg_csr *g, uint32_t k, uint32_t num_edges, const uint32_t *first,
+                    const uint32_t *second, const uint32_t *candmask, int threads, uint64_t limit,
+                    uint64_t *rows) {
+  if (!g || !first || !second || !candmask || !rows || k < 2 || k > 32 || num_edges < 1) return 1;
+  const uint32_t E = num_edges, root = first[0];
+  // an edge extends the rows when its second vertex is new at that point
+  std::vector<char> extends(E, 0);
+  {
+    uint32_t mapped = 1u << root;
+    for (uint32_t e = 0; e < E; ++e) {
+      if (first[e] >= k || second[e] >= k || !(mapped >> first[e] & 1)) return 1;
+      extends[e] = !(mapped >> second[e] & 1);
+      mapped |= 1u << second[e];
+    }
+  }
+  std::vector<uint32_t> roots;
+  for (uint32_t v = 0; v < g->num_vertices; ++v)
+    if (candmask[v] >> root & 1) roots.push_back(v);
+  std::vector<uint64_t> total(E + 1, 0);
+  total[0] = roots.size();
+  bool over = total[0] > limit;
+  int nt = threads;
+#ifdef _OPENMP
+  if (nt <= 0) nt = omp_get_max_threads();
+#else
+  nt = 1;
+#endif
+#pragma omp parallel num_threads(nt)
+  {
+    std::vector<uint64_t> local(E + 1, 0);
+    uint64_t pending = 0;
+    uint32_t m[32];
+    auto flush = [&]() {
+      for (uint32_t j = 1; j <= E; ++j) {
+        if (!local[j]) continue;
+        if (__atomic_add_fetch(&total[j], local[j], __ATOMIC_RELAXED) > limit)
+          __atomic_store_n(&over, true, __ATOMIC_RELAXED);
+        local[j] = 0;
+      }
+      pending = 0;
+    };
+    // per level j < E: next neighbour position and end of the anchor's list
+    // (extending edge), or whether the single adjacency test is still to do
+    std::vector<uint64_t> pos(E), end(E);
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t r = 0; r < static_cast<int64_t>(roots.size()); ++r) {
+      if (__atomic_load_n(&over, __ATOMIC_RELAXED)) continue;
+      for (uint32_t u = 0; u < k; ++u) m[u] = UINT32_MAX;
+      m[root] = roots[r];
+      int64_t j = 0;  // rows at depth j have edges [0, j) applied
+      bool enter = true;
+      while (j >= 0) {
+        if (j == static_cast<int64_t>(E)) {  // a full row: back up
+          --j;
+          enter = false;
+          continue;
+        }
+        const uint32_t a = first[j], b = second[j];
+        if (enter) {
+          if (extends[j]) {
+            pos[j] = g->offsets[m[a]];
+            end[j] = g->offsets[m[a] + 1];
+          } else {
+            pos[j] = 0;
+            end[j] = 1;
+          }
+        }
+        bool down = false;
+        if (extends[j]) {
+          while (pos[j] < end[j]) {
+            const uint32_t w = g->neighbors[pos[j]++];
+            if (!(candmask[w] >> b & 1)) continue;
+            bool used = false;
+            for (uint32_t u = 0; u < k && !used; ++u) used = u != b && m[u] == w;
+            if (used) continue;
+            m[b] = w;
+            down = true;
+            break;
+          }
+          if (!down) m[b] = UINT32_MAX;
+        } else if (pos[j] < end[j]) {
+          pos[j] = end[j];
+          down = has_edge(g, m[a], m[b]);
+        }
+        if (++pending >= 4096) {
+          flush();
+          if (__atomic_load_n(&over, __ATOMIC_RELAXED)) break;
+        }
+        if (down) {
+          ++local[j + 1];
+          ++j;
+          enter = true;
+        } else {
+          --j;
+          enter = false;
+        }
+      }
+      flush();
+    }
+  }
+  for (uint32_t j = 0; j <= E; ++j) rows[j] = total[j];
+  if (over) {
+    uint32_t j = 0;
+    while (j <= E && total[j] <= limit) ++j;
+    for (; j <= E; ++j) rows[j] = UINT64_MAX;
+  }
+  return 0;
+}
+
 // filter.cu:404-539 restated: one pass over the data vertices.
 int oracle_nlc_filter(const smg_csr *g, const smg_plan_view *p, uint32_t *vmask0) {
   if (!g || !p || !vmask0) return 1;

@@ -59,6 +59,15 @@ int oracle_nlc_filter(const smg_csr *g, const smg_plan_view *p, uint32_t *vmask0
 int oracle_encode(const smg_csr *g, const smg_plan_view *p, const uint32_t *vmask0,
                   uint32_t *enc, uint32_t *candmask);
 
+/* Rows of the reference's breadth-first join tables after each step of its
+ * edge order (join.cu:290-435): rows[0] = candidates of first[0], rows[e+1] =
+ * rows after edge (first[e] -> second[e]).  candmask: final candidates
+ * (bit u of candmask[v]).  Gives up once a level holds more than `limit`
+ * rows; that level and the later ones then read UINT64_MAX.  rows: [num_edges + 1]. */
+int oracle_ref_rows(const smg_csr *g, uint32_t k, uint32_t num_edges, const uint32_t *first,
+                    const uint32_t *second, const uint32_t *candmask, int threads, uint64_t limit,
+                    uint64_t *rows);
+
 #ifdef __cplusplus
 }
 #endif
