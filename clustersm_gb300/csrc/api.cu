@@ -479,7 +479,7 @@ QueryFootprint query_footprint(const DevGraph &g, const Plan &P) {
 }
 
 smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffers &b, uint64_t count_limit,
-                              FilterQuery &f, JoinQuery &j) {
+                              FilterQuery &f, JoinQuery &j, uint64_t work_limit) {
   smg_status st = fill_filter_query(P, g, f);
   if (st) return st;
   uint64_t acc = 0;
@@ -529,6 +529,8 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
   j.emb_count = &b.counters->emb_count;
   j.count_limit = count_limit;
   j.over = &b.counters->over;
+  j.work_limit = work_limit;
+  j.work = &b.counters->work;
   j.pending = &b.counters->pending;
   return SMG_OK;
 }
@@ -658,7 +660,7 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     b.counters = ch.counters + i;
     b.emb = ch.emb;
     b.emb_cap = ch.emb ? o.emb_cap : 0;
-    smg_status st = make_query_records(P, g, b, o.count_limit, hf[i], hj[i]);
+    smg_status st = make_query_records(P, g, b, o.count_limit, hf[i], hj[i], o.work_limit);
     if (st) return st;
     if (o.tuning && !o.root_chunk) {
       const TuneSetting &t = o.tuning[plan_class(P)];
@@ -883,6 +885,7 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
       key.push_back(&g);
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.root_chunk)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.count_limit)));
+      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.work_limit)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.profile)));
       for (uint32_t i = 0; i < nq; ++i) key.push_back(plans[i]);
     }
@@ -908,6 +911,7 @@ smg_status smg_match(smg_ctx *c, const smg_graph *G, const smg_plan *p, const sm
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
     o.count_limit = opts->max_count;
+    o.work_limit = opts->max_work;
     if (opts->flags & SMG_FLAG_EMIT) {
       if (!opts->embeddings && opts->max_embeddings) return fail(SMG_ERR_INVALID, "null embeddings buffer");
       o.emb_host = opts->embeddings;
@@ -950,6 +954,7 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
     o.count_limit = opts->max_count;
+    o.work_limit = opts->max_work;
     o.use_graph = (opts->flags & SMG_FLAG_NO_GRAPH) == 0;
   }
   std::vector<QueryOut> q(n);

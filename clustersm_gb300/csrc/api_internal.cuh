@@ -39,7 +39,8 @@ struct QCounters {
   unsigned long long count;    // embeddings
   unsigned long long emb_count;
   unsigned long long pending;  // tasks of this query not yet finished
-  unsigned long long pad2[7];
+  unsigned long long work;     // join steps taken (counted only under a work limit)
+  unsigned long long pad2[6];
 };
 static_assert(sizeof(QCounters) % 16 == 0, "QCounters must keep 16-byte alignment");
 
@@ -61,6 +62,7 @@ struct RunOpts {
   uint64_t emb_cap = 0;
   bool use_graph = false;        // capture the launches in a CUDA graph
   uint64_t count_limit = 0;      // 0: none
+  uint64_t work_limit = 0;       // 0: none
 };
 
 struct QueryOut {
@@ -120,7 +122,7 @@ struct QueryFootprint {
 QueryFootprint query_footprint(const DevGraph &g, const Plan &P);
 // Fills the filter and join records of one query whose state lives in `b`.
 smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffers &b, uint64_t count_limit,
-                              FilterQuery &f, JoinQuery &j);
+                              FilterQuery &f, JoinQuery &j, uint64_t work_limit = 0);
 constexpr uint32_t kMaxWalkPhases = 2 * 100;  // 2 * MAX_LAYERS - 1 phases at most
 constexpr uint32_t kWalkCap = 1u << 20;        // chunk-pass items per filter launch
 

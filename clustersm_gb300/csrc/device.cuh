@@ -180,7 +180,9 @@ struct JoinQuery {
   unsigned long long emb_cap;
   unsigned long long *emb_count;
   unsigned long long count_limit;  // 0: none; else stop once the count exceeds it
-  uint32_t *over;             // set to 1 when the count exceeded count_limit
+  uint32_t *over;             // set to 1 when the count exceeded count_limit (or the work work_limit)
+  unsigned long long work_limit;   // 0: none; else stop once the join has taken more steps
+  unsigned long long *work;   // join steps taken (under a work limit)
   unsigned long long *pending;  // tasks of this query queued or running
   uint32_t root_chunk;        // root candidates per seeded task (0: from max_seed_tasks)
   uint32_t donate_min;        // shortest list worth splitting off (0: launch default)

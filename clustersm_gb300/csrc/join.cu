@@ -974,7 +974,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     const uint32_t k = Q.k, P = k - 2;
     if (!SMG_DCHECK(L0 <= P + 1, 110, L0, k)) break;
     int drop = 0;
-    if (lane == 0) drop = Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over);
+    if (lane == 0) drop = (Q.count_limit || Q.work_limit) && *reinterpret_cast<volatile uint32_t *>(Q.over);
     drop = __shfl_sync(0xFFFFFFFFu, drop, 0);
     if (drop) {  // the query is over its count limit
       if (lane == 0) {
@@ -1045,7 +1045,8 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
               if (before + cnt > Q.count_limit) *Q.over = 1;
             }
           }
-          if (Q.count_limit && *reinterpret_cast<volatile uint32_t *>(Q.over)) {
+          if (Q.work_limit && atomicAdd(Q.work, 256ull) + 256ull > Q.work_limit) *Q.over = 1;
+          if ((Q.count_limit || Q.work_limit) && *reinterpret_cast<volatile uint32_t *>(Q.over)) {
             stop = 2;  // this query is over its limit: drop the task, keep running
           } else if (*vabort) {
             stop = 1;

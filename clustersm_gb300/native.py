@@ -63,7 +63,7 @@ class PlanView(C.Structure):
 class MatchOpts(C.Structure):
     _fields_ = [("flags", C.c_uint32), ("bfs_depth", C.c_uint32), ("root_chunk", C.c_uint32),
                 ("reserved", C.c_uint32), ("max_embeddings", C.c_uint64), ("embeddings", u32p),
-                ("max_count", C.c_uint64)]
+                ("max_count", C.c_uint64), ("max_work", C.c_uint64)]
 
 
 class MatchResult(C.Structure):
@@ -407,10 +407,11 @@ class DeviceGraph:
 
 
 def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=False, bfs_depth=0,
-          root_chunk=0, max_count=0):
+          root_chunk=0, max_count=0, max_work=0):
     """Plain path.  Returns (MatchResult, embeddings array or None)."""
     opts = MatchOpts()
     opts.max_count = max_count
+    opts.max_work = max_work
     opts.flags = (FLAG_EMIT if emit else 0) | (FLAG_PROFILE if profile else 0)
     opts.bfs_depth = bfs_depth
     opts.root_chunk = root_chunk
@@ -427,9 +428,9 @@ def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=F
 
 
 def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk=0, profile=False, max_count=0,
-                use_graph=True):
-    """Batched path.  Returns (counts, BatchStats); with max_count, queries over
-    the limit report 2**64-1."""
+                use_graph=True, max_work=0):
+    """Batched path.  Returns (counts, BatchStats); with max_count or
+    max_work, queries over a limit report 2**64-1."""
     n = len(plans)
     arr = (C.c_void_p * n)(*[p.handle.value for p in plans])
     counts = np.zeros(n, dtype=np.uint64)
@@ -438,6 +439,7 @@ def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk
     opts.bfs_depth = bfs_depth
     opts.root_chunk = root_chunk
     opts.max_count = max_count
+    opts.max_work = max_work
     st = BatchStats()
     check(lib.smg_match_batch(ctx.handle, graph.handle, arr, n, C.byref(opts), counts.ctypes.data_as(u64p),
                               C.byref(st)), "smg_match_batch")

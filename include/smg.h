@@ -230,6 +230,13 @@ typedef struct smg_match_opts {
   uint64_t max_count;      /* 0 = none; otherwise a query stops as soon as
                               its count is known to exceed max_count, and
                               reports UINT64_MAX (batch) / limit_hit = 1   */
+  uint64_t max_work;       /* 0 = none; otherwise a query stops once its
+                              join warps have taken more than max_work
+                              steps (one step: one pass of a warp's task
+                              loop, a batch of list entries or one
+                              descent), reported like max_count: a bound
+                              on the work of queries whose count may be
+                              out of reach                                 */
 } smg_match_opts;
 
 typedef struct smg_match_result {

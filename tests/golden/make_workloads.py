@@ -8,6 +8,9 @@ embedding counts checked by two independent implementations.
     python tests/golden/make_workloads.py verify rmat22 rmat20
     # small workloads drawn and counted by the oracle alone
     python tests/golden/make_workloads.py cpu er1k
+    # on a GPU host: per-(k, shape) feasibility of walk queries on a
+    # workload's graph (writes tests/golden/feasibility_<name>.json)
+    python tests/golden/make_workloads.py feasibility rmat22 rmat20
 
 Queries are drawn by seeded random-walk extraction (smg_gen_query).  On R-MAT
 graphs with Zipf labels, walk-extracted queries have embedding counts far
@@ -235,6 +238,67 @@ def gen_cpu(name):
     print(f"{name}: kept {len(out)} -> {dst}")
 
 
+FEAS_KS = list(range(4, 17))
+FEAS_SHAPES = ["tree", "sparse", "dense"]
+FEAS_DRAWS = 64
+FEAS_LIMITS = [10**7, 10**8, 10**10]
+FEAS_WORK = 1 << 30  # join steps per query (about 0.1 s of the whole GPU)
+
+
+def feasibility(name):
+    """For every query size k = 4..16 and shape, draw FEAS_DRAWS walk queries
+    (seeds apart from the workload's own) and count them in one batched call
+    per cell with the count limit 10^10 and the work limit FEAS_WORK join
+    steps per query.  A draw is decided when its exact count comes back; the
+    cell records how many decided draws have at most 10^7, 10^8 and 10^10
+    embeddings.  A cell whose batch hits the device deadline (SMG_TIME_LIMIT_S,
+    set to 120 s here) is recorded as such."""
+    from clustersm_gb300 import native
+    from clustersm_gb300.native import Context, DeviceGraph, Plan
+    os.environ.setdefault("SMG_TIME_LIMIT_S", "120")
+    wl = load(name)
+    host = wl.graph()
+    ctx = Context(0)
+    dev = DeviceGraph(ctx, host)
+    cells = []
+    t_all = time.time()
+    for k in FEAS_KS:
+        for si, shape in enumerate(FEAS_SHAPES):
+            t0 = time.time()
+
+            def draw(a):
+                try:
+                    return Query.generate(host, k, shape, seed=(1 << 40) | (k << 24) | (si << 20) | a)
+                except SmgError:
+                    return None
+
+            with cf.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+                qs = [q for q in ex.map(draw, range(FEAS_DRAWS)) if q is not None]
+            cell = {"k": k, "shape": shape, "draws": FEAS_DRAWS, "generated": len(qs), "timeout": False}
+            counts = []
+            if qs:
+                try:
+                    got, _ = native.match_batch(ctx, dev, [Plan(q) for q in qs], max_count=FEAS_LIMITS[-1],
+                                                max_work=FEAS_WORK)
+                    counts = [None if c == 2**64 - 1 else int(c) for c in got.tolist()]
+                except SmgError as e:
+                    cell["timeout"] = True
+                    cell["error"] = str(e)[:200]
+            decided = sorted(c for c in counts if c is not None)
+            for lim in FEAS_LIMITS:
+                cell[f"le_{lim:.0e}".replace("+", "")] = sum(1 for c in decided if c <= lim)
+            cell["undecided"] = len(counts) - len(decided)
+            cell["median_decided"] = decided[len(decided) // 2] if decided else None
+            cell["seconds"] = round(time.time() - t0, 2)
+            cells.append(cell)
+            print(json.dumps(cell), flush=True)
+    dst = ROOT / "tests" / "golden" / f"feasibility_{name}.json"
+    dst.write_text(json.dumps({"workload": name, "graph": wl.description.split(",")[0], "draws_per_cell": FEAS_DRAWS,
+                               "count_limit": FEAS_LIMITS[-1], "work_limit_steps": FEAS_WORK,
+                               "seconds": round(time.time() - t_all, 1), "cells": cells}, indent=0))
+    print(f"{name}: feasibility table -> {dst}")
+
+
 if __name__ == "__main__":
     mode, names = sys.argv[1], sys.argv[2:]
     budget = float(os.environ.get("WORKLOAD_SECONDS", "0")) or None
@@ -242,5 +306,7 @@ if __name__ == "__main__":
     for n in names:
         if mode == "gpu":
             gen_gpu(n, budget, resume)
+        elif mode == "feasibility":
+            feasibility(n)
         else:
             {"verify": verify, "cpu": gen_cpu}[mode](n)

@@ -12,9 +12,16 @@ reasons with their file:line).
           queries after one read of the data graph) on all of them
   rmat20  ref_match over every screened query of the 2^20-vertex graph
 
-Each count must equal the committed oracle count and the library's count
-(smg_match through the C ABI).  The tests skip when the reference's sources
-are not available to build it.
+The library's count (smg_match through the C ABI) must equal the committed
+oracle count on every query.  The reference's count must equal it too, with
+one known exception: encodeKernel and mergeKernel set a candidate's core bit
+with a plain read-modify-write (filter.cu:633, 713) while other warps
+atomicOr bits into the same word, so a bit can be lost.  A lost bit removes
+a candidate, never adds one, so a reference count may fall short of the
+oracle's and never exceed it, and the shortfall changes from run to run.  The
+tests assert that bound on every run, exact equality on at least 95% of them,
+and write the divergences to gpurun_out/ (when present) for the record.  They
+skip when the reference's sources are not available to build it.
 """
 import json
 import os
@@ -46,6 +53,26 @@ def screened(name):
     return [r for r in data["screen"] if r["run"]]
 
 
+def judge(runs, name):
+    """runs: (how, query index, reference, oracle, library).  Returns the
+    failures; records the reference's shortfalls."""
+    lib_bad = [r for r in runs if r[4] != r[3]]
+    over = [r for r in runs if r[2] > r[3]]
+    short = [r for r in runs if r[2] < r[3]]
+    out = ROOT / "gpurun_out"
+    if out.is_dir():
+        (out / f"reference_divergence_{name}.json").write_text(json.dumps(
+            {"runs": len(runs), "short": [list(r) for r in short]}))
+    fails = []
+    if lib_bad:
+        fails.append(f"library != oracle on {lib_bad[:10]}")
+    if over:
+        fails.append(f"reference above the oracle on {over[:10]}")
+    if len(short) > 0.05 * len(runs):
+        fails.append(f"reference short of the oracle on {len(short)} of {len(runs)} runs: {short[:10]}")
+    return fails
+
+
 def run_harness(harness, gpath, qpaths):
     p = subprocess.run([str(harness), "0", str(gpath), *map(str, qpaths)], capture_output=True, text=True,
                        timeout=1800)
@@ -71,18 +98,17 @@ def test_reference_binary_er1k(tmp_path, ctx):
         qpaths.append(tmp_path / f"q{r['index']}.in")
         qs[r["index"]].write(qpaths[-1])
     lib = {r["index"]: native.match(ctx, dev, Plan(qs[r["index"]]))[0].count for r in rows}
-    bad = []
+    runs = []
     for r, qpath in list(zip(rows, qpaths))[::4]:
         p = subprocess.run([str(binary), "-q", str(qpath), "-d", str(gpath), "--gpu", "0"], capture_output=True,
                            text=True, timeout=300)
         assert p.returncode == 0, (r["index"], p.stderr[-2000:])
         ref = int(p.stdout.strip().splitlines()[-1].split()[1])
-        if not (ref == counts[r["index"]] == lib[r["index"]]):
-            bad.append(("binary", r["index"], ref, counts[r["index"]], lib[r["index"]]))
+        runs.append(("binary", r["index"], ref, counts[r["index"]], lib[r["index"]]))
     for r, o in zip(rows, run_harness(harness, gpath, qpaths)):
-        if not (o["num_res"] == counts[r["index"]] == lib[r["index"]]):
-            bad.append(("ref_match", r["index"], o["num_res"], counts[r["index"]], lib[r["index"]]))
-    assert not bad, f"reference / oracle / library disagree on {len(bad)} runs: {bad[:10]}"
+        runs.append(("ref_match", r["index"], o["num_res"], counts[r["index"]], lib[r["index"]]))
+    fails = judge(runs, "er1k")
+    assert not fails, "; ".join(fails)
 
 
 def test_reference_filter_join_rmat20(tmp_path, ctx):
@@ -101,10 +127,9 @@ def test_reference_filter_join_rmat20(tmp_path, ctx):
         qfiles.append(str(qpath))
     res = run_harness(harness, gpath, qfiles)
     dev = DeviceGraph(ctx, host)
-    bad = []
+    runs = []
     for r, o in zip(rows, res):
         i = r["index"]
-        lib = native.match(ctx, dev, Plan(qs[i]))[0].count
-        if not (o["num_res"] == counts[i] == lib):
-            bad.append((i, o["num_res"], counts[i], lib))
-    assert not bad, f"reference / oracle / library disagree on {len(bad)} queries: {bad[:10]}"
+        runs.append(("ref_match", i, o["num_res"], counts[i], native.match(ctx, dev, Plan(qs[i]))[0].count))
+    fails = judge(runs, "rmat20")
+    assert not fails, "; ".join(fails)
