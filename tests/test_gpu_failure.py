@@ -62,3 +62,16 @@ def test_server_time_limit(ctx, heavy, monkeypatch):
     assert [r.status for r in res] == [0] * len(plans)
     assert [int(r.count) for r in res] == want
     srv.close()
+
+
+def test_work_limit(ctx, heavy):
+    """A per-query work limit (smg_match_opts.max_work) stops a heavy query
+    without failing the call: the plain path reports limit_hit, the batch
+    UINT64_MAX for that query, and the other queries of the batch stay exact."""
+    dev, plans, want = heavy
+    r, _ = native.match(ctx, dev, plans[0], max_work=1024)
+    assert r.limit_hit == 1
+    counts, _ = native.match_batch(ctx, dev, plans[:2], max_work=1024)
+    assert [int(c) for c in counts] == [2**64 - 1] * 2
+    counts, _ = native.match_batch(ctx, dev, plans[:2], max_work=1 << 40)
+    assert [int(c) for c in counts] == want[:2]
