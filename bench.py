@@ -128,9 +128,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(host, queries, seconds):
-    """The oracle (backtracking, all cores) on the first queries until `seconds` pass."""
+def cpu_baseline(host, queries, seconds, meta_queries=()):
+    """The oracle (backtracking, all cores) on a shape- and size-stratified
+    sample of the queries until `seconds` pass."""
     import oracle
+    if meta_queries:
+        queries = [queries[i] for i in stratified(list(meta_queries), len(queries))]
     t0 = time.perf_counter()
     done, emb = 0, 0
     for q in queries:
@@ -149,7 +152,8 @@ def cpu_baseline(host, queries, seconds):
             break
     dt1 = time.perf_counter() - t1
     return {"value": done / dt, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"first {done} of {len(queries)} queries of the workload, oracle_count with "
+            "sample": f"{done} of {len(queries)} queries of the workload (one per (shape, k) stratum in turn), "
+                      f"oracle_count with "
                       f"{os.cpu_count()} OpenMP threads, {dt:.1f} s", "embeddings_per_s": emb / dt,
             "single_core": {"value": done1 / dt1, "unit": "queries/s", "embeddings_per_s": emb1 / dt1,
                             "sample": f"first {done1} of those queries on 1 thread, {dt1:.1f} s"}}
@@ -258,19 +262,35 @@ def reference_binary_leg(ctx, repeats=3):
             "count_mismatches": sum(1 for a, b, c in zip(ref_counts, want, lib_counts) if not a == b == c)}
 
 
-def run_reference(args, wl, host, queries, rank):
+def stratified(meta_queries, n_all):
+    """Query indices in an order that takes one query of every (shape, k)
+    stratum in turn, each stratum in workload order, so that any prefix of
+    it is a shape- and size-stratified sample."""
+    strata = {}
+    for i in range(n_all):
+        q = meta_queries[i] if i < len(meta_queries) else {}
+        strata.setdefault((q.get("shape", ""), q.get("k", 0)), []).append(i)
+    order, lists = [], [strata[k] for k in sorted(strata)]
+    for r in range(max((len(x) for x in lists), default=0)):
+        order += [x[r] for x in lists if r < len(x)]
+    return order
+
+
+def run_reference(args, wl, host, queries, rank, meta_queries):
     if rank != 0:
         return
     import oracle
-    # calibrate a bounded per-step sample (about 5 s of CPU work)
+    order = stratified(meta_queries, len(queries))
+    # calibrate a bounded per-step sample (about 5 s of CPU work), taken in
+    # stratified order
     t0 = time.perf_counter()
     sample = 0
-    for q in queries:
-        oracle.count(host, q)
+    for i in order:
+        oracle.count(host, queries[i])
         sample += 1
         if time.perf_counter() - t0 > 5.0:
             break
-    sub = queries[:sample]
+    sub = [queries[i] for i in order[:sample]]
     for _ in range(args.warmup):
         for q in sub[: max(1, sample // 4)]:
             oracle.count(host, q)
@@ -282,6 +302,7 @@ def run_reference(args, wl, host, queries, rank):
         times.append(time.perf_counter() - t)
     tot = sum(times)
     value = args.steps * sample / tot
+    strata = sorted({(meta_queries[i].get("shape"), meta_queries[i].get("k")) for i in order[:sample]})
     line = {"metric": "queries/s (batched subgraph matching, exact uint64 counts)", "value": value,
             "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -289,7 +310,8 @@ def run_reference(args, wl, host, queries, rank):
             "config": {"workload": wl.name, "description": wl.description, "queries_per_step": sample},
             "embeddings_per_s": embs / tot,
             "cpu_baseline": {"value": value, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"first {sample} queries of the workload per step"},
+                             "sample": f"{sample} queries per step, one per (shape, k) stratum in turn "
+                                       f"({len(strata)} strata)"},
             "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -303,13 +325,15 @@ def main():
     if args.shape:
         keep = [i for i, q in enumerate(meta["queries"]) if q.get("shape") == args.shape]
         queries_all, expected = [queries_all[i] for i in keep], [expected[i] for i in keep]
+        meta["queries"] = [meta["queries"][i] for i in keep]
     if args.subset:
         queries_all, expected = queries_all[: args.subset], expected[: args.subset]
+        meta["queries"] = meta["queries"][: args.subset]
     mine = shard(len(queries_all), rank, world)
     queries = [queries_all[i] for i in mine]
     host = wl.graph()
     if args.impl == "reference":
-        return run_reference(args, wl, host, queries_all, rank)
+        return run_reference(args, wl, host, queries_all, rank, meta["queries"])
 
     import torch
     from clustersm_gb300 import native
@@ -456,7 +480,7 @@ def main():
             "serving": serve,
         }
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(host, queries_all, args.cpu_seconds)
+            line["cpu_baseline"] = cpu_baseline(host, queries_all, args.cpu_seconds, meta["queries"])
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
