@@ -20,6 +20,10 @@ the device-resident data graph.  Prints one JSON line (rank 0).
              server (smg_server_*) under seeded Poisson arrivals of the same
              queries at 100, 1,000 and 5,000 queries/s offered
 
+  wide       the batched path on the 4..7-vertex queries of the same 2^22
+             graph (workload rmat22_k4to7, the widest query sizes with
+             decidable draws): device-timed queries/s and embeddings/s,
+             every count checked
   reference_binary  the reference's own filter and join (compiled from its
              sources for sm_103a, oracle/_ref/ref_match) against the plain
              path on the same 2^20-vertex R-MAT queries (those the reference
@@ -67,6 +71,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-rates", default="100,1000,5000")
+    ap.add_argument("--no-wide", action="store_true", help="skip the 4..7-vertex query leg")
     ap.add_argument("--no-reference-binary", action="store_true",
                     help="skip the leg that runs the reference's own GPU filter and join")
     ap.add_argument("--tune", action="store_true",
@@ -197,6 +202,45 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
                     "sustained_qps": n / (last - first), "counts_ok": ok, "slices": ss.slices, "bells": ss.bells,
                     "retired_in_slice": ss.retired_in_slice, "slice_s": ss.slice_s, "between_s": ss.between_s})
     return out
+
+
+def wide_leg(ctx, dev, stream, flush, steps=3, warmup=2):
+    """Batched path on the rmat22_k4to7 queries against the resident 2^22
+    graph (the same graph as rmat22): device time of `steps` passes after
+    `warmup`, L2 flushed before each, every count checked."""
+    import torch
+    from clustersm_gb300 import native
+    from clustersm_gb300.native import Plan
+    from clustersm_gb300.workloads import load
+    wl = load("rmat22_k4to7")
+    if not (ROOT / wl.queries_file).exists():
+        return {"unavailable": f"{wl.queries_file} not generated"}
+    qs, want, meta = wl.queries()
+    plans = [Plan(q) for q in qs]
+    counts, _ = native.match_batch(ctx, dev, plans)
+    bad = sum(1 for c, w in zip(counts.tolist(), want) if w is not None and int(c) != int(w))
+    for _ in range(warmup):
+        native.match_batch(ctx, dev, plans, profile=True)
+    ms, jms, fms = [], 0.0, 0.0
+    for _ in range(steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        counts, st = native.match_batch(ctx, dev, plans, profile=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        jms += st.join_ms
+        fms += st.filter_ms
+    tot = sum(ms) / 1e3
+    ks = sorted({q["k"] for q in meta["queries"]})
+    return {"workload": wl.name, "description": wl.description, "queries": len(plans), "k": ks,
+            "queries_per_s": len(plans) * steps / tot, "embeddings_per_s": int(counts.sum()) * steps / tot,
+            "embeddings_per_step": int(counts.sum()), "ms_per_step": 1e3 * tot / steps,
+            "join_ms_per_step": jms / steps, "filter_ms_per_step": fms / steps,
+            "counts_checked": sum(1 for w in want if w is not None), "count_mismatches": bad,
+            "verified_by": meta.get("verified_by")}
 
 
 def reference_binary_leg(ctx, repeats=3):
@@ -422,6 +466,10 @@ def main():
             native.match(ctx, dev, p)
         plain_qps = ns / (time.perf_counter() - t)
 
+    wide = None
+    if not args.no_wide and world == 1 and wl.name == "rmat22" and not args.shape and not args.subset:
+        wide = wide_leg(ctx, dev, stream, flush)
+
     ref_bin = None
     if not args.no_reference_binary and world == 1:
         ref_bin = reference_binary_leg(ctx)
@@ -476,6 +524,7 @@ def main():
                                 "algorithmic_bytes_per_step": fbytes / args.steps},
             "clocks": clocks,
             "tuning": tuning,
+            "wide": wide,
             "reference_binary": ref_bin,
             "serving": serve,
         }

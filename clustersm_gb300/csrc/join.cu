@@ -439,6 +439,104 @@ __device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, c
   return true;
 }
 
+// Entries a lane tests per refill of an intermediate level.  The tests are
+// chains of dependent loads (candidate bit, then a hub bitmap word or a
+// binary search per back edge); a lane runs kWays chains in lockstep so that
+// their loads are in flight together.
+constexpr int kWays = 1;
+
+// accept() for the kWays entries w[i] of a lane whose bit i of `live` is set;
+// returns the entries that pass.  The same tests in the same order as
+// accept(), with every step issued for all live entries before any of them
+// is resolved.
+__device__ __forceinline__ uint32_t accept_multi(const WarpView &S, const JoinLaunch &p, const CandView &cv,
+                                                 bool use_labels, uint32_t level, const uint32_t (&w)[kWays],
+                                                 uint32_t live, uint32_t &probes) {
+  const uint32_t u = S.ord[level];
+  // candidate bits
+  uint32_t word[kWays];
+#pragma unroll
+  for (int i = 0; i < kWays; ++i) {
+    word[i] = 0;
+    if ((live >> i) & 1u) {
+      if (!SMG_DCHECK(w[i] < p.n, 105, w[i], level)) {
+        live &= ~(1u << i);
+        continue;
+      }
+      word[i] = cv.bits ? __ldg(cv.bits + u * cv.words + (w[i] >> 5)) : __ldg(cv.mask + w[i]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < kWays; ++i) {
+    const uint32_t bit = cv.bits ? (w[i] & 31) : u;
+    if (!((word[i] >> bit) & 1u)) live &= ~(1u << i);
+  }
+  // injectivity against the matched vertices of the same label
+  for (uint32_t b = S.slab[level]; b && live; b &= b - 1) {
+    const uint32_t x = S.m[__ffs(b) - 1];
+#pragma unroll
+    for (int i = 0; i < kWays; ++i)
+      if (w[i] == x) live &= ~(1u << i);
+  }
+  // membership in the lists of the back neighbours other than the pivot
+  const uint32_t bucket = use_labels ? S.lbk[level] : kNone;
+  for (uint32_t b = S.bmask[level] & ~(1u << S.piv[level]); b && live; b &= b - 1) {
+    const uint32_t j = __ffs(b) - 1;
+    const uint32_t hub = S.hub[j];
+    if (p.probe_runs || p.lab_rank) {  // the rarer layouts: one entry at a time
+#pragma unroll
+      for (int i = 0; i < kWays; ++i)
+        if (((live >> i) & 1u) && !is_neighbor(p, S.m[j], S.beg[j], S.deg[j], hub, bucket, w[i], probes))
+          live &= ~(1u << i);
+    } else if (hub != kNone && SMG_DCHECK(hub < p.num_hubs, 102, hub, p.num_hubs)) {
+      const uint32_t *row = p.hub_bits + hub * p.hub_words;
+#pragma unroll
+      for (int i = 0; i < kWays; ++i) {
+        word[i] = 0;
+        if ((live >> i) & 1u) {
+          ++probes;
+          word[i] = __ldg(row + (w[i] >> 5));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kWays; ++i)
+        if (!((word[i] >> (w[i] & 31)) & 1u)) live &= ~(1u << i);
+    } else {
+      // lockstep branchless lower bound over the id-ordered list: every
+      // search takes the same steps for one list, so the loads of all live
+      // entries go out together; an entry equal to w seen on the way, or at
+      // the final position, is a hit
+      const uint32_t *a = p.adj + S.beg[j];
+      uint32_t len = S.deg[j];
+      if (!SMG_DCHECK(static_cast<uint64_t>(S.beg[j]) + len <= p.m2, 104, S.beg[j], len)) len = 0;
+      uint32_t base[kWays], hit = 0;
+#pragma unroll
+      for (int i = 0; i < kWays; ++i) base[i] = 0;
+      for (uint32_t nn = len; nn > 1;) {
+        const uint32_t half = nn >> 1;
+#pragma unroll
+        for (int i = 0; i < kWays; ++i) {
+          if ((live >> i) & 1u) {
+            ++probes;
+            const uint32_t x = __ldg(a + base[i] + half);
+            if (x < w[i]) base[i] += half;
+            if (x == w[i]) hit |= 1u << i;
+          }
+        }
+        nn -= half;
+      }
+#pragma unroll
+      for (int i = 0; i < kWays; ++i) {
+        if (((live >> i) & 1u) && !((hit >> i) & 1u)) {
+          ++probes;
+          if (!(len && __ldg(a + base[i]) == w[i])) live &= ~(1u << i);
+        }
+      }
+    }
+  }
+  return live;
+}
+
 // A last-level list longer than kSplitLen is cut into slices of that length:
 // the first stays with this lane, the others become tasks (level P + 1, range
 // [lo, hi) of the list, prefix m[0..P-1] plus candidate v) when warps are
@@ -1007,6 +1105,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     cv.mask = Q.candmask;
     unsigned long long cnt = 0;
     bool aborted = false, preempted = false;
+    uint32_t iter = 0;  // steps of this task (work limit)
     if (L0 == P + 1) {
       // a slice of one last-level list, split off by last_level
       cnt = last_level_range(S, p, Q, cv, P, lo, hi, lane, scanned, probes);
@@ -1030,7 +1129,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     }
     __syncwarp();
 
-    uint32_t level = L0, iter = 0, tick = 0;  // tick paces donation checks
+    uint32_t level = L0, tick = 0;  // tick paces donation checks
 
     const uint32_t donate_min = max(2u, Q.donate_min ? Q.donate_min : p.donate_min);
     while (true) {
@@ -1147,28 +1246,45 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       const uint32_t c = S.cur[level];
       uint32_t e = S.end[level];
       if (c < e) {
-        // refill the batch with the next 32 tested entries
-        const uint32_t n = min(32u, e - c);
+        // refill the batch: test the next 32 x kWays entries (entry c + 32 i
+        // + lane in way i), keep the first 32 that pass in list order, and
+        // resume after the last one kept (entries beyond it are tested again)
+        const uint32_t n = min(32u * kWays, e - c);
         scanned += n;
         const uint32_t *base = S.lbase[level];
-        bool good = false;
-        uint32_t w = 0;
-        if (lane < n && SMG_DCHECK(level == 0 ? c + lane < *Q.num_roots
-                                                : in_lists(p, base + c + lane),
-                                   114, c + lane, level)) {
-          w = __ldg(base + c + lane);
-          good = SMG_DCHECK(w < p.n, 112, w, level) && (level == 0 || accept(S, p, cv, Q.use_labels, level, w, probes));
+        uint32_t w[kWays], live = 0;
+#pragma unroll
+        for (int i = 0; i < kWays; ++i) {
+          const uint32_t t = 32u * i + lane;
+          w[i] = 0;
+          if (t < n && SMG_DCHECK(level == 0 ? c + t < *Q.num_roots : in_lists(p, base + c + t), 114, c + t, level)) {
+            w[i] = __ldg(base + c + t);
+            if (SMG_DCHECK(w[i] < p.n, 112, w[i], level)) live |= 1u << i;
+          }
         }
-        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
-        if (good) {
-          S.batch[level * 32 + __popc(bal & lt)] = w;
-          S.bpos[level * 32 + __popc(bal & lt)] = c + lane;
+        if (level != 0) live = accept_multi(S, p, cv, Q.use_labels, level, w, live, probes);
+        uint32_t taken = 0, stop = n;
+#pragma unroll
+        for (int i = 0; i < kWays; ++i) {
+          const bool good = (live >> i) & 1u;
+          const uint32_t bal = __ballot_sync(0xFFFFFFFFu, good);
+          if (taken < 32 && bal) {
+            const uint32_t room = 32 - taken;
+            const uint32_t keep = __ballot_sync(0xFFFFFFFFu, good && __popc(bal & lt) < room);
+            if ((keep >> lane) & 1u) {
+              const uint32_t pos = taken + __popc(keep & lt);
+              S.batch[level * 32 + pos] = w[i];
+              S.bpos[level * 32 + pos] = c + 32u * i + lane;
+            }
+            taken += __popc(keep);
+            if (taken == 32) stop = 32u * i + (31 - __clz(keep)) + 1;
+          }
         }
         __syncwarp();
         if (lane == 0) {
-          S.bcnt[level] = __popc(bal);
+          S.bcnt[level] = taken;
           S.bidx[level] = 0;
-          S.cur[level] = c + n;
+          S.cur[level] = c + stop;
         }
         __syncwarp();
         continue;
@@ -1184,6 +1300,12 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       if (cnt) {
         const unsigned long long before = atomicAdd(Q.count, cnt);
         if (Q.count_limit && before + cnt > Q.count_limit) *Q.over = 1;
+      }
+      // the steps of this task not yet charged in blocks of 256, plus one for
+      // the task itself (a query split into many short tasks is charged too)
+      if (Q.work_limit) {
+        const unsigned long long w = (iter & 255u) + 1u;
+        if (atomicAdd(Q.work, w) + w > Q.work_limit) *Q.over = 1;
       }
       atomicAdd(&qs->scanned, scanned);
       atomicAdd(&qs->descents, descents);

@@ -52,7 +52,21 @@ SPECS = {
     "er1k": (96, [4], ["induced"], 10**8),
     "rmat20": (96, [4, 5], ["tree", "sparse", "dense"], 10**8),
     "rmat22": (1024, [4, 5], ["tree", "sparse", "dense"], 10**7),
+    # the widest query sizes with decidable draws on R-MAT 2^22 (the
+    # feasibility table): k = 4..7 in turn, each with every shape in turn
+    "rmat22_k4to7": (128, [4, 5, 6, 7], ["tree", "sparse", "dense"], 10**10),
 }
+# join steps a screened query may take (bounds the draws whose count is out of reach)
+WORK_LIMIT = {"rmat22_k4to7": 1 << 30}
+
+
+def slot_shape(name, slot):
+    """(k, shape) of a slot: the wide workload cycles k first, then shapes;
+    the others draw k at random and cycle shapes."""
+    nq, ks, shapes, _ = SPECS[name]
+    if name == "rmat22_k4to7":
+        return ks[slot % len(ks)], shapes[(slot // len(ks)) % len(shapes)]
+    return None, shapes[slot % len(shapes)]
 
 
 def draws(name):
@@ -78,6 +92,10 @@ def phases(name):
     their shape, and then to 4-vertex dense ones."""
     if name == "rmat22":
         return [(64, None, None), (256, 4, None), (64, 4, "dense")]
+    if name == "rmat22_k4to7":
+        # trees of 6 or more vertices and most sparse ones are out of reach:
+        # such slots fall back to dense queries of their size
+        return [(64, None, None), (512, None, "dense")]
     return [(MAX_DRAWS, None, None)]
 
 
@@ -111,7 +129,12 @@ def gen_gpu(name, seconds=None, resume=None, per_round=16):
     dev = DeviceGraph(ctx, host)
     rng = random.Random(f"{name}-slots")
     slot_k = [rng.choice(ks) for _ in range(nq)]
-    plan_of = {s: list(slot_attempts(name, s, slot_k[s], shapes[s % len(shapes)])) for s in range(nq)}
+    slot_sh = [shapes[s % len(shapes)] for s in range(nq)]
+    for s in range(nq):
+        k0, sh0 = slot_shape(name, s)
+        if k0 is not None:
+            slot_k[s], slot_sh[s] = k0, sh0
+    plan_of = {s: list(slot_attempts(name, s, slot_k[s], slot_sh[s])) for s in range(nq)}
     kept, nxt = {}, {s: 0 for s in range(nq)}
     tried = timeouts = 0
     if resume:
@@ -158,14 +181,14 @@ def gen_gpu(name, seconds=None, resume=None, per_round=16):
         tried += len(batch)
         plans = [Plan(b[5]) for b in batch]
         try:
-            counts, _ = native.match_batch(ctx, dev, plans, max_count=limit)
+            counts, _ = native.match_batch(ctx, dev, plans, max_count=limit, max_work=WORK_LIMIT.get(name, 0))
             results = [None if c == 2**64 - 1 else int(c) for c in counts.tolist()]
         except SmgError as e:
             print(f"{name}: round {rnd}: batched screening failed ({e}); screening one by one", flush=True)
             results = []
             for p in plans:
                 try:
-                    r, _ = native.match(ctx, dev, p, max_count=limit)
+                    r, _ = native.match(ctx, dev, p, max_count=limit, max_work=WORK_LIMIT.get(name, 0))
                     results.append(None if r.limit_hit else int(r.count))
                 except SmgError as e1:
                     timeouts += 1
@@ -197,9 +220,13 @@ def verify(name, src=None):
     host = wl.graph()
     t0 = time.time()
     bad = 0
-    for rec in data["queries"]:
+    for j, rec in enumerate(data["queries"]):
         q = Query(rec["labels"], rec["edges"])
+        t1 = time.time()
         rec["count"] = oracle.count(host, q)
+        if os.environ.get("WORKLOAD_PROGRESS"):
+            print(f"{name}: {j + 1}/{len(data['queries'])} k={rec['k']} count={rec['count']} "
+                  f"{time.time() - t1:.1f} s", flush=True)
         if rec["count"] != rec["gpu_count"]:
             bad += 1
             print(f"MISMATCH slot {rec['slot']}: oracle {rec['count']} gpu {rec['gpu_count']}")
@@ -305,7 +332,9 @@ if __name__ == "__main__":
     resume = os.environ.get("WORKLOAD_RESUME") or None
     for n in names:
         if mode == "gpu":
-            gen_gpu(n, budget, resume)
+            # rounds of the wide workload hold queries of up to 10^10 embeddings
+            per_round = int(os.environ.get("WORKLOAD_PER_ROUND", "4" if n == "rmat22_k4to7" else "16"))
+            gen_gpu(n, budget, resume, per_round=per_round)
         elif mode == "feasibility":
             feasibility(n)
         else:
