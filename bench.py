@@ -24,6 +24,12 @@ the device-resident data graph.  Prints one JSON line (rank 0).
              graph (workload rmat22_k4to7, the widest query sizes with
              decidable draws): device-timed queries/s and embeddings/s,
              every count checked
+  c4         the large graph: R-MAT 2^25 vertices, avg degree 32, 64 Zipf
+             labels, built on the device from its raw edge draws
+             (smg_graph_build: radix sort, de-duplication, 64-bit offsets),
+             its resident bytes, and 12-vertex sparse and dense walk queries:
+             how many are decidable under a work limit, and the filter's time
+             and roofline on them
   reference_binary  the reference's own filter and join (compiled from its
              sources for sm_103a, oracle/_ref/ref_match) against the plain
              path on the same 2^20-vertex R-MAT queries (those the reference
@@ -72,6 +78,8 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-rates", default="100,1000,5000")
     ap.add_argument("--no-wide", action="store_true", help="skip the 4..7-vertex query leg")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 2^25-vertex graph leg")
+    ap.add_argument("--c4-scale", type=int, default=25)
     ap.add_argument("--no-reference-binary", action="store_true",
                     help="skip the leg that runs the reference's own GPU filter and join")
     ap.add_argument("--tune", action="store_true",
@@ -201,6 +209,52 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
         out.append({"offered_qps": rate, "requests": n, "p50_ms": lat[n // 2], "p99_ms": lat[(99 * (n - 1)) // 100],
                     "sustained_qps": n / (last - first), "counts_ok": ok, "slices": ss.slices, "bells": ss.bells,
                     "retired_in_slice": ss.retired_in_slice, "slice_s": ss.slice_s, "between_s": ss.between_s})
+    return out
+
+
+def c4_leg(ctx, peak, scale=25, avg_degree=32, labels=64, seed=1, draws=64, k=12):
+    """The large-graph configuration: build, resident bytes, and k-vertex
+    sparse and dense walk queries (decided under a count and a work limit;
+    the filter's device time and algorithmic bytes over all of them)."""
+    from clustersm_gb300 import native
+    from clustersm_gb300.native import DeviceGraph, HostGraph, Plan, Query, SmgError
+    t0 = time.perf_counter()
+    pairs = HostGraph.rmat_pairs(scale, avg_degree, seed)
+    lab = HostGraph.labels_for(1 << scale, labels, seed)
+    t_gen = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    dev = DeviceGraph.build(ctx, 1 << scale, pairs, lab)
+    t_build = time.perf_counter() - t1
+    del pairs
+    st = dev.stats()
+    off, adj = dev.download()
+
+    class CsrView:  # the downloaded CSR as the query generator's input (no copy)
+        csr = native.Csr(len(lab), len(adj) // 2, off.ctypes.data_as(native.u64p), adj.ctypes.data_as(native.u32p),
+                         lab.ctypes.data_as(native.u32p))
+    host = CsrView()
+    out = {"graph": f"R-MAT(0.57,0.19,0.19,0.05) 2^{scale} vertices, avg degree {avg_degree}, {labels} Zipf labels",
+           "vertices": st.num_vertices, "edges": st.num_edges, "max_degree": st.max_degree,
+           "device_bytes": st.device_bytes, "generate_s": t_gen, "smg_graph_build_s": t_build, "queries": {}}
+    for shape in ("sparse", "dense"):
+        qs = []
+        for a in range(draws):
+            try:
+                qs.append(Query.generate(host, k, shape, seed=(1 << 41) | (k << 24) | a))
+            except SmgError:
+                pass
+        plans = [Plan(q) for q in qs]
+        try:
+            counts, bst = native.match_batch(ctx, dev, plans, profile=True, max_count=10**10, max_work=1 << 30)
+            decided = [int(c) for c in counts.tolist() if c != 2**64 - 1]
+            fgb = bst.filter_bytes / (bst.filter_ms / 1e3) / 1e9 if bst.filter_ms > 0 else 0.0
+            out["queries"][shape] = {"k": k, "drawn": len(qs), "decided": len(decided),
+                                     "counts_decided": sorted(decided)[:8], "filter_ms": bst.filter_ms,
+                                     "filter_bytes": bst.filter_bytes, "filter_gbs": fgb, "filter_frac": fgb / peak,
+                                     "join_ms": bst.join_ms}
+        except SmgError as e:
+            out["queries"][shape] = {"k": k, "drawn": len(qs), "error": str(e)[:200]}
+    dev.free()
     return out
 
 
@@ -470,6 +524,11 @@ def main():
     if not args.no_wide and world == 1 and wl.name == "rmat22" and not args.shape and not args.subset:
         wide = wide_leg(ctx, dev, stream, flush)
 
+    peaks0 = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    c4 = None
+    if not args.no_c4 and world == 1 and not args.shape and not args.subset:
+        c4 = c4_leg(ctx, peaks0.get("hbm_gbs", 6800.0), scale=args.c4_scale)
+
     ref_bin = None
     if not args.no_reference_binary and world == 1:
         ref_bin = reference_binary_leg(ctx)
@@ -525,6 +584,7 @@ def main():
             "clocks": clocks,
             "tuning": tuning,
             "wide": wide,
+            "c4": c4,
             "reference_binary": ref_bin,
             "serving": serve,
         }

@@ -32,7 +32,7 @@ ORACLE_LIB = ORACLE_DIR / "lib"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SRCS = ["io.cpp", "gen.cpp", "plan.cpp", "serve.cpp"]
-CUDA_SRCS = ["api.cu", "filter.cu", "join.cu", "noalloc.cu"]
+CUDA_SRCS = ["api.cu", "filter.cu", "join.cu", "noalloc.cu", "graph_build.cu"]
 HEADERS = [INCLUDE / "smg.h"] + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh"))
 
 

@@ -107,6 +107,61 @@ uint64_t time_limit_ns() {
 
 using namespace smg;
 
+namespace smg {
+// Everything a resident graph holds besides off/adj (already on the device):
+// labels, vertices grouped by label, neighbour-label counts, the label index
+// and the hub bitmaps.  offsets/adj/labels are the same CSR in host memory.
+smg_status finish_resident(smg_ctx *c, DevGraph &g, const uint64_t *offsets, const uint32_t *adj_src,
+                           const uint32_t *labels, uint32_t maxl, uint32_t maxd) {
+  const uint32_t n = g.n;
+  g.num_labels = n ? maxl + 1 : 0;
+  g.max_degree = maxd;
+  g.label_count.assign(std::min<uint32_t>(g.num_labels, kMaxLabels), 0);
+  for (uint32_t v = 0; v < n; ++v)
+    if (labels[v] < kMaxLabels) ++g.label_count[labels[v]];
+  // vertex ids grouped by label (labels >= kMaxLabels, which no query has, at the end)
+  std::vector<uint32_t> lverts(std::max<uint32_t>(n, 1));
+  {
+    const size_t nl = g.label_count.size();
+    g.lvert_start.assign(nl + 1, 0);
+    for (size_t l = 0; l < nl; ++l) g.lvert_start[l + 1] = g.lvert_start[l] + static_cast<uint32_t>(g.label_count[l]);
+    std::vector<uint32_t> at(g.lvert_start.begin(), g.lvert_start.end() - 1);
+    uint32_t tail = g.lvert_start[nl];
+    for (uint32_t v = 0; v < n; ++v) {
+      const uint32_t l = labels[v];
+      lverts[l < nl ? at[l]++ : tail++] = v;
+    }
+  }
+  const uint32_t ncols = std::min<uint32_t>(g.num_labels, kMaxLabels);
+  g.nlc_stride = std::max<uint32_t>(16, (ncols + 15) & ~15u);
+  const size_t b_lab = std::max<size_t>(n, 1) * 4, b_nlc = std::max<size_t>(n, 1) * g.nlc_stride;
+  SMG_CUDA(cudaMalloc(&g.label, b_lab));
+  SMG_CUDA(cudaMalloc(&g.nlc, b_nlc));
+  SMG_CUDA(cudaMalloc(&g.lverts, b_lab));
+  g.bytes += 2 * b_lab + b_nlc;
+  if (n) SMG_CUDA(cudaMemcpyAsync(g.label, labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
+  if (n) SMG_CUDA(cudaMemcpyAsync(g.lverts, lverts.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
+  smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
+  if (st) return st;
+  if (label_index_enabled()) {
+    // the id-ordered lists the device got; built first: the hub bitmaps take
+    // its label layout
+    st = build_label_index(g, offsets, adj_src, labels, label_index_min_degree(), 1ull << 30, c->stream);
+    if (st) return st;
+  }
+  {
+    std::vector<uint32_t> deg(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t v = 0; v < static_cast<int64_t>(n); ++v)
+      deg[v] = static_cast<uint32_t>(offsets[v + 1] - offsets[v]);
+    st = build_hub_bitmaps(g, hub_min_degree(), hub_max_bytes(), c->stream, deg);
+    if (st) return st;
+  }
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
+  return SMG_OK;
+}
+}  // namespace smg
+
 extern "C" {
 
 smg_status smg_open(int device, smg_ctx **out) {
@@ -205,57 +260,78 @@ smg_status smg_graph_upload(smg_ctx *c, const smg_csr *in, smg_graph **out) {
     if (bad) return fail(SMG_ERR_INVALID, "repeated edge");
     adj_src = sorted.data();
   }
-  g.num_labels = n ? maxl + 1 : 0;
-  g.max_degree = maxd;
-  g.label_count.assign(std::min<uint32_t>(g.num_labels, kMaxLabels), 0);
-  for (uint32_t v = 0; v < n; ++v)
-    if (in->labels[v] < kMaxLabels) ++g.label_count[in->labels[v]];
-  // vertex ids grouped by label (labels >= kMaxLabels, which no query has, at the end)
-  std::vector<uint32_t> lverts(std::max<uint32_t>(n, 1));
-  {
-    const size_t nl = g.label_count.size();
-    g.lvert_start.assign(nl + 1, 0);
-    for (size_t l = 0; l < nl; ++l) g.lvert_start[l + 1] = g.lvert_start[l] + static_cast<uint32_t>(g.label_count[l]);
-    std::vector<uint32_t> at(g.lvert_start.begin(), g.lvert_start.end() - 1);
-    uint32_t tail = g.lvert_start[nl];
-    for (uint32_t v = 0; v < n; ++v) {
-      const uint32_t l = in->labels[v];
-      lverts[l < nl ? at[l]++ : tail++] = v;
-    }
-  }
-  const uint32_t ncols = std::min<uint32_t>(g.num_labels, kMaxLabels);
-  g.nlc_stride = std::max<uint32_t>(16, (ncols + 15) & ~15u);
-  const size_t b_off = (static_cast<size_t>(n) + 1) * 4, b_adj = std::max<uint64_t>(m2, 1) * 4,
-               b_lab = std::max<size_t>(n, 1) * 4, b_nlc = std::max<size_t>(n, 1) * g.nlc_stride;
+  const size_t b_off = (static_cast<size_t>(n) + 1) * 4, b_adj = std::max<uint64_t>(m2, 1) * 4;
   SMG_CUDA(cudaMalloc(&g.off, b_off));
   SMG_CUDA(cudaMalloc(&g.adj, b_adj));
-  SMG_CUDA(cudaMalloc(&g.label, b_lab));
-  SMG_CUDA(cudaMalloc(&g.nlc, b_nlc));
-  SMG_CUDA(cudaMalloc(&g.lverts, b_lab));
-  g.bytes = b_off + b_adj + 2 * b_lab + b_nlc;
+  g.bytes = b_off + b_adj;
   SMG_CUDA(cudaMemcpyAsync(g.off, off32.data(), b_off, cudaMemcpyHostToDevice, c->stream));
   if (m2) SMG_CUDA(cudaMemcpyAsync(g.adj, adj_src, m2 * 4, cudaMemcpyHostToDevice, c->stream));
-  if (n) SMG_CUDA(cudaMemcpyAsync(g.label, in->labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
-  if (n) SMG_CUDA(cudaMemcpyAsync(g.lverts, lverts.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
-  smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
+  smg_status st = finish_resident(c, g, in->offsets, adj_src, in->labels, maxl, maxd);
   if (st) return st;
-  if (label_index_enabled()) {
-    // the id-ordered lists the device got (the caller's, or their sorted copy);
-    // built first: the hub bitmaps take its label layout
-    st = build_label_index(g, in->offsets, adj_src, in->labels, label_index_min_degree(), 1ull << 30, c->stream);
-    if (st) return st;
-  }
-  {
-    std::vector<uint32_t> deg(n);
-#pragma omp parallel for schedule(static)
-    for (int64_t v = 0; v < static_cast<int64_t>(n); ++v)
-      deg[v] = static_cast<uint32_t>(in->offsets[v + 1] - in->offsets[v]);
-    st = build_hub_bitmaps(g, hub_min_degree(), hub_max_bytes(), c->stream, deg);
-    if (st) return st;
-  }
-  SMG_CUDA(cudaStreamSynchronize(c->stream));
   G->device = c->device;
   *out = G.release();
+  return SMG_OK;
+}
+
+smg_status smg_graph_build(smg_ctx *c, uint32_t num_vertices, uint64_t num_pairs, const uint32_t *pairs,
+                           const uint32_t *labels, smg_graph **out, uint64_t *num_edges) {
+  if (!c || !out || (num_vertices && !labels) || (num_pairs && !pairs)) return fail(SMG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const uint32_t n = num_vertices;
+  if (n == 0xFFFFFFFFu) return fail(SMG_ERR_LIMIT, "too many vertices");
+  if (num_pairs >= (1ull << 31)) return fail(SMG_ERR_LIMIT, "2^31 or more edge pairs");
+  SMG_CUDA(cudaSetDevice(c->device));
+  std::unique_ptr<smg_graph> G(new smg_graph);
+  DevGraph &g = G->g;
+  g.n = n;
+  unsigned long long *off64 = nullptr;
+  uint32_t *adj = nullptr;
+  uint64_t m2 = 0;
+  smg_status st = build_csr_device(c, n, num_pairs, pairs, &off64, &adj, &m2);
+  if (st) return st;
+  g.m2 = m2;
+  g.adj = adj;
+  // the join indexes lists with 32-bit offsets; 2|E| < 2^32 holds here
+  // because the pairs are fewer than 2^31
+  const size_t b_off = (static_cast<size_t>(n) + 1) * 4;
+  SMG_CUDA(cudaMalloc(&g.off, b_off));
+  g.bytes = b_off + std::max<uint64_t>(m2, 1) * 4;
+  st = narrow_offsets(off64, g.off, static_cast<uint64_t>(n) + 1, c->stream, c->num_sms);
+  if (st) {
+    cudaFree(off64);
+    return st;
+  }
+  // the host copy of the CSR the label index and the hub selection read
+  std::vector<uint64_t> offsets(static_cast<size_t>(n) + 1);
+  std::vector<uint32_t> adj_host(std::max<uint64_t>(m2, 1));
+  SMG_CUDA(cudaMemcpyAsync(offsets.data(), off64, offsets.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (m2) SMG_CUDA(cudaMemcpyAsync(adj_host.data(), adj, m2 * 4, cudaMemcpyDeviceToHost, c->stream));
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
+  cudaFree(off64);
+  uint32_t maxl = 0, maxd = 0;
+#pragma omp parallel for schedule(static) reduction(max : maxl, maxd)
+  for (int64_t v = 0; v < static_cast<int64_t>(n); ++v) {
+    maxd = std::max<uint32_t>(maxd, static_cast<uint32_t>(offsets[v + 1] - offsets[v]));
+    maxl = std::max(maxl, labels[v]);
+  }
+  st = finish_resident(c, g, offsets.data(), adj_host.data(), labels, maxl, maxd);
+  if (st) return st;
+  if (num_edges) *num_edges = m2 / 2;
+  G->device = c->device;
+  *out = G.release();
+  return SMG_OK;
+}
+
+smg_status smg_graph_download(smg_ctx *c, const smg_graph *G, uint64_t *offsets, uint32_t *neighbors) {
+  if (!c || !G || !offsets || (G->g.m2 && !neighbors)) return fail(SMG_ERR_INVALID, "null argument");
+  if (G->device != c->device) return fail(SMG_ERR_INVALID, "graph lives on another device");
+  SMG_CUDA(cudaSetDevice(c->device));
+  const DevGraph &g = G->g;
+  std::vector<uint32_t> off32(static_cast<size_t>(g.n) + 1);
+  SMG_CUDA(cudaMemcpyAsync(off32.data(), g.off, off32.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (g.m2) SMG_CUDA(cudaMemcpyAsync(neighbors, g.adj, g.m2 * 4, cudaMemcpyDeviceToHost, c->stream));
+  SMG_CUDA(cudaStreamSynchronize(c->stream));
+  for (size_t i = 0; i < off32.size(); ++i) offsets[i] = off32[i];
   return SMG_OK;
 }
 

@@ -126,6 +126,16 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
 constexpr uint32_t kMaxWalkPhases = 2 * 100;  // 2 * MAX_LAYERS - 1 phases at most
 constexpr uint32_t kWalkCap = 1u << 20;        // chunk-pass items per filter launch
 
+// Sorted, duplicate-free CSR of an undirected edge list (host pairs), built
+// on the device (graph_build.cu): 64-bit offsets [n + 1] and neighbours
+// [*m2], both device allocations the caller frees.
+smg_status build_csr_device(smg_ctx *c, uint32_t n, uint64_t np, const uint32_t *pairs_host,
+                            unsigned long long **off64, uint32_t **adj, uint64_t *m2);
+smg_status narrow_offsets(const unsigned long long *off64, uint32_t *off32, uint64_t n1, cudaStream_t s, int num_sms);
+// Labels, label groups, neighbour-label counts, label index and hub bitmaps
+// of a graph whose off/adj are on the device (the same CSR in host memory).
+smg_status finish_resident(smg_ctx *c, DevGraph &g, const uint64_t *offsets, const uint32_t *adj,
+                           const uint32_t *labels, uint32_t maxl, uint32_t maxd);
 // Filter + join for `nq` plans against a resident graph; splits into chunks
 // that fit the device memory.  out[i] receives plan i's results.
 smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, uint32_t nq, const RunOpts &o,

@@ -75,17 +75,21 @@ struct LabelSampler {
   }
 };
 
-void draw_labels(HostGraph &g, uint32_t L, uint32_t dist, uint64_t seed) {
+void draw_labels_into(uint32_t n, uint32_t L, uint32_t dist, uint64_t seed, uint32_t *label) {
   LabelSampler ls(L, dist);
-  g.label.resize(g.n);
   const int64_t chunk = 1 << 16;
-  const int64_t nchunks = (static_cast<int64_t>(g.n) + chunk - 1) / chunk;
+  const int64_t nchunks = (static_cast<int64_t>(n) + chunk - 1) / chunk;
 #pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < nchunks; ++c) {
     Rng r(stream_seed(seed, 2, static_cast<uint64_t>(c)));
-    int64_t e = std::min<int64_t>(g.n, (c + 1) * chunk);
-    for (int64_t v = c * chunk; v < e; ++v) g.label[v] = ls.draw(r);
+    int64_t e = std::min<int64_t>(n, (c + 1) * chunk);
+    for (int64_t v = c * chunk; v < e; ++v) label[v] = ls.draw(r);
   }
+}
+
+void draw_labels(HostGraph &g, uint32_t L, uint32_t dist, uint64_t seed) {
+  g.label.resize(g.n);
+  draw_labels_into(g.n, L, dist, seed, g.label.data());
 }
 
 // Symmetrise a directed edge list into a CSR with sorted, duplicate-free
@@ -128,6 +132,38 @@ void build_simple_csr(uint32_t n, const std::vector<uint32_t> &src, const std::v
     std::copy(tmp.begin() + static_cast<int64_t>(cnt[v]),
               tmp.begin() + static_cast<int64_t>(cnt[v] + (uniq[v + 1] - uniq[v])),
               g.adj.begin() + static_cast<int64_t>(uniq[v]));
+}
+
+// R-MAT edge draws of stream 3: draw i goes to src[i * stride], dst[i * stride].
+void rmat_draws(uint32_t scale, uint64_t draws, uint64_t seed, uint32_t *src, uint32_t *dst, uint64_t stride) {
+  // (a, a+b, a+b+c) = (0.57, 0.76, 0.95) on a 16-bit grid
+  const uint32_t TA = 37356, TB = 49807, TC = 62259;
+  const int64_t chunk = 1 << 20;
+  const int64_t nchunks = static_cast<int64_t>((draws + chunk - 1) / chunk);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    Rng r(stream_seed(seed, 3, static_cast<uint64_t>(c)));
+    const int64_t e = std::min<int64_t>(static_cast<int64_t>(draws), (c + 1) * chunk);
+    for (int64_t i = c * chunk; i < e; ++i) {
+      uint32_t u = 0, v = 0;
+      uint64_t bits = 0;
+      int left = 0;
+      for (uint32_t lvl = 0; lvl < scale; ++lvl) {
+        if (left == 0) {
+          bits = r.next();
+          left = 4;
+        }
+        uint32_t x = static_cast<uint32_t>(bits & 0xFFFF);
+        bits >>= 16;
+        --left;
+        uint32_t bu = x >= TB, bv = (x >= TA && x < TB) || x >= TC;
+        u = (u << 1) | bu;
+        v = (v << 1) | bv;
+      }
+      src[static_cast<uint64_t>(i) * stride] = u;
+      dst[static_cast<uint64_t>(i) * stride] = v;
+    }
+  }
 }
 
 bool adjacent(const smg_csr &g, uint32_t a, uint32_t b) {
@@ -184,41 +220,35 @@ smg_status smg_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels
 #endif
   const uint32_t n = 1u << scale;
   const uint64_t draws = static_cast<uint64_t>(n) * avg_degree / 2;
-  // (a, a+b, a+b+c) = (0.57, 0.76, 0.95) on a 16-bit grid
-  const uint32_t TA = 37356, TB = 49807, TC = 62259;
   std::vector<uint32_t> src(draws), dst(draws);
-  const int64_t chunk = 1 << 20;
-  const int64_t nchunks = static_cast<int64_t>((draws + chunk - 1) / chunk);
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t c = 0; c < nchunks; ++c) {
-    Rng r(stream_seed(seed, 3, static_cast<uint64_t>(c)));
-    const int64_t e = std::min<int64_t>(static_cast<int64_t>(draws), (c + 1) * chunk);
-    for (int64_t i = c * chunk; i < e; ++i) {
-      uint32_t u = 0, v = 0;
-      uint64_t bits = 0;
-      int left = 0;
-      for (uint32_t lvl = 0; lvl < scale; ++lvl) {
-        if (left == 0) {
-          bits = r.next();
-          left = 4;
-        }
-        uint32_t x = static_cast<uint32_t>(bits & 0xFFFF);
-        bits >>= 16;
-        --left;
-        uint32_t bu = x >= TB, bv = (x >= TA && x < TB) || x >= TC;
-        u = (u << 1) | bu;
-        v = (v << 1) | bv;
-      }
-      src[i] = u;
-      dst[i] = v;
-    }
-  }
+  rmat_draws(scale, draws, seed, src.data(), dst.data(), 1);
   std::unique_ptr<smg_host_graph> h(new smg_host_graph);
   build_simple_csr(n, src, dst, h->g);
   std::vector<uint32_t>().swap(src);
   std::vector<uint32_t>().swap(dst);
   draw_labels(h->g, num_labels, label_dist, seed);
   *out = h.release();
+  return SMG_OK;
+}
+
+smg_status smg_gen_rmat_pairs(uint32_t scale, uint32_t avg_degree, uint64_t seed, int threads, uint32_t *pairs,
+                              uint64_t *num_pairs) {
+  if (!num_pairs || scale < 1 || scale > 31 || avg_degree == 0) return fail(SMG_ERR_INVALID, "bad R-MAT arguments");
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  const uint64_t draws = (static_cast<uint64_t>(1) << scale) * avg_degree / 2;
+  *num_pairs = draws;
+  if (pairs) rmat_draws(scale, draws, seed, pairs, pairs + 1, 2);
+  return SMG_OK;
+}
+
+smg_status smg_gen_labels(uint32_t num_vertices, uint32_t num_labels, uint32_t label_dist, uint64_t seed,
+                          uint32_t *labels) {
+  if ((num_vertices && !labels) || num_labels == 0) return fail(SMG_ERR_INVALID, "bad label arguments");
+  draw_labels_into(num_vertices, num_labels, label_dist, seed, labels);
   return SMG_OK;
 }
 

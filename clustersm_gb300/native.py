@@ -132,6 +132,8 @@ def _load():
         "smg_gen_rmat": (st, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int,
                               C.POINTER(vp)]),
         "smg_gen_query": (st, [C.POINTER(Csr), C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(vp), u32p]),
+        "smg_gen_rmat_pairs": (st, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_int, u32p, u64p]),
+        "smg_gen_labels": (st, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, u32p]),
         "smg_plan_create": (st, [C.POINTER(QueryDesc), C.POINTER(vp)]),
         "smg_plan_free": (None, [vp]),
         "smg_plan_get": (st, [vp, C.POINTER(PlanView)]),
@@ -141,6 +143,8 @@ def _load():
         "smg_close": (None, [vp]),
         "smg_ctx_stream": (vp, [vp]),
         "smg_graph_upload": (st, [vp, C.POINTER(Csr), C.POINTER(vp)]),
+        "smg_graph_build": (st, [vp, C.c_uint32, C.c_uint64, u32p, u32p, C.POINTER(vp), u64p]),
+        "smg_graph_download": (st, [vp, vp, u64p, u32p]),
         "smg_graph_free": (None, [vp]),
         "smg_graph_get_stats": (st, [vp, C.POINTER(GraphStats)]),
         "smg_match": (st, [vp, vp, vp, C.POINTER(MatchOpts), C.POINTER(MatchResult)]),
@@ -223,6 +227,23 @@ class HostGraph:
         check(lib.smg_gen_rmat(scale, avg_degree, num_labels, LABELS_ZIPF1 if zipf else LABELS_UNIFORM, seed,
                                threads, C.byref(h)), "smg_gen_rmat")
         return cls(h)
+
+    @staticmethod
+    def rmat_pairs(scale, avg_degree, seed, threads=0):
+        """The raw R-MAT edge draws of rmat() for the same seed: uint32 [m, 2]."""
+        m = C.c_uint64()
+        check(lib.smg_gen_rmat_pairs(scale, avg_degree, seed, threads, None, C.byref(m)), "smg_gen_rmat_pairs")
+        out = np.zeros((m.value, 2), dtype=np.uint32)
+        check(lib.smg_gen_rmat_pairs(scale, avg_degree, seed, threads, out.ctypes.data_as(u32p), C.byref(m)),
+              "smg_gen_rmat_pairs")
+        return out
+
+    @staticmethod
+    def labels_for(n, num_labels, seed, zipf=True):
+        """The labels er()/rmat() draw for the same seed."""
+        out = np.zeros(n, dtype=np.uint32)
+        check(lib.smg_gen_labels(n, num_labels, 1 if zipf else 0, seed, out.ctypes.data_as(u32p)), "smg_gen_labels")
+        return out
 
     @property
     def csr(self) -> Csr:
@@ -382,11 +403,36 @@ class Context:
 class DeviceGraph:
     """A data graph resident in device memory."""
 
-    def __init__(self, ctx: Context, host: HostGraph):
+    def __init__(self, ctx: Context, host: HostGraph | None):
         self.ctx = ctx
         self.host = host
         self._h = C.c_void_p()
-        check(lib.smg_graph_upload(ctx.handle, C.byref(host.csr), C.byref(self._h)), "smg_graph_upload")
+        if host is not None:
+            self.n = host.n
+            check(lib.smg_graph_upload(ctx.handle, C.byref(host.csr), C.byref(self._h)), "smg_graph_upload")
+
+    @classmethod
+    def build(cls, ctx: Context, num_vertices: int, pairs, labels):
+        """smg_graph_build: the CSR is sorted and de-duplicated on the device
+        from an undirected edge list (pairs: [m, 2] or flat uint32)."""
+        g = cls(ctx, None)
+        g.n = int(num_vertices)
+        pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1)
+        labels = np.ascontiguousarray(labels, dtype=np.uint32)
+        ne = C.c_uint64()
+        check(lib.smg_graph_build(ctx.handle, g.n, pairs.size // 2, pairs.ctypes.data_as(u32p),
+                                  labels.ctypes.data_as(u32p), C.byref(g._h), C.byref(ne)), "smg_graph_build")
+        g.num_edges = ne.value
+        return g
+
+    def download(self):
+        """(offsets uint64 [n+1], neighbors uint32 [2m]) of the resident CSR."""
+        st = self.stats()
+        off = np.zeros(st.num_vertices + 1, dtype=np.uint64)
+        nb = np.zeros(max(1, 2 * st.num_edges), dtype=np.uint32)
+        check(lib.smg_graph_download(self.ctx.handle, self._h, off.ctypes.data_as(u64p), nb.ctypes.data_as(u32p)),
+              "smg_graph_download")
+        return off, nb[: 2 * st.num_edges]
 
     @property
     def handle(self):
@@ -455,7 +501,7 @@ def autotune(ctx: Context, graph: DeviceGraph, plans):
 
 
 def filter_inspect(ctx: Context, graph: DeviceGraph, plan: Plan):
-    n = graph.host.n
+    n = graph.n
     vm = np.zeros(n, np.uint32)
     enc = np.zeros(n * plan.view.num_words, np.uint32)
     cm = np.zeros(n, np.uint32)

@@ -75,6 +75,6 @@ WORKLOADS = {
     "rmat22_k4to7": Workload("rmat22_k4to7", "rmat", scale=22, avg_degree=16, labels=32, seed=1,
                              queries_file="tests/golden/workload_rmat22_k4to7.json",
                              description="R-MAT(0.57,0.19,0.19,0.05) 2^22 vertices, avg degree 16, 32 Zipf labels, "
-                                         "128 walk queries of 4, 5, 6 and 7 vertices (32 each; tree/sparse/dense "
-                                         "where decidable, else dense) of at most 10^10 embeddings"),
+                                         "64 walk queries of 4, 5, 6 and 7 vertices (16 each; tree/sparse/dense "
+                                         "where decidable, else dense) of at most 10^9 embeddings"),
 }

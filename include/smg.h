@@ -119,6 +119,16 @@ smg_status smg_gen_er(uint32_t n, uint64_t m, uint32_t num_labels,
 smg_status smg_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels,
                         uint32_t label_dist, uint64_t seed, int threads,
                         smg_host_graph **out);
+/* The raw edge draws of smg_gen_rmat (same seed, same draws, before they are
+ * symmetrised and de-duplicated) as pairs (a0, b0, a1, b1, ...) in
+ * pairs[2 * *num_pairs]; with pairs == NULL only *num_pairs is set.  With the
+ * labels of smg_gen_labels (same seed) they make the same graph through
+ * smg_graph_build. */
+smg_status smg_gen_rmat_pairs(uint32_t scale, uint32_t avg_degree, uint64_t seed, int threads,
+                              uint32_t *pairs, uint64_t *num_pairs);
+/* The vertex labels smg_gen_er / smg_gen_rmat draw for a seed. */
+smg_status smg_gen_labels(uint32_t num_vertices, uint32_t num_labels, uint32_t label_dist,
+                          uint64_t seed, uint32_t *labels);
 /* Random-walk query extraction: k distinct vertices reached by a seeded walk,
  * labels copied, so at least one embedding exists.  shape: */
 #define SMG_SHAPE_TREE 0   /* first-visit edges only                       */
@@ -202,6 +212,23 @@ void *smg_ctx_stream(smg_ctx *ctx);
  * per-vertex neighbour-label counts become device-resident until freed. */
 smg_status smg_graph_upload(smg_ctx *ctx, const smg_csr *g, smg_graph **out);
 void smg_graph_free(smg_graph *g);
+/* Build a data graph on the device from an undirected edge list in host
+ * memory, pairs[2 * num_pairs] = (a0, b0, a1, b1, ...): any order, repeats
+ * and both orientations allowed, self-loops dropped, every endpoint below
+ * num_vertices (else SMG_ERR_INVALID); fewer than 2^31 pairs.  The device
+ * writes both directions of every pair, radix-sorts them by (source,
+ * target), keeps one of each and scans the degrees into 64-bit offsets; the
+ * resident graph is then the same as smg_graph_upload of that CSR.  Replaces
+ * the reference's host CSR build (readGraphToCPU2 io.cu:60-96, one std::map
+ * insert per edge).  *num_edges (may be NULL) receives the distinct
+ * undirected edges. */
+smg_status smg_graph_build(smg_ctx *ctx, uint32_t num_vertices, uint64_t num_pairs,
+                           const uint32_t *pairs, const uint32_t *labels, smg_graph **out,
+                           uint64_t *num_edges);
+/* Copy a resident graph's CSR to host memory: offsets[num_vertices + 1] and
+ * neighbors[2 * num_edges], lists sorted by id. */
+smg_status smg_graph_download(smg_ctx *ctx, const smg_graph *g, uint64_t *offsets,
+                              uint32_t *neighbors);
 
 typedef struct smg_graph_stats {
   uint32_t num_vertices;

@@ -53,8 +53,9 @@ SPECS = {
     "rmat20": (96, [4, 5], ["tree", "sparse", "dense"], 10**8),
     "rmat22": (1024, [4, 5], ["tree", "sparse", "dense"], 10**7),
     # the widest query sizes with decidable draws on R-MAT 2^22 (the
-    # feasibility table): k = 4..7 in turn, each with every shape in turn
-    "rmat22_k4to7": (128, [4, 5, 6, 7], ["tree", "sparse", "dense"], 10**10),
+    # feasibility table): k = 4..7 in turn, each with every shape in turn; at
+    # most 10^9 embeddings, so that the CPU oracle can verify every count
+    "rmat22_k4to7": (64, [4, 5, 6, 7], ["tree", "sparse", "dense"], 10**9),
 }
 # join steps a screened query may take (bounds the draws whose count is out of reach)
 WORK_LIMIT = {"rmat22_k4to7": 1 << 30}
@@ -94,8 +95,9 @@ def phases(name):
         return [(64, None, None), (256, 4, None), (64, 4, "dense")]
     if name == "rmat22_k4to7":
         # trees of 6 or more vertices and most sparse ones are out of reach:
-        # such slots fall back to dense queries of their size
-        return [(64, None, None), (512, None, "dense")]
+        # such slots fall back to dense queries of their size (at k = 7 about
+        # one dense draw in 800 has at most 10^9 embeddings)
+        return [(64, None, None), (8192, None, "dense")]
     return [(MAX_DRAWS, None, None)]
 
 
@@ -333,7 +335,7 @@ if __name__ == "__main__":
     for n in names:
         if mode == "gpu":
             # rounds of the wide workload hold queries of up to 10^10 embeddings
-            per_round = int(os.environ.get("WORKLOAD_PER_ROUND", "4" if n == "rmat22_k4to7" else "16"))
+            per_round = int(os.environ.get("WORKLOAD_PER_ROUND", "16"))
             gen_gpu(n, budget, resume, per_round=per_round)
         elif mode == "feasibility":
             feasibility(n)

@@ -73,3 +73,30 @@ def test_query_shapes(shape):
             assert len(e) == k + 1
         else:
             assert 2 * len(e) >= 3 * k
+
+
+def _csr_from_pairs(n, pairs):
+    """Reference CSR of an undirected edge list in numpy: both directions,
+    self-loops dropped, duplicates removed, lists sorted."""
+    import numpy as np
+    p = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    p = p[p[:, 0] != p[:, 1]]
+    d = np.concatenate([p, p[:, ::-1]])
+    key = np.unique(d[:, 0] * (1 << 32) + d[:, 1])
+    src, dst = key >> 32, key & 0xFFFFFFFF
+    off = np.zeros(n + 1, dtype=np.uint64)
+    np.add.at(off, src + 1, 1)
+    return np.cumsum(off).astype(np.uint64), dst.astype(np.uint32)
+
+
+def test_rmat_pairs_make_the_rmat_graph():
+    """smg_gen_rmat_pairs are smg_gen_rmat's draws: symmetrised and
+    de-duplicated they give its CSR; smg_gen_labels gives its labels."""
+    import numpy as np
+    from clustersm_gb300.native import HostGraph
+    g = HostGraph.rmat(12, 8, 6, seed=5)
+    pairs = HostGraph.rmat_pairs(12, 8, 5)
+    assert pairs.shape == ((1 << 12) * 8 // 2, 2)
+    off, adj = _csr_from_pairs(g.n, pairs)
+    assert np.array_equal(off, g.offsets()) and np.array_equal(adj, g.neighbors())
+    assert np.array_equal(HostGraph.labels_for(g.n, 6, 5), g.labels())
