@@ -197,18 +197,27 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
                 srv.step()
         srv.drain()
         ss = srv.stats()
-        lat, ok, first, last = [], 0, None, None
+        lat, wait, run, ok, first, last = [], [], [], 0, None, None
         for tk, j in tickets:
             r = srv.poll(tk)
             lat.append((r.finish_s - r.submit_s) * 1e3)
+            wait.append((r.start_s - r.submit_s) * 1e3)
+            run.append((r.finish_s - r.start_s) * 1e3)
             ok += int(r.status == 0 and (want[j] is None or int(r.count) == int(want[j])))
             first = r.submit_s if first is None else min(first, r.submit_s)
             last = r.finish_s if last is None else max(last, r.finish_s)
         srv.close()
         lat.sort()
+        wait.sort()
+        run.sort()
         out.append({"offered_qps": rate, "requests": n, "p50_ms": lat[n // 2], "p99_ms": lat[(99 * (n - 1)) // 100],
-                    "sustained_qps": n / (last - first), "counts_ok": ok, "slices": ss.slices, "bells": ss.bells,
-                    "retired_in_slice": ss.retired_in_slice, "slice_s": ss.slice_s, "between_s": ss.between_s})
+                    "sustained_qps": n / (last - first), "counts_ok": ok,
+                    # submit -> admission, and admission -> result
+                    "wait_p50_ms": wait[n // 2], "wait_p99_ms": wait[(99 * (n - 1)) // 100],
+                    "run_p50_ms": run[n // 2], "run_p99_ms": run[(99 * (n - 1)) // 100],
+                    "slices": ss.slices, "bells": ss.bells,
+                    "retired_in_slice": ss.retired_in_slice, "carried_tasks": ss.carried_tasks,
+                    "slice_s": ss.slice_s, "between_s": ss.between_s})
     return out
 
 
@@ -535,7 +544,19 @@ def main():
 
     serve = None
     if not args.no_serve and world == 1:
-        serve = serving(ctx, dev, plans, want, [float(r) for r in args.serve_rates.split(",") if r])
+        rates = [float(r) for r in args.serve_rates.split(",") if r]
+        swl = load("rmat24")
+        if not args.shape and not args.subset and (ROOT / swl.queries_file).exists():
+            # the serving configuration: R-MAT 2^24 resident, its own requests
+            sq, swant, _ = swl.queries()
+            sdev = DeviceGraph.build(ctx, 1 << swl.scale, native.HostGraph.rmat_pairs(swl.scale, swl.avg_degree,
+                                                                                      swl.seed),
+                                     native.HostGraph.labels_for(1 << swl.scale, swl.labels, swl.seed))
+            serve = {"workload": swl.name, "description": swl.description,
+                     "rates": serving(ctx, sdev, [Plan(q) for q in sq], swant, rates)}
+            sdev.free()
+        else:
+            serve = {"workload": wl.name, "rates": serving(ctx, dev, plans, want, rates)}
 
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)

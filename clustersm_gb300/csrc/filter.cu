@@ -659,6 +659,16 @@ smg_status FilterDev::upload(const FilterBatch &fb, cudaStream_t s) {
   return SMG_OK;
 }
 
+smg_status FilterDev::reserve(size_t bytes) {
+  if (bytes <= cap) return SMG_OK;
+  if (buf) cudaFree(buf);
+  buf = nullptr;
+  cap = 0;
+  SMG_CUDA(cudaMalloc(&buf, bytes));
+  cap = bytes;
+  return SMG_OK;
+}
+
 FilterDev::~FilterDev() {
   if (buf) cudaFree(buf);
 }

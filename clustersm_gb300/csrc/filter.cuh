@@ -48,6 +48,9 @@ struct FilterDev {
   uint32_t *aux = nullptr;
   std::vector<uint32_t> phase_first, phase_count;
   smg_status upload(const FilterBatch &fb, cudaStream_t s);
+  // Grows the device buffer ahead of time, so that an upload of at most
+  // `bytes` allocates nothing (a cudaFree would wait for every running kernel).
+  smg_status reserve(size_t bytes);
   FilterDev() = default;
   FilterDev(const FilterDev &) = delete;
   FilterDev &operator=(const FilterDev &) = delete;

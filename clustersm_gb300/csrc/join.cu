@@ -78,7 +78,7 @@ __device__ int wait_ticket(const JoinLaunch &p, unsigned long long ticket, uint6
       return 1;
     }
     if ((polls++ & 15) == 0) {
-      if (vload(qs->pending) == 0) return 0;
+      if (vload(qs->pending) == 0 && !(p.hold && *p.hold)) return 0;
       if (*reinterpret_cast<volatile int *>(&qs->abort)) return 0;
       if (*reinterpret_cast<volatile int *>(&qs->closing)) return 0;
       const uint64_t pr = vload(qs->progress), t = now_ns();
@@ -89,9 +89,16 @@ __device__ int wait_ticket(const JoinLaunch &p, unsigned long long ticket, uint6
         set_error(qs, JOIN_ERR_IDLE_TIMEOUT);
         return -1;
       }
-      if (t - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns) > p.time_limit_ns) {
+      const uint64_t el = t - *reinterpret_cast<volatile unsigned long long *>(&qs->start_ns);
+      if (el > p.time_limit_ns) {
         set_error(qs, JOIN_ERR_DEADLINE);
         return -1;
+      }
+      // a time slice also ends for a waiting warp (under a hold, every warp
+      // may be waiting when the slice time runs out or the bell rings)
+      if (p.slice_ns && (el > p.slice_ns || (el > p.slice_min_ns && p.bell && *p.bell))) {
+        atomicExch(&qs->closing, 1);
+        return 0;
       }
     }
     __nanosleep(ns);
@@ -105,7 +112,9 @@ __device__ int wait_ticket(const JoinLaunch &p, unsigned long long ticket, uint6
 __global__ void __launch_bounds__(256) k_seed(JoinLaunch p) {
   __shared__ unsigned long long s_first;
   __shared__ uint32_t s_nt, s_chunk, s_nr;
-  if (blockIdx.y == 0 && threadIdx.x == 0) p.qs->start_ns = now_ns();
+  // a whole batch starts its clock here; seeds of admitted requests (a seed
+  // list) join a slice whose clock k_slice_begin set
+  if (!p.seed_list && blockIdx.y == 0 && threadIdx.x == 0) p.qs->start_ns = now_ns();
   const uint32_t nseed = p.seed_list ? p.seed_n : p.nq;
   const uint32_t tw = 4 + p.kmax;
   for (uint32_t si = blockIdx.y; si < nseed; si += gridDim.y) {
@@ -126,6 +135,14 @@ __global__ void __launch_bounds__(256) k_seed(JoinLaunch p) {
           atomicAdd(&p.qs->pending.v, static_cast<unsigned long long>(nt));
           atomicAdd(p.queries[q].pending, static_cast<unsigned long long>(nt));
         }
+      }
+      // a served query without root candidates never runs a task: its count
+      // (zero) is final now
+      if (nr == 0 && p.queries[q].done_gen) {
+        const JoinQuery &Q = p.queries[q];
+        *reinterpret_cast<volatile unsigned long long *>(Q.done_count) = 0ull;
+        __threadfence_system();
+        *reinterpret_cast<volatile uint32_t *>(Q.done_gen) = Q.gen;
       }
       s_first = first;
       s_nt = nt;
@@ -1516,6 +1533,7 @@ smg_status launch_persistent(const JoinLaunch &jl_in, cudaStream_t s, int num_sm
     SMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   SMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpsPerBlock * 32, smem));
+  if (jl.max_blocks_per_sm) per_sm = std::min(per_sm, static_cast<int>(jl.max_blocks_per_sm));
   per_sm = std::max(1, per_sm);
   kern<<<num_sms * per_sm, kWarpsPerBlock * 32, smem, s>>>(jl);
   SMG_CUDA(cudaGetLastError());

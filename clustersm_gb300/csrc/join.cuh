@@ -83,6 +83,15 @@ struct JoinLaunch {
   unsigned int *next_count;  // tasks written to the next queue, zero on entry
   const uint32_t *seed_list; // seed only these query indices (null: 0 .. nq-1)
   uint32_t seed_n;
+  // Serving with admission into the running slice: while the host-mapped
+  // word *hold is non-zero, warps keep waiting for work when the queue
+  // drains instead of leaving (the host may still append root tasks), so no
+  // claimed ticket is ever abandoned; the host clears it once nothing more
+  // will be appended.  Null: leave when the queue drains.
+  const volatile uint32_t *hold;
+  // Join blocks per SM at most (0: as many as fit); the server leaves room
+  // for the filter kernels of requests admitted into a running slice.
+  uint32_t max_blocks_per_sm;
 };
 
 // The resident graph's arrays in a launch record (every launch site uses

@@ -9,14 +9,24 @@
 //     state (candidate masks, cluster bitmap, candidate lists) fits the memory
 //     budget; admission order is arrival order;
 //   * newly admitted queries are filtered together and their root tasks are
-//     appended to the live queue;
+//     appended to the live queue.  By default this happens while a slice
+//     runs: on a second stream, the filter kernels take the SM room the join
+//     leaves (3 of its 4 blocks per SM), and the seeds join the running
+//     queue, whose waiting warps pick them up.  A host-mapped hold word keeps
+//     the join's warps waiting, rather than leaving, while the queue is
+//     empty but more work may be appended; the host clears it when nothing is
+//     running or waiting.  Slots and memory a request frees during a slice
+//     are reused only after the slice, so that no SM can hold a stale cached
+//     line of the previous tenant's records or bitmaps.  SMG_SERVE_LIVE=0
+//     admits only between slices;
 //   * the join runs in slices.  A slice ends when its work is done, after
-//     SMG_SLICE_MS (default 250 ms), or, once SMG_SLICE_MIN_MS (default 2 ms)
-//     have passed, when the host rings a doorbell in host-mapped memory
-//     because requests are waiting and slots are free.  At the end of a slice
-//     every warp writes the unfinished part of its depth-first stack into the
-//     next slice's queue, so requests that arrived meanwhile start in the next
-//     slice alongside the ones still running;
+//     SMG_SLICE_MS (default 1,000 ms; 250 ms with SMG_SERVE_LIVE=0), or, once
+//     SMG_SLICE_MIN_MS (default 2 ms) have passed, when the host rings a
+//     doorbell in host-mapped memory: without live admission because
+//     requests are waiting and slots are free, with it when the queue has
+//     used half its slots.  At the end of a slice every warp writes the
+//     unfinished part of its depth-first stack into the next slice's queue,
+//     and the untaken tasks follow;
 //   * a query is finished when its count of queued and running tasks reaches
 //     zero.  The warp that brings it there writes the final count to a
 //     host-mapped completion record, so the host retires the request (and
@@ -29,6 +39,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <string>
 #include <memory>
 #include <thread>
 #include <unordered_set>
@@ -51,6 +62,7 @@ struct Request {
 
 struct Slot {
   bool used = false;
+  bool held = false;         // retired during a live slice; free once it ends
   uint64_t ticket = 0;
   uint32_t gen = 0;          // admission number, echoed by the completion record
   const smg::Plan *plan = nullptr;
@@ -118,6 +130,7 @@ struct smg_server {
   std::deque<Request> waiting;
   std::vector<Slot> slots;
   uint32_t free_slots = 0;
+  uint32_t running = 0;      // admitted requests not yet retired
   std::map<uint64_t, smg_request_result> done;  // finished, not yet collected by smg_server_poll
   std::unordered_set<uint64_t> outstanding;     // submitted, not yet finished
   Pool pool;
@@ -135,6 +148,17 @@ struct smg_server {
   unsigned int *walk_count = nullptr;
   uint4 *walk_items = nullptr;
   uint32_t cap = 0, cur = 0;
+  // admission into the running slice (SMG_SERVE_LIVE, default on)
+  bool live = true;
+  cudaStream_t s2 = nullptr;        // its stream
+  cudaEvent_t ev_admit = nullptr;   // the last admission's work on s2
+  bool admitting = false;           // that work may still be running
+  uint32_t join_blocks = 3;         // join blocks per SM while admitting live
+  void *stage = nullptr;            // page-locked staging of admissions
+  uint32_t *h_hold = nullptr, *d_hold = nullptr;
+  unsigned long long *h_tail = nullptr;  // the live queue's tail, read after each admission
+  std::vector<std::pair<size_t, size_t>> freed_mem;  // released at the end of the slice
+  std::vector<uint32_t> freed_slots;
   uint32_t kmax = smg::kMaxK;  // task width: the largest query accepted
   uint32_t admit_batch = 1;    // free slots that ring the doorbell (SMG_ADMIT_BATCH; default an eighth)
   uint64_t slice_ns = 0, slice_min_ns = 0;
@@ -164,9 +188,11 @@ struct smg_server {
                     static_cast<void *>(walk_items), static_cast<void *>(xbuf)})
       if (p) cudaFree(p);
     for (void *p : {static_cast<void *>(h_cnt), static_cast<void *>(h_qs), static_cast<void *>(h_bell),
-                    static_cast<void *>(h_done)})
+                    static_cast<void *>(h_done), stage, static_cast<void *>(h_hold), static_cast<void *>(h_tail)})
       if (p) cudaFreeHost(p);
     if (ev) cudaEventDestroy(ev);
+    if (ev_admit) cudaEventDestroy(ev_admit);
+    if (s2) cudaStreamDestroy(s2);
   }
 };
 
@@ -207,10 +233,14 @@ smg::JoinLaunch join_launch(smg_server *s) {
   jl.next_count = s->next_count;
   jl.xbuf = s->xbuf;
   jl.xcap = smg::hoist_global_cap();
+  if (s->live) {
+    jl.hold = s->d_hold;
+    jl.max_blocks_per_sm = s->join_blocks;
+  }
   return jl;
 }
 
-bool any_active(const smg_server *s) { return s->free_slots < s->slots.size(); }
+bool any_active(const smg_server *s) { return s->running > 0; }
 
 // Empty queue: head = tail = pending = 0, every ready flag clear.
 smg_status reset_queue(smg_server *s) {
@@ -232,15 +262,37 @@ void retire(smg_server *s, Slot &sl, smg_status status, uint64_t count) {
   r.finish_s = now_s();
   s->done[sl.ticket] = r;
   s->outstanding.erase(sl.ticket);
+  --s->running;
+  if (s->live && s->inflight) {
+    // the running join may have this slot's records and bitmaps cached:
+    // they are reused only after the slice
+    s->freed_mem.emplace_back(sl.off, sl.size);
+    s->freed_slots.push_back(static_cast<uint32_t>(&sl - s->slots.data()));
+    sl = Slot();
+    sl.used = true;
+    sl.held = true;
+    return;
+  }
   s->pool.release(sl.off, sl.size);
   sl = Slot();
   ++s->free_slots;
 }
 
+// Slots and memory retired during the slice just ended become free.
+void release_freed(smg_server *s) {
+  for (const auto &m : s->freed_mem) s->pool.release(m.first, m.second);
+  for (uint32_t i : s->freed_slots) {
+    s->slots[i] = Slot();
+    ++s->free_slots;
+  }
+  s->freed_mem.clear();
+  s->freed_slots.clear();
+}
+
 // Retires the requests whose completion records the join has published.
 void poll_done(smg_server *s) {
   for (Slot &sl : s->slots) {
-    if (!sl.used) continue;
+    if (!sl.used || sl.held) continue;
     const uint32_t i = static_cast<uint32_t>(&sl - s->slots.data());
     if (__atomic_load_n(&s->h_done[i].gen, __ATOMIC_ACQUIRE) != sl.gen) continue;
     retire(s, sl, SMG_OK, __atomic_load_n(&s->h_done[i].count, __ATOMIC_RELAXED));
@@ -279,9 +331,8 @@ smg_status end_slice(smg_server *s) {
 // Admit waiting requests (arrival order) while slots and memory allow; filter
 // them together and append their root tasks to the live queue.  Only
 // enqueues: the caller synchronises once for admission and read-back.
-smg_status admit(smg_server *s) {
+smg_status admit(smg_server *s, cudaStream_t st) {
   const smg::DevGraph &g = s->graph->g;
-  cudaStream_t st = s->ctx->stream;
   std::vector<uint32_t> fresh;
   std::vector<smg::QueryFootprint> fps;
   const double t = now_s();
@@ -302,6 +353,7 @@ smg_status admit(smg_server *s) {
     sl.submit_s = r.submit_s;
     sl.start_s = t;
     --s->free_slots;
+    ++s->running;
     ++s->stats.admitted;
     s->waiting.pop_front();
     fresh.push_back(idx);
@@ -309,7 +361,7 @@ smg_status admit(smg_server *s) {
   }
   if (fresh.empty()) return SMG_OK;
   const uint32_t n = static_cast<uint32_t>(fresh.size());
-  smg::FilterQuery *hf = static_cast<smg::FilterQuery *>(s->ctx->pinned);
+  smg::FilterQuery *hf = static_cast<smg::FilterQuery *>(s->stage);
   smg::JoinQuery *hj = reinterpret_cast<smg::JoinQuery *>(hf + n);
   uint32_t *hseed = reinterpret_cast<uint32_t *>(hj + n);
   smg::FilterBatch fb;
@@ -364,7 +416,8 @@ smg_status admit(smg_server *s) {
 // and fail every active request if the join reported an error.
 smg_status settle(smg_server *s) {
   cudaStream_t st = s->ctx->stream;
-  smg_status rc = admit(s);
+  release_freed(s);
+  smg_status rc = admit(s, st);
   if (rc) return rc;
   SMG_CUDA(cudaMemcpyAsync(s->h_cnt, s->d_cnt, s->slots.size() * sizeof(smg::QCounters), cudaMemcpyDeviceToHost,
                            st));
@@ -375,12 +428,12 @@ smg_status settle(smg_server *s) {
   if (s->h_qs->error) {
     const smg_status why = s->h_qs->error == smg::JOIN_ERR_QUEUE_FULL ? SMG_ERR_LIMIT : SMG_ERR_TIMEOUT;
     for (Slot &sl : s->slots)
-      if (sl.used) retire(s, sl, why, 0);
+      if (sl.used && !sl.held) retire(s, sl, why, 0);
     return reset_queue(s);
   }
   for (size_t i = 0; i < s->slots.size(); ++i) {
     Slot &sl = s->slots[i];
-    if (sl.used && s->h_cnt[i].pending == 0) retire(s, sl, SMG_OK, s->h_cnt[i].count);
+    if (sl.used && !sl.held && s->h_cnt[i].pending == 0) retire(s, sl, SMG_OK, s->h_cnt[i].count);
   }
   if (!any_active(s)) return reset_queue(s);
   return SMG_OK;
@@ -390,6 +443,7 @@ smg_status launch_slice(smg_server *s) {
   cudaStream_t st = s->ctx->stream;
   __atomic_store_n(s->h_bell, 0u, __ATOMIC_RELEASE);
   s->bell_rung = false;
+  if (s->live) __atomic_store_n(s->h_hold, 1u, __ATOMIC_RELEASE);  // live admission may append work
   smg_status rc = smg::launch_slice_begin(s->qs, st);
   if (rc) return rc;
   rc = smg::launch_join_only(join_launch(s), st, s->ctx->num_sms);
@@ -401,18 +455,60 @@ smg_status launch_slice(smg_server *s) {
   return SMG_OK;
 }
 
+// While a slice runs with live admission: finish the last admission (and
+// read the queue's tail it left), admit waiting requests into the running
+// queue on the second stream, ring the doorbell when the queue has used half
+// its slots, and clear the hold once nothing is running, waiting or being
+// admitted (then the join leaves when its queue drains, and later requests
+// start the next slice).
+smg_status live_step(smg_server *s) {
+  if (s->admitting) {
+    const cudaError_t e = cudaEventQuery(s->ev_admit);
+    if (e == cudaErrorNotReady) return SMG_OK;
+    if (e != cudaSuccess) return smg::cuda_fail(e, "server admission");
+    s->admitting = false;
+    if (*s->h_tail > s->cap / 2 && !s->bell_rung) {
+      __atomic_store_n(s->h_bell, 1u, __ATOMIC_RELEASE);
+      s->bell_rung = true;
+      ++s->stats.bells;
+    }
+  }
+  const bool open = __atomic_load_n(s->h_hold, __ATOMIC_ACQUIRE) != 0;
+  if (open && !s->bell_rung && !s->waiting.empty() && s->free_slots) {
+    const uint64_t before = s->stats.admitted;
+    smg_status rc = admit(s, s->s2);
+    if (rc) return rc;
+    if (s->stats.admitted != before) {
+      s->stats.admitted_live += s->stats.admitted - before;
+      SMG_CUDA(cudaMemcpyAsync(s->h_tail, &s->qs->tail.v, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->s2));
+      SMG_CUDA(cudaEventRecord(s->ev_admit, s->s2));
+      s->admitting = true;
+    }
+  }
+  if (open && !s->admitting && s->waiting.empty() && s->running == 0)
+    __atomic_store_n(s->h_hold, 0u, __ATOMIC_RELEASE);
+  return SMG_OK;
+}
+
 smg_status step(smg_server *s) {
   SMG_CUDA(cudaSetDevice(s->ctx->device));
   if (s->inflight) {
     const cudaError_t e = cudaEventQuery(s->ev);
     if (e == cudaErrorNotReady) {
       poll_done(s);
+      if (s->live) return live_step(s);
       maybe_ring(s);
       return SMG_OK;
     }
     if (e != cudaSuccess) return smg::cuda_fail(e, "server slice");
     s->inflight = false;
     s->stats.slice_s += now_s() - s->slice_start_s;
+    if (s->admitting) {
+      // its seeds may have landed after the join left: the compaction moves them
+      SMG_CUDA(cudaStreamWaitEvent(s->ctx->stream, s->ev_admit, 0));
+      s->admitting = false;
+    }
+    poll_done(s);  // completions written during the slice, before their slots are freed
     smg_status rc = end_slice(s);
     if (rc) return rc;
   } else if (s->waiting.empty() && !any_active(s)) {
@@ -456,7 +552,13 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   size_t free_b = 0, total_b = 0;
   SMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
   if (!s->cfg.memory_budget_bytes) s->cfg.memory_budget_bytes = std::min<size_t>(64ull << 30, free_b / 3);
-  s->slice_ns = static_cast<uint64_t>(env_ms("SMG_SLICE_MS", 250.0) * 1e6);
+  {
+    const char *lv = std::getenv("SMG_SERVE_LIVE");
+    s->live = !(lv && std::string(lv) == "0");
+    const char *jb = std::getenv("SMG_SERVE_JOIN_BLOCKS");
+    if (jb) s->join_blocks = static_cast<uint32_t>(std::max(1, std::atoi(jb)));
+  }
+  s->slice_ns = static_cast<uint64_t>(env_ms("SMG_SLICE_MS", s->live ? 1000.0 : 250.0) * 1e6);
   s->slice_min_ns = std::min(s->slice_ns, static_cast<uint64_t>(env_ms("SMG_SLICE_MIN_MS", 2.0) * 1e6));
   s->cap = 2u << 20;
   s->admit_batch = std::max<uint32_t>(1, static_cast<uint32_t>(env_ms("SMG_ADMIT_BATCH", s->cfg.max_inflight / 8.0)));
@@ -481,6 +583,20 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   SMG_CUDA(cudaHostAlloc(&s->h_qs, sizeof(smg::QueueState), cudaHostAllocDefault));
   SMG_CUDA(cudaHostAlloc(&s->h_bell, sizeof(uint32_t), cudaHostAllocMapped));
   SMG_CUDA(cudaHostAlloc(&s->h_done, m * sizeof(Done), cudaHostAllocMapped));
+  SMG_CUDA(cudaHostAlloc(&s->stage, m * per_rec + 4096, cudaHostAllocDefault));
+  SMG_CUDA(cudaHostAlloc(&s->h_hold, sizeof(uint32_t), cudaHostAllocMapped));
+  SMG_CUDA(cudaHostAlloc(&s->h_tail, sizeof(unsigned long long), cudaHostAllocDefault));
+  SMG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_hold), s->h_hold, 0));
+  *s->h_hold = 0;
+  *s->h_tail = 0;
+  SMG_CUDA(cudaStreamCreateWithFlags(&s->s2, cudaStreamNonBlocking));
+  SMG_CUDA(cudaEventCreateWithFlags(&s->ev_admit, cudaEventDisableTiming));
+  // the filter's step tables of up to max_inflight admissions at once, sized
+  // now: growing them later would free memory under a running join
+  {
+    smg_status rc0 = s->fdev.reserve(static_cast<size_t>(m) * 64 * 1024 + (1u << 20));
+    if (rc0) return rc0;
+  }
   SMG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_bell), s->h_bell, 0));
   SMG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_done), s->h_done, 0));
   *s->h_bell = 0;

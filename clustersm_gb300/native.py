@@ -101,7 +101,7 @@ class ServerConfig(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("slices", C.c_uint64), ("bells", C.c_uint64), ("admitted", C.c_uint64),
                 ("retired_in_slice", C.c_uint64), ("carried_tasks", C.c_uint64), ("slice_s", C.c_double),
-                ("between_s", C.c_double)]
+                ("between_s", C.c_double), ("admitted_live", C.c_uint64)]
 
 
 class RequestResult(C.Structure):

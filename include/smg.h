@@ -403,6 +403,7 @@ typedef struct smg_server_stats {
   double slice_s;           /* time from a slice's launch to its end seen    */
   double between_s;         /* time between slices (compaction, admission,
                                read-back) with requests active or waiting    */
+  uint64_t admitted_live;   /* requests admitted into a running slice       */
 } smg_server_stats;
 smg_status smg_server_get_stats(const smg_server *s, smg_server_stats *out);
 void smg_server_destroy(smg_server *s);

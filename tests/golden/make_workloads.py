@@ -56,6 +56,9 @@ SPECS = {
     # feasibility table): k = 4..7 in turn, each with every shape in turn; at
     # most 10^9 embeddings, so that the CPU oracle can verify every count
     "rmat22_k4to7": (64, [4, 5, 6, 7], ["tree", "sparse", "dense"], 10**9),
+    # the serving graph (R-MAT 2^24): requests of the sizes that stay exact
+    # within a serving budget (at most 10^7 embeddings each)
+    "rmat24": (256, [4, 5], ["tree", "sparse", "dense"], 10**7),
 }
 # join steps a screened query may take (bounds the draws whose count is out of reach)
 WORK_LIMIT = {"rmat22_k4to7": 1 << 30}
@@ -91,7 +94,7 @@ def phases(name):
     5-vertex sparse queries exceed 10^7 embeddings in every one of 64 draws, so
     slots still empty after the first phase fall back to 4-vertex queries of
     their shape, and then to 4-vertex dense ones."""
-    if name == "rmat22":
+    if name in ("rmat22", "rmat24"):
         return [(64, None, None), (256, 4, None), (64, 4, "dense")]
     if name == "rmat22_k4to7":
         # trees of 6 or more vertices and most sparse ones are out of reach:

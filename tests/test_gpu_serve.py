@@ -47,8 +47,12 @@ def rmat22(ctx):
     return DeviceGraph(ctx, wl.graph()), [Plan(q) for q in qs[:96]], want[:96]
 
 
-def test_arrivals_while_running(ctx, rmat22):
+@pytest.mark.parametrize("live", ["1", "0"])
+def test_arrivals_while_running(ctx, rmat22, monkeypatch, live):
+    """Requests submitted while others run: admitted into the running slice
+    (default), or between slices (SMG_SERVE_LIVE=0); counts exact either way."""
     dev, plans, want = rmat22
+    monkeypatch.setenv("SMG_SERVE_LIVE", live)
     srv = Server(ctx, dev, max_inflight=32)
     tickets = []
     for i, p in enumerate(plans):
@@ -57,22 +61,27 @@ def test_arrivals_while_running(ctx, rmat22):
             srv.step()  # non-blocking: admits, launches or retires
     srv.drain()
     results = [srv.poll(tk) for tk in tickets]
+    ss = srv.stats()
     srv.close()
     for r, w in zip(results, want):
         assert r.status == 0 and r.count == w
+    if live == "0":
+        assert ss.admitted_live == 0
     for p, w in list(zip(plans, want))[:8]:
         res, _ = native.match(ctx, dev, p)
         assert res.count == w
 
 
-@pytest.mark.parametrize("slice_ms,min_ms", [("0.3", "0.1"), ("250", "0.2")])
-def test_preempted_slices_keep_counts(ctx, rmat22, monkeypatch, slice_ms, min_ms):
+@pytest.mark.parametrize("slice_ms,min_ms,live", [("0.3", "0.1", "1"), ("0.3", "0.1", "0"), ("250", "0.2", "0"),
+                                                  ("250", "0.2", "1")])
+def test_preempted_slices_keep_counts(ctx, rmat22, monkeypatch, slice_ms, min_ms, live):
     """Sub-millisecond slices (every warp's stack is handed over to the next
-    queue hundreds of times) and doorbell-driven closings (arrivals while
-    slots are free) leave every count exact."""
+    queue hundreds of times), doorbell-driven closings (arrivals while slots
+    are free) and admission into running slices leave every count exact."""
     dev, plans, want = rmat22
     monkeypatch.setenv("SMG_SLICE_MS", slice_ms)
     monkeypatch.setenv("SMG_SLICE_MIN_MS", min_ms)
+    monkeypatch.setenv("SMG_SERVE_LIVE", live)
     srv = Server(ctx, dev, max_inflight=24)
     tickets = []
     for i, p in enumerate(plans):
@@ -86,6 +95,8 @@ def test_preempted_slices_keep_counts(ctx, rmat22, monkeypatch, slice_ms, min_ms
     ss = srv.stats()
     srv.close()
     assert ss.admitted == len(plans) and ss.slices >= 1
+    if live == "0":
+        assert ss.admitted_live == 0
     assert [r.status for r in results] == [0] * len(plans)
     assert [int(r.count) for r in results] == [int(w) for w in want]
 
