@@ -82,8 +82,8 @@ def parse():
     ap.add_argument("--c4-scale", type=int, default=25)
     ap.add_argument("--no-reference-binary", action="store_true",
                     help="skip the leg that runs the reference's own GPU filter and join")
-    ap.add_argument("--tune", action="store_true",
-                    help="run the library's per-shape-class autotuner on the workload before timing (untimed)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the library's per-shape-class autotuner (run on the workload before timing, untimed)")
     return ap.parse_args()
 
 
@@ -462,10 +462,13 @@ def main():
         torch.cuda.synchronize()
 
     tuning = None
-    if args.tune:  # setup, outside the timed region
-        tuning = [{"shape_class": e.shape_class, "root_chunk": e.root_chunk, "donate_min": e.donate_min,
-                   "best_ms": e.best_ms, "default_ms": e.default_ms}
-                  for e in native.autotune(ctx, dev, plans) if e.samples]
+    if not args.no_tune:  # setup, outside the timed region
+        t_tune = time.perf_counter()
+        tuning = {"classes": [{"shape_class": e.shape_class, "root_chunk": e.root_chunk, "donate_min": e.donate_min,
+                               "split_len": e.split_len, "hoist_cap": e.hoist_cap, "samples": e.samples,
+                               "best_ms": e.best_ms, "default_ms": e.default_ms}
+                              for e in native.autotune(ctx, dev, plans) if e.samples]}
+        tuning["seconds"] = time.perf_counter() - t_tune
     # correctness against the committed counts before timing
     counts, _ = native.match_batch(ctx, dev, plans)
     want = [expected[i] for i in mine]

@@ -740,10 +740,7 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
     if (st) return st;
     if (o.tuning && !o.root_chunk) {
       const TuneSetting &t = o.tuning[plan_class(P)];
-      if (t.valid) {
-        hj[i].root_chunk = t.root_chunk;
-        hj[i].donate_min = t.donate_min;
-      }
+      if (t.valid) apply_tuning(t, hj[i]);
     }
     st = append_filter_steps(P, i, fb);
     if (st) return st;
@@ -1109,6 +1106,8 @@ smg_status smg_set_tuning(smg_ctx *c, const smg_tune_entry *e, uint32_t n) {
     TuneSetting &t = c->tuning[e[i].shape_class];
     t.root_chunk = e[i].root_chunk;
     t.donate_min = e[i].donate_min;
+    t.split_len = e[i].split_len;
+    t.hoist_cap = e[i].hoist_cap;
     t.valid = e[i].samples > 0;
   }
   ++c->run_gen;  // the settings are staged into the query records: a captured batch is stale
@@ -1120,47 +1119,86 @@ smg_status smg_autotune(smg_ctx *c, const smg_graph *G, const smg_plan *const *p
   if (!c || !G || (n && !plans)) return fail(SMG_ERR_INVALID, "null argument");
   static const uint32_t kChunks[] = {1, 8, 64};
   static const uint32_t kDonate[] = {2, 33, 129};
+  static const uint32_t kSplits[] = {8192, 2048, 32768};
+  static const uint32_t kHoists[] = {4096, 1024, 256};
   std::vector<std::vector<const Plan *>> by_class(SMG_TUNE_CLASSES);
   for (uint32_t i = 0; i < n; ++i)
     if (plans[i] && by_class[plan_class(plans[i]->p)].size() < 32) by_class[plan_class(plans[i]->p)].push_back(&plans[i]->p);
   for (uint32_t cls = 0; cls < SMG_TUNE_CLASSES; ++cls) {
-    smg_tune_entry e{cls, 0, 0, 0, 0.f, 0.f};
+    smg_tune_entry e{};
+    e.shape_class = cls;
     const auto &sample = by_class[cls];
     if (!sample.empty()) {
-      float best = -1.f;
-      for (uint32_t rc : kChunks)
-        for (uint32_t dm : kDonate) {
-          TuneSetting t[SMG_TUNE_CLASSES];
-          t[cls].root_chunk = rc;
-          t[cls].donate_min = dm;
-          t[cls].valid = true;
-          RunOpts o;
-          o.tuning = t;
-          o.profile = true;
-          std::vector<QueryOut> q(sample.size());
-          float ms = 0.f;
-          for (int rep = 0; rep < 2; ++rep) {  // first run warms caches
-            RunStats st;
-            smg_status s = run_queries(c, G->g, sample.data(), static_cast<uint32_t>(sample.size()), o, q.data(), &st);
-            if (s) return s;
-            ms = st.filter_ms + st.join_ms;
-          }
-          if (rc == kChunks[0] && dm == kDonate[0]) e.default_ms = ms;
-          if (best < 0 || ms < best) {
-            best = ms;
-            e.root_chunk = rc;
-            e.donate_min = dm;
+      // device time of the sample under setting `cand` (second of two runs)
+      auto time_of = [&](const TuneSetting &cand, float &ms) -> smg_status {
+        TuneSetting t[SMG_TUNE_CLASSES];
+        t[cls] = cand;
+        t[cls].valid = true;
+        RunOpts o;
+        o.tuning = t;
+        o.profile = true;
+        std::vector<QueryOut> q(sample.size());
+        for (int rep = 0; rep < 2; ++rep) {  // the first run warms the caches
+          RunStats st;
+          smg_status s = run_queries(c, G->g, sample.data(), static_cast<uint32_t>(sample.size()), o, q.data(), &st);
+          if (s) return s;
+          ms = st.filter_ms + st.join_ms;
+        }
+        return SMG_OK;
+      };
+      TuneSetting best;
+      best.root_chunk = kChunks[0];
+      best.donate_min = kDonate[0];
+      best.split_len = kSplits[0];
+      best.hoist_cap = kHoists[0];
+      float best_ms = -1.f;
+      // one knob group at a time, each from the best of the groups before
+      for (int group = 0; group < 3; ++group) {
+        std::vector<TuneSetting> cands;
+        if (group == 0) {
+          for (uint32_t rc : kChunks)
+            for (uint32_t dm : kDonate) {
+              TuneSetting t = best;
+              t.root_chunk = rc;
+              t.donate_min = dm;
+              cands.push_back(t);
+            }
+        } else {
+          for (uint32_t v : group == 1 ? kSplits : kHoists) {
+            TuneSetting t = best;
+            (group == 1 ? t.split_len : t.hoist_cap) = v;
+            cands.push_back(t);
           }
         }
+        TuneSetting group_best = best;
+        float group_ms = best_ms;
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+          if (group > 0 && ci == 0) continue;  // the incumbent, timed already
+          float ms = 0.f;
+          smg_status s = time_of(cands[ci], ms);
+          if (s) return s;
+          if (group == 0 && ci == 0) e.default_ms = ms;
+          if (group_ms < 0 || ms < group_ms) {
+            group_ms = ms;
+            group_best = cands[ci];
+          }
+        }
+        best = group_best;
+        best_ms = group_ms;
+      }
+      e.root_chunk = best.root_chunk;
+      e.donate_min = best.donate_min;
+      e.split_len = best.split_len;
+      e.hoist_cap = best.hoist_cap;
       e.samples = static_cast<uint32_t>(sample.size());
-      e.best_ms = best;
+      e.best_ms = best_ms;
       TuneSetting &t = c->tuning[cls];
-      t.root_chunk = e.root_chunk;
-      t.donate_min = e.donate_min;
+      t = best;
       t.valid = true;
     }
     if (out) out[cls] = e;
   }
+  ++c->run_gen;
   return SMG_OK;
 }
 

@@ -48,9 +48,16 @@ uint64_t time_limit_ns();
 
 // Options of one run (plain path: one query; batched: many).
 struct TuneSetting {
-  uint32_t root_chunk = 0, donate_min = 0;
+  uint32_t root_chunk = 0, donate_min = 0, split_len = 0, hoist_cap = 0;
   bool valid = false;
 };
+// The tuned knobs of a shape class into a query's join record.
+inline void apply_tuning(const TuneSetting &t, JoinQuery &j) {
+  j.root_chunk = t.root_chunk;
+  j.donate_min = t.donate_min;
+  j.split_len = t.split_len;
+  j.hoist_cap = t.hoist_cap;
+}
 uint32_t plan_class(const Plan &P);
 
 struct RunOpts {

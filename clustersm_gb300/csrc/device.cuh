@@ -186,6 +186,8 @@ struct JoinQuery {
   unsigned long long *pending;  // tasks of this query queued or running
   uint32_t root_chunk;        // root candidates per seeded task (0: from max_seed_tasks)
   uint32_t donate_min;        // shortest list worth splitting off (0: launch default)
+  uint32_t split_len;         // last-level lists are cut into slices this long (0: 8,192)
+  uint32_t hoist_cap;         // stored hoisted sets hold at most this many (0: the warp's buffer)
   // Completion notice (serving; null: none).  The warp that finishes the
   // query's last task writes the final count to done_count and then `gen` to
   // done_gen, both in host-mapped memory, so the host sees the result while

@@ -554,7 +554,8 @@ __device__ __forceinline__ uint32_t accept_multi(const WarpView &S, const JoinLa
   return live;
 }
 
-// A last-level list longer than kSplitLen is cut into slices of that length:
+// A last-level list longer than the query's split length (split_len, default
+// kSplitLen) is cut into slices of that length:
 // the first stays with this lane, the others become tasks (level P + 1, range
 // [lo, hi) of the list, prefix m[0..P-1] plus candidate v) when warps are
 // waiting for work or the list is very long.  Returns the length this lane
@@ -562,10 +563,11 @@ __device__ __forceinline__ uint32_t accept_multi(const WarpView &S, const JoinLa
 __device__ uint32_t split_last(const WarpView &S, const JoinLaunch &p, const JoinQuery &Q, uint32_t q, uint32_t P,
                                uint32_t v, uint32_t len) {
   QueueState *qs = p.qs;
+  const uint32_t sl = Q.split_len ? Q.split_len : kSplitLen;
   const unsigned long long h = vload(qs->head), t = vload(qs->tail);
-  if (!(h > t || len > 8 * kSplitLen)) return len;
+  if (!(h > t || len > 8 * sl)) return len;
   if (*reinterpret_cast<volatile int *>(&qs->closing)) return len;
-  const uint32_t slices = (len - 1) / kSplitLen;  // beyond the first
+  const uint32_t slices = (len - 1) / sl;  // beyond the first
   const unsigned long long first = atomicAdd(&qs->tail.v, static_cast<unsigned long long>(slices));
   if (first + slices > p.cap) {
     // no room: the slot numbers taken stay unpublished and are never waited
@@ -580,15 +582,15 @@ __device__ uint32_t split_last(const WarpView &S, const JoinLaunch &p, const Joi
     uint32_t *T = p.tasks + (first + i) * tw;
     T[0] = q;
     T[1] = P + 1;
-    T[2] = (i + 1) * kSplitLen;
-    T[3] = min(len, (i + 2) * kSplitLen);
+    T[2] = (i + 1) * sl;
+    T[3] = min(len, (i + 2) * sl);
     for (uint32_t j = 0; j < P; ++j) T[4 + j] = S.m[j];
     T[4 + P] = v;
   }
   __threadfence();
   for (uint32_t i = 0; i < slices; ++i) atomicExch(p.ready + first + i, 1u);
   atomicAdd(&qs->donations, static_cast<unsigned long long>(slices));
-  return kSplitLen;
+  return sl;
 }
 
 // Counts (and optionally emits) the last level over entries [lo, hi) of one
@@ -822,7 +824,7 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
       const uint32_t *lst =
           scan_list(p, S, Q.use_labels, L, piv == P ? v : S.m[piv], pb, piv == P ? vd : S.deg[piv], len);
       const bool from_l = lst != p.adj + pb;
-      if (len > kSplitLen) len = split_last(S, p, Q, q, P, v, len);
+      if (len > (Q.split_len ? Q.split_len : kSplitLen)) len = split_last(S, p, Q, q, P, v, len);
       S.sv[lane] = v;
       S.sbeg[lane] = vb;
       S.sdeg[lane] = vd;
@@ -1088,6 +1090,8 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     const JoinQuery &Q = p.queries[q];
     const uint32_t k = Q.k, P = k - 2;
     if (!SMG_DCHECK(L0 <= P + 1, 110, L0, k)) break;
+    // the query's cap on stored hoisted sets, within this warp's buffer
+    S.xcap = min(p.xbuf ? p.xcap : kHoistCap, Q.hoist_cap ? Q.hoist_cap : 0xFFFFFFFFu);
     int drop = 0;
     if (lane == 0) drop = (Q.count_limit || Q.work_limit) && *reinterpret_cast<volatile uint32_t *>(Q.over);
     drop = __shfl_sync(0xFFFFFFFFu, drop, 0);

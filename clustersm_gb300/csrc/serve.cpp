@@ -379,10 +379,7 @@ smg_status admit(smg_server *s, cudaStream_t st) {
     smg_status rc = smg::make_query_records(*sl.plan, g, b, 0, hf[i], hj[i]);
     if (rc) return rc;
     const smg::TuneSetting &tune = s->ctx->tuning[smg::plan_class(*sl.plan)];
-    if (tune.valid) {
-      hj[i].root_chunk = tune.root_chunk;
-      hj[i].donate_min = tune.donate_min;
-    }
+    if (tune.valid) smg::apply_tuning(tune, hj[i]);
     hj[i].done_count = &s->d_done[idx].count;
     hj[i].done_gen = &s->d_done[idx].gen;
     hj[i].gen = sl.gen;

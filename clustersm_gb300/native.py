@@ -61,7 +61,7 @@ class PlanView(C.Structure):
 
 
 class MatchOpts(C.Structure):
-    _fields_ = [("flags", C.c_uint32), ("bfs_depth", C.c_uint32), ("root_chunk", C.c_uint32),
+    _fields_ = [("flags", C.c_uint32), ("reserved0", C.c_uint32), ("root_chunk", C.c_uint32),
                 ("reserved", C.c_uint32), ("max_embeddings", C.c_uint64), ("embeddings", u32p),
                 ("max_count", C.c_uint64), ("max_work", C.c_uint64)]
 
@@ -85,7 +85,8 @@ class BatchStats(C.Structure):
 
 class TuneEntry(C.Structure):
     _fields_ = [("shape_class", C.c_uint32), ("root_chunk", C.c_uint32), ("donate_min", C.c_uint32),
-                ("samples", C.c_uint32), ("best_ms", C.c_float), ("default_ms", C.c_float)]
+                ("samples", C.c_uint32), ("best_ms", C.c_float), ("default_ms", C.c_float),
+                ("split_len", C.c_uint32), ("hoist_cap", C.c_uint32)]
 
 
 class GraphStats(C.Structure):
@@ -452,14 +453,13 @@ class DeviceGraph:
         self.free()
 
 
-def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=False, bfs_depth=0,
+def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=False,
           root_chunk=0, max_count=0, max_work=0):
     """Plain path.  Returns (MatchResult, embeddings array or None)."""
     opts = MatchOpts()
     opts.max_count = max_count
     opts.max_work = max_work
     opts.flags = (FLAG_EMIT if emit else 0) | (FLAG_PROFILE if profile else 0)
-    opts.bfs_depth = bfs_depth
     opts.root_chunk = root_chunk
     buf = None
     if emit:
@@ -473,7 +473,7 @@ def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=F
     return res, buf
 
 
-def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk=0, profile=False, max_count=0,
+def match_batch(ctx: Context, graph: DeviceGraph, plans, root_chunk=0, profile=False, max_count=0,
                 use_graph=True, max_work=0):
     """Batched path.  Returns (counts, BatchStats); with max_count or
     max_work, queries over a limit report 2**64-1."""
@@ -482,7 +482,6 @@ def match_batch(ctx: Context, graph: DeviceGraph, plans, bfs_depth=0, root_chunk
     counts = np.zeros(n, dtype=np.uint64)
     opts = MatchOpts()
     opts.flags = (FLAG_PROFILE if profile else 0) | (0 if use_graph else FLAG_NO_GRAPH)
-    opts.bfs_depth = bfs_depth
     opts.root_chunk = root_chunk
     opts.max_count = max_count
     opts.max_work = max_work

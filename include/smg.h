@@ -247,8 +247,8 @@ smg_status smg_graph_get_stats(const smg_graph *g, smg_graph_stats *out);
 
 typedef struct smg_match_opts {
   uint32_t flags;
-  uint32_t bfs_depth;     /* levels expanded breadth-first before the
-                             depth-first phase; 0 = autotuned             */
+  uint32_t reserved0;     /* must be 0 (the join is depth-first from a
+                             work queue; it has no breadth-first phase)   */
   uint32_t root_chunk;    /* root candidates per initial task; 0 = auto    */
   uint32_t reserved;
   uint64_t max_embeddings; /* rows of k ids the embeddings buffer can hold */
@@ -315,11 +315,14 @@ smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
 
 /* Autotuning.  Queries fall into shape classes: class = 4 * shape + size,
  * shape 0 tree (m = k-1), 2 dense (2m >= 3k), 1 sparse otherwise; size 0 for
- * k <= 5, 1 for 6..8, 2 for 9..12, 3 for 13+.  smg_autotune runs the sample
- * plans of each class under every candidate setting of the join (root
- * candidates per seeded task x shortest list worth splitting off to an idle
- * warp), keeps the fastest per class in the context, and reports them; later
- * smg_match / smg_match_batch calls on this context apply them. */
+ * k <= 5, 1 for 6..8, 2 for 9..12, 3 for 13+.  smg_autotune times up to 32
+ * sample plans of each class (filter + join device time) under the join's
+ * settings, one knob group at a time from the defaults: root candidates per
+ * seeded task x shortest list worth splitting off to an idle warp (3 x 3),
+ * then the slice length of long last-level lists (2,048 / 8,192 / 32,768),
+ * then the cap on stored hoisted sets (256 / 1,024 / 4,096 entries).  It
+ * keeps the fastest setting per class in the context and reports it; later
+ * smg_match / smg_match_batch calls and servers on this context apply it. */
 #define SMG_TUNE_CLASSES 12u
 typedef struct smg_tune_entry {
   uint32_t shape_class;
@@ -328,6 +331,8 @@ typedef struct smg_tune_entry {
   uint32_t samples;  /* sample queries timed for this class (0: untuned) */
   float best_ms;     /* device time of the sample under the kept setting */
   float default_ms;  /* device time of the sample under the default setting */
+  uint32_t split_len; /* last-level list slice length (0: 8,192)           */
+  uint32_t hoist_cap; /* entries of a stored hoisted set (0: the warp's buffer) */
 } smg_tune_entry;
 smg_status smg_autotune(smg_ctx *ctx, const smg_graph *g, const smg_plan *const *plans, uint32_t n,
                         smg_tune_entry *out /* [SMG_TUNE_CLASSES] or NULL */);
