@@ -473,6 +473,10 @@ def main():
     counts, _ = native.match_batch(ctx, dev, plans)
     want = [expected[i] for i in mine]
     mismatches = sum(1 for c, w in zip(counts.tolist(), want) if w is not None and int(c) != int(w))
+    # the per-level byte model of a breadth-first table join over the same
+    # partial matches (one untimed pass with the model counter on)
+    _, mst = native.match_batch(ctx, dev, plans, model=True)
+    model_bytes = mst.model_bytes
     # warm-up with the timed call: the first captures the batch's CUDA graph
     # (with its filter/join event nodes), the rest replay it
     for _ in range(args.warmup):
@@ -598,6 +602,14 @@ def main():
                          "traffic_gbs": traffic / (join_ms / args.steps / 1e3) / 1e9 if traffic and join_ms else None,
                          "traffic_frac": traffic / (join_ms / args.steps / 1e3) / 1e9 / peak if traffic and join_ms
                          else None},
+            # the same join time against the per-level byte model of a breadth-first
+            # table join over the same partial matches (rows read and written,
+            # anchors' whole lists, adjacency scans per back edge): what the
+            # reference's algorithm would have to move for this work
+            "roofline_model": {"bound": "hbm", "kernel": "k_join", "model_bytes_per_step": model_bytes,
+                               "achieved": model_bytes / (join_ms / args.steps / 1e3) / 1e9 if join_ms else None,
+                               "peak": peak, "unit": "GB/s",
+                               "frac": model_bytes / (join_ms / args.steps / 1e3) / 1e9 / peak if join_ms else None},
             # the filter kernels of the same passes (k_nlc_filter, k_cluster_walk, k_walk_chunks,
             # k_collect): their algorithmic bytes over their event-timed duration
             "roofline_filter": {"bound": "hbm", "kernels": "k_nlc_filter+k_cluster_walk+k_walk_chunks+k_collect",

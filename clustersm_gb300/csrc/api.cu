@@ -774,6 +774,7 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
   jl.emit = ch.emb != nullptr;
   jl.xbuf = ch.xbuf;
   jl.xcap = hoist_global_cap();
+  jl.count_model = o.model ? 1u : 0u;
   return jl;
 }
 
@@ -889,6 +890,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   st->descents += hq->descents;
   st->probes += hq->probes;
   st->last_count_entries += hq->last_count_entries;
+  st->model_bytes += hq->model_bytes;
   st->join_bytes += 8ull * hq->scanned + 8ull * hq->descents + 4ull * hq->probes + 8ull * hq->last_count_entries;
   if (o.profile) {
     float f = 0, j = 0;
@@ -960,6 +962,7 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.count_limit)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.work_limit)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.profile)));
+      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.model)));
       for (uint32_t i = 0; i < nq; ++i) key.push_back(plans[i]);
     }
     s = run_chunk(c, g, plans, ch, o, out, st, key.empty() ? nullptr : &key);
@@ -1029,6 +1032,7 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
     o.count_limit = opts->max_count;
     o.work_limit = opts->max_work;
     o.use_graph = (opts->flags & SMG_FLAG_NO_GRAPH) == 0;
+    o.model = (opts->flags & SMG_FLAG_MODEL) != 0;
   }
   std::vector<QueryOut> q(n);
   RunStats st;
@@ -1056,6 +1060,7 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
     stats->probes = st.probes;
     stats->last_count_entries = st.last_count_entries;
     stats->donations = st.donations;
+    stats->model_bytes = st.model_bytes;
   }
   return SMG_OK;
 }

@@ -70,6 +70,7 @@ struct RunOpts {
   bool use_graph = false;        // capture the launches in a CUDA graph
   uint64_t count_limit = 0;      // 0: none
   uint64_t work_limit = 0;       // 0: none
+  bool model = false;            // count the breadth-first byte model
 };
 
 struct QueryOut {
@@ -81,6 +82,7 @@ struct QueryOut {
 struct RunStats {
   float filter_ms = 0, join_ms = 0;
   uint64_t tasks = 0, donations = 0, scanned = 0, descents = 0, probes = 0, last_count_entries = 0;
+  uint64_t model_bytes = 0;
   uint64_t filter_bytes = 0, join_bytes = 0;
   uint64_t launches = 0, h2d = 0, d2h = 0;
   uint32_t chunks = 0;

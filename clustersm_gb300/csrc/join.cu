@@ -441,6 +441,28 @@ __device__ __forceinline__ uint32_t choose_pivot(const JoinLaunch &p, const Warp
   return best;
 }
 
+// The per-level byte model of a breadth-first join that keeps every partial
+// match in a table (the reference's join.cu:290-435): a row of `level`
+// mapped vertices is read (4 B per column), expanded along its anchor (the
+// back neighbour of least degree: its offsets and its whole list, one
+// candidate-bitmap word per entry, 8 + 8 B per entry) and checked against
+// every other back edge by an adjacency scan (8 + 4 B per entry); the rows it
+// produces are written (4 B per column, counted where they are produced).
+// cand_level / cand_deg stand in for a level whose vertex is not in S.m yet.
+__device__ __forceinline__ unsigned long long level_model(const WarpView &S, uint32_t level,
+                                                          uint32_t cand_level = kNone, uint32_t cand_deg = 0) {
+  uint32_t dmin = 0xFFFFFFFFu;
+  unsigned long long scans = 0;
+  for (uint32_t b = S.bmask[level]; b; b &= b - 1) {
+    const uint32_t j = __ffs(b) - 1;
+    const uint32_t d = j == cand_level ? cand_deg : S.deg[j];
+    dmin = min(dmin, d);
+    scans += 8ull + 4ull * d;
+  }
+  if (dmin == 0xFFFFFFFFu) return 4ull * level;
+  return 4ull * level + 8ull + 8ull * dmin + (scans - 8ull - 4ull * dmin);
+}
+
 // Candidate test for list entry w at `level` (>= 1, not the last level).
 __device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const CandView &cv, bool use_labels,
                                        uint32_t level, uint32_t w, uint32_t &probes) {
@@ -1063,7 +1085,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
   QueueState *qs = p.qs;
   volatile int *vabort = &qs->abort;
   uint64_t idle_mark = 0, idle_t0 = 0;
-  unsigned long long scanned = 0, descents = 0;
+  unsigned long long scanned = 0, descents = 0, model = 0;
   uint32_t probes = 0;
 
   while (true) {
@@ -1143,6 +1165,8 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         S.lbase[L0] = scan_list(p, S, Q.use_labels, L0, S.m[pv], S.beg[pv], S.deg[pv], len);
         S.cur[L0] = lo;
         S.end[L0] = hi == kNone ? len : min(hi, len);
+        // a split-off batch candidate: its row was never expanded by the donor
+        if (p.count_model && hi == kNone) model += 4ull * L0 + level_model(S, L0);
       }
       S.bcnt[L0] = 0;
       S.bidx[L0] = 0;
@@ -1213,6 +1237,18 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       if (level == P) {
         const uint32_t bc = S.bcnt[level];
         if (bc) {
+          if (p.count_model) {
+            // each candidate's row of P + 1 vertices, written and expanded
+            // (complete embeddings are counted, not written)
+            unsigned long long mb = 0;
+            if (lane < bc) {
+              const uint32_t v = S.batch[P * 32 + lane];
+              const uint32_t vd = __ldg(p.off + v + 1) - __ldg(p.off + v);
+              mb = 4ull * (P + 1) + level_model(S, P + 1, P, vd);
+            }
+            for (int o = 16; o; o >>= 1) mb += __shfl_down_sync(0xFFFFFFFFu, mb, o);
+            if (lane == 0) model += mb;
+          }
           cnt += last_level(S, p, Q, q, cv, P, bc, lane, scanned, probes);
           descents += bc;
           if (lane == 0) S.bcnt[level] = 0;
@@ -1257,6 +1293,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
             S.bcnt[nl] = 0;
             S.bidx[nl] = 0;
             if (nl == P) *S.xlen = kHoistInvalid;  // the prefix m[0..P-1] changed
+            if (p.count_model) model += 4ull * nl + level_model(S, nl);  // the row written, then expanded
           }
           __syncwarp();
           ++descents;
@@ -1330,6 +1367,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
       }
       atomicAdd(&qs->scanned, scanned);
       atomicAdd(&qs->descents, descents);
+      if (model) atomicAdd(&qs->model_bytes, model);
       if (pr) atomicAdd(&qs->probes, pr);
       if (!aborted) {
         atomicAdd(&qs->tasks_done, 1ull);
@@ -1342,6 +1380,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     }
     scanned = 0;
     descents = 0;
+    model = 0;
     if (aborted || preempted) break;
   }
 }

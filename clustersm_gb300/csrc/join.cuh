@@ -21,6 +21,10 @@ struct QueueState {
   QLine head, tail, pending, progress;
   unsigned long long tasks_done, donations, start_ns, scanned, descents, probes;
   unsigned long long last_count_entries;  // list entries read by k_last_counts
+  // bytes a breadth-first table join would move for the same partial
+  // matches (JoinLaunch::count_model; the per-level model of the join's
+  // minimum traffic)
+  unsigned long long model_bytes;
   int error;  // JOIN_ERR_* below, first one wins
   int abort;  // set on error or deadline: every warp leaves
   int full;   // a donation found the queue full (load balance only)
@@ -92,6 +96,9 @@ struct JoinLaunch {
   // Join blocks per SM at most (0: as many as fit); the server leaves room
   // for the filter kernels of requests admitted into a running slice.
   uint32_t max_blocks_per_sm;
+  // Accumulate QueueState::model_bytes (a measurement run; costs a few loads
+  // per partial match).
+  uint32_t count_model;
 };
 
 // The resident graph's arrays in a launch record (every launch site uses

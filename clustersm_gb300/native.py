@@ -80,7 +80,7 @@ class BatchStats(C.Structure):
                 ("d2h_bytes", C.c_uint64), ("filter_bytes", C.c_uint64), ("join_bytes", C.c_uint64),
                 ("chunks", C.c_uint32), ("reserved", C.c_uint32), ("scanned", C.c_uint64),
                 ("descents", C.c_uint64), ("probes", C.c_uint64), ("last_count_entries", C.c_uint64),
-                ("donations", C.c_uint64)]
+                ("donations", C.c_uint64), ("model_bytes", C.c_uint64)]
 
 
 class TuneEntry(C.Structure):
@@ -474,14 +474,14 @@ def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=F
 
 
 def match_batch(ctx: Context, graph: DeviceGraph, plans, root_chunk=0, profile=False, max_count=0,
-                use_graph=True, max_work=0):
+                use_graph=True, max_work=0, model=False):
     """Batched path.  Returns (counts, BatchStats); with max_count or
     max_work, queries over a limit report 2**64-1."""
     n = len(plans)
     arr = (C.c_void_p * n)(*[p.handle.value for p in plans])
     counts = np.zeros(n, dtype=np.uint64)
     opts = MatchOpts()
-    opts.flags = (FLAG_PROFILE if profile else 0) | (0 if use_graph else FLAG_NO_GRAPH)
+    opts.flags = (FLAG_PROFILE if profile else 0) | (0 if use_graph else FLAG_NO_GRAPH) | (FLAG_MODEL if model else 0)
     opts.root_chunk = root_chunk
     opts.max_count = max_count
     opts.max_work = max_work

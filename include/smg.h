@@ -244,6 +244,11 @@ smg_status smg_graph_get_stats(const smg_graph *g, smg_graph_stats *out);
 #define SMG_FLAG_PROFILE 2u   /* record per-phase device times (adds syncs)  */
 #define SMG_FLAG_NO_GRAPH 4u  /* batched path: launch directly instead of
                                  capturing the launches in a CUDA graph    */
+#define SMG_FLAG_MODEL 8u     /* batched path: also count model_bytes, the
+                                 bytes a breadth-first table join (the
+                                 reference's, join.cu:290-435) would move
+                                 for the same partial matches (costs a few
+                                 loads per partial match)                 */
 
 typedef struct smg_match_opts {
   uint32_t flags;
@@ -307,6 +312,11 @@ typedef struct smg_batch_stats {
   uint64_t probes;           /* membership probes (bitmap words, searches) */
   uint64_t last_count_entries; /* list entries read to build last counts   */
   uint64_t donations;        /* tasks split off to idle warps              */
+  uint64_t model_bytes;      /* with SMG_FLAG_MODEL: per row of r mapped
+                                vertices, 4r read + 8 + 8 x the anchor's
+                                degree + (8 + 4 x degree) per other back
+                                edge, plus 4r written where a row is made;
+                                0 otherwise                               */
 } smg_batch_stats;
 smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
                            const smg_plan *const *plans, uint32_t n,

@@ -265,3 +265,24 @@ def test_memory_bounded_chunks(ctx, monkeypatch):
     assert st2.chunks > 1
     assert parts.tolist() == whole.tolist()
     dev.free()
+
+
+def test_model_counter_leaves_counts(ctx):
+    """SMG_FLAG_MODEL counts the breadth-first byte model and changes no count;
+    without the flag the model reads 0.  For a 2-vertex query (one edge u-w)
+    the model is exact by hand: every root v is a row of one vertex, written
+    (4 B) and expanded along its own list (4 B read + 8 B offsets + 8 B per
+    entry), with no complete row written."""
+    from clustersm_gb300.native import HostGraph
+    host = HostGraph.er(1000, 4000, 4, seed=1)
+    dev = DeviceGraph(ctx, host)
+    qs = [Query.generate(host, k, sh, seed=40 + k) for k in (3, 4, 5) for sh in ("tree", "sparse")]
+    plans = [Plan(q) for q in qs]
+    c0, s0 = native.match_batch(ctx, dev, plans)
+    c1, s1 = native.match_batch(ctx, dev, plans, model=True)
+    assert c0.tolist() == c1.tolist() and s0.model_bytes == 0 and s1.model_bytes > 0
+    edge = Plan(Query([1, 1], [0, 1]))  # both ends alike: either may be the join's first vertex
+    _, se = native.match_batch(ctx, dev, [edge], model=True)
+    roots = np.nonzero(native.filter_inspect(ctx, dev, edge)[2] & 1)[0]
+    deg = np.diff(host.offsets().astype(np.int64))
+    assert se.model_bytes == sum(4 + 4 + 8 + 8 * int(deg[v]) for v in roots)
