@@ -420,6 +420,9 @@ def run_reference(args, wl, host, queries, rank, meta_queries):
                              "sample": f"{sample} queries per step, one per (shape, k) stratum in turn "
                                        f"({len(strata)} strata)"},
             "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    maps = Path("/proc/self/maps")
+    if maps.exists():  # this arm runs the oracle alone: the library must not be mapped
+        line["library_mapped"] = "libsmg.so" in maps.read_text()
     print(json.dumps(line), flush=True)
 
 
@@ -428,6 +431,20 @@ def main():
     rank, world, local = dist_env()
     from clustersm_gb300.workloads import load, shard
     wl = load(args.workload)
+    if args.impl == "reference":
+        # the oracle's own graph generator and query records: this arm maps
+        # nothing of the library
+        import oracle
+        meta = json.loads((ROOT / wl.queries_file).read_text())
+        mq = meta["queries"]
+        if args.shape:
+            mq = [q for q in mq if q.get("shape") == args.shape]
+        if args.subset:
+            mq = mq[: args.subset]
+        host = (oracle.Graph.er(wl.n, wl.m, wl.labels, wl.seed, zipf=wl.zipf) if wl.kind == "er"
+                else oracle.Graph.rmat(wl.scale, wl.avg_degree, wl.labels, wl.seed, zipf=wl.zipf))
+        qs = [oracle.QueryArrays(q["labels"], q["edges"]) for q in mq]
+        return run_reference(args, wl, host, qs, rank, mq)
     queries_all, expected, meta = wl.queries()
     if args.shape:
         keep = [i for i, q in enumerate(meta["queries"]) if q.get("shape") == args.shape]
@@ -439,8 +456,6 @@ def main():
     mine = shard(len(queries_all), rank, world)
     queries = [queries_all[i] for i in mine]
     host = wl.graph()
-    if args.impl == "reference":
-        return run_reference(args, wl, host, queries_all, rank, meta["queries"])
 
     import torch
     from clustersm_gb300 import native

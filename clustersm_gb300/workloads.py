@@ -13,7 +13,6 @@ import json
 from dataclasses import dataclass, field
 from pathlib import Path
 
-from .native import HostGraph, Query
 
 ROOT = Path(__file__).resolve().parents[1]
 
@@ -33,7 +32,8 @@ class Workload:
     description: str = ""
     extra: dict = field(default_factory=dict)
 
-    def graph(self, threads: int = 0) -> HostGraph:
+    def graph(self, threads: int = 0):
+        from .native import HostGraph  # the library is loaded only when a graph is made
         if self.kind == "er":
             return HostGraph.er(self.n, self.m, self.labels, seed=self.seed, zipf=self.zipf)
         return HostGraph.rmat(self.scale, self.avg_degree, self.labels, seed=self.seed, zipf=self.zipf,
@@ -41,6 +41,7 @@ class Workload:
 
     def queries(self):
         """(queries, expected counts or None) from the committed fixture."""
+        from .native import Query
         data = json.loads((ROOT / self.queries_file).read_text())
         qs = [Query(q["labels"], q["edges"]) for q in data["queries"]]
         counts = [q.get("count") for q in data["queries"]]

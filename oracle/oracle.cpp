@@ -4,6 +4,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -511,5 +512,210 @@ int oracle_encode(const smg_csr *g, const smg_plan_view *p, const uint32_t *vmas
     }
   return 0;
 }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ inputs
+// The seeded synthetic graphs of the workloads, restated here so that the
+// CPU baseline needs nothing from the library: a counter-seeded xoshiro256**
+// stream (splitmix64 seeding), R-MAT quadrants on a 16-bit grid with
+// (a, a+b, a+b+c) = (0.57, 0.76, 0.95), Zipf(s=1) labels as integer weights
+// floor(2^40 / (l + 1)), and a symmetrised, sorted, duplicate- and loop-free
+// CSR.  tests/test_oracle.py checks them bit for bit against the library's
+// generator.
+namespace {
+
+uint64_t sm64(uint64_t &x) {
+  uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+struct Xs {
+  uint64_t s[4];
+  explicit Xs(uint64_t seed) {
+    uint64_t x = seed;
+    for (auto &w : s) w = sm64(x);
+  }
+  static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+  uint64_t next() {
+    const uint64_t r = rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 45);
+    return r;
+  }
+  uint64_t below(uint64_t bound) { return static_cast<uint64_t>((static_cast<unsigned __int128>(next()) * bound) >> 64); }
+};
+
+uint64_t stream_of(uint64_t seed, uint64_t stream, uint64_t chunk) {
+  uint64_t x = seed ^ (stream * 0xD1B54A32D192ED03ull);
+  const uint64_t a = sm64(x);
+  x = a ^ (chunk * 0x8CB92BA72F3D8DD7ull);
+  return sm64(x);
+}
+
+void gen_labels(uint32_t n, uint32_t L, bool zipf, uint64_t seed, uint32_t *label) {
+  std::vector<uint64_t> cum;
+  uint64_t acc = 0;
+  for (uint32_t l = 0; l < L; ++l) {
+    acc += zipf ? ((1ull << 40) / (l + 1)) : (1ull << 32);
+    cum.push_back(acc);
+  }
+  const int64_t chunk = 1 << 16, nchunks = (static_cast<int64_t>(n) + chunk - 1) / chunk;
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    Xs r(stream_of(seed, 2, static_cast<uint64_t>(c)));
+    const int64_t e = std::min<int64_t>(n, (c + 1) * chunk);
+    for (int64_t v = c * chunk; v < e; ++v)
+      label[v] = static_cast<uint32_t>(std::upper_bound(cum.begin(), cum.end(), r.below(cum.back())) - cum.begin());
+  }
+}
+
+// CSR of a directed pair list, symmetrised, sorted, without loops or repeats.
+void to_csr(uint32_t n, const std::vector<uint32_t> &a, const std::vector<uint32_t> &b, std::vector<uint64_t> &off,
+            std::vector<uint32_t> &adj) {
+  std::vector<uint64_t> cnt(static_cast<size_t>(n) + 1, 0);
+  for (size_t i = 0; i < a.size(); ++i)
+    if (a[i] != b[i]) {
+      ++cnt[a[i] + 1];
+      ++cnt[b[i] + 1];
+    }
+  for (uint32_t v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
+  std::vector<uint32_t> tmp(cnt[n]);
+  std::vector<uint64_t> at(cnt.begin(), cnt.end() - 1);
+  for (size_t i = 0; i < a.size(); ++i)
+    if (a[i] != b[i]) {
+      tmp[at[a[i]]++] = b[i];
+      tmp[at[b[i]]++] = a[i];
+    }
+  off.assign(static_cast<size_t>(n) + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < static_cast<int64_t>(n); ++v) {
+    auto lo = tmp.begin() + static_cast<int64_t>(cnt[v]), hi = tmp.begin() + static_cast<int64_t>(cnt[v + 1]);
+    std::sort(lo, hi);
+    off[v + 1] = static_cast<uint64_t>(std::unique(lo, hi) - lo);
+  }
+  for (uint32_t v = 0; v < n; ++v) off[v + 1] += off[v];
+  adj.resize(off[n]);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < static_cast<int64_t>(n); ++v)
+    std::copy(tmp.begin() + static_cast<int64_t>(cnt[v]),
+              tmp.begin() + static_cast<int64_t>(cnt[v] + (off[v + 1] - off[v])), adj.begin() + static_cast<int64_t>(off[v]));
+}
+
+int hand_out(const std::vector<uint64_t> &off, const std::vector<uint32_t> &adj, const std::vector<uint32_t> &lab,
+             uint64_t **o_off, uint32_t **o_adj, uint32_t **o_lab, uint64_t *o_m2) {
+  *o_off = static_cast<uint64_t *>(std::malloc(off.size() * 8));
+  *o_adj = static_cast<uint32_t *>(std::malloc(std::max<size_t>(adj.size(), 1) * 4));
+  *o_lab = static_cast<uint32_t *>(std::malloc(std::max<size_t>(lab.size(), 1) * 4));
+  if (!*o_off || !*o_adj || !*o_lab) return 1;
+  std::memcpy(*o_off, off.data(), off.size() * 8);
+  if (!adj.empty()) std::memcpy(*o_adj, adj.data(), adj.size() * 4);
+  if (!lab.empty()) std::memcpy(*o_lab, lab.data(), lab.size() * 4);
+  *o_m2 = adj.size();
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels, uint32_t zipf, uint64_t seed,
+                    uint64_t **off, uint32_t **adj, uint32_t **labels, uint64_t *m2) {
+  if (!off || !adj || !labels || !m2 || scale < 1 || scale > 31 || !avg_degree || !num_labels) return 1;
+  const uint32_t n = 1u << scale;
+  const uint64_t draws = static_cast<uint64_t>(n) * avg_degree / 2;
+  const uint32_t TA = 37356, TB = 49807, TC = 62259;
+  std::vector<uint32_t> a(draws), b(draws);
+  const int64_t chunk = 1 << 20, nchunks = static_cast<int64_t>((draws + chunk - 1) / chunk);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    Xs r(stream_of(seed, 3, static_cast<uint64_t>(c)));
+    const int64_t e = std::min<int64_t>(static_cast<int64_t>(draws), (c + 1) * chunk);
+    for (int64_t i = c * chunk; i < e; ++i) {
+      uint32_t u = 0, v = 0;
+      uint64_t bits = 0;
+      int left = 0;
+      for (uint32_t lvl = 0; lvl < scale; ++lvl) {
+        if (left == 0) {
+          bits = r.next();
+          left = 4;
+        }
+        const uint32_t x = static_cast<uint32_t>(bits & 0xFFFF);
+        bits >>= 16;
+        --left;
+        u = (u << 1) | (x >= TB ? 1u : 0u);
+        v = (v << 1) | (((x >= TA && x < TB) || x >= TC) ? 1u : 0u);
+      }
+      a[i] = u;
+      b[i] = v;
+    }
+  }
+  std::vector<uint64_t> o;
+  std::vector<uint32_t> d, lab(n);
+  to_csr(n, a, b, o, d);
+  gen_labels(n, num_labels, zipf != 0, seed, lab.data());
+  return hand_out(o, d, lab, off, adj, labels, m2);
+}
+
+int oracle_gen_er(uint32_t n, uint64_t m, uint32_t num_labels, uint32_t zipf, uint64_t seed, uint64_t **off,
+                  uint32_t **adj, uint32_t **labels, uint64_t *m2) {
+  if (!off || !adj || !labels || !m2 || n < 2 || !num_labels || m > static_cast<uint64_t>(n) * (n - 1) / 2) return 1;
+  Xs r(stream_of(seed, 1, 0));
+  std::vector<uint32_t> a, b;
+  a.reserve(m);
+  b.reserve(m);
+  // distinct unordered pairs in draw order: an open-addressing set of the
+  // keys (min, max) + 1, so that 0 marks an empty cell
+  std::vector<uint64_t> table;
+  size_t mask = 0, filled = 0;
+  auto grow = [&]() {
+    std::vector<uint64_t> old;
+    old.swap(table);
+    table.assign(old.size() * 2, 0);
+    mask = table.size() - 1;
+    for (uint64_t k : old)
+      if (k) {
+        size_t h = static_cast<size_t>(k * 0x9E3779B97F4A7C15ull) & mask;
+        while (table[h]) h = (h + 1) & mask;
+        table[h] = k;
+      }
+  };
+  table.assign(1024, 0);
+  mask = 1023;
+  while (a.size() < m) {
+    const uint32_t x = static_cast<uint32_t>(r.below(n)), y = static_cast<uint32_t>(r.below(n));
+    if (x == y) continue;
+    // +1 so that the key is never 0 (the empty marker)
+    const uint64_t k = ((static_cast<uint64_t>(std::min(x, y)) << 32) | std::max(x, y)) + 1;
+    if (2 * (filled + 1) > table.size()) grow();
+    size_t h = static_cast<size_t>(k * 0x9E3779B97F4A7C15ull) & mask;
+    bool dup = false;
+    while (table[h]) {
+      if (table[h] == k) {
+        dup = true;
+        break;
+      }
+      h = (h + 1) & mask;
+    }
+    if (dup) continue;
+    table[h] = k;
+    ++filled;
+    a.push_back(x);
+    b.push_back(y);
+  }
+  std::vector<uint64_t> o;
+  std::vector<uint32_t> d, lab(n);
+  to_csr(n, a, b, o, d);
+  gen_labels(n, num_labels, zipf != 0, seed, lab.data());
+  return hand_out(o, d, lab, off, adj, labels, m2);
+}
+
+void oracle_free(void *p) { std::free(p); }
 
 }  // extern "C"

@@ -68,6 +68,16 @@ int oracle_ref_rows(const smg_csr *g, uint32_t k, uint32_t num_edges, const uint
                     const uint32_t *second, const uint32_t *candmask, int threads, uint64_t limit,
                     uint64_t *rows);
 
+/* The workloads' seeded graphs (R-MAT and Erdos-Renyi, with uniform or
+ * Zipf(s=1) labels), restated from the same integer generator so that the
+ * CPU baseline needs nothing from the library.  The arrays are malloc'd;
+ * release them with oracle_free.  *m2 = entries of adj (2 x edges). */
+int oracle_gen_rmat(uint32_t scale, uint32_t avg_degree, uint32_t num_labels, uint32_t zipf, uint64_t seed,
+                    uint64_t **offsets, uint32_t **adj, uint32_t **labels, uint64_t *m2);
+int oracle_gen_er(uint32_t n, uint64_t m, uint32_t num_labels, uint32_t zipf, uint64_t seed,
+                  uint64_t **offsets, uint32_t **adj, uint32_t **labels, uint64_t *m2);
+void oracle_free(void *p);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,3 +49,5 @@ def test_reference_arm_line():
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["workload"] == "er1k"
+    # the arm times the oracle alone: nothing of the library is loaded
+    assert line.get("library_mapped", False) is False

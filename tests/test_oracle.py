@@ -110,3 +110,20 @@ def test_filter_prunes():
         vm = oracle.nlc_filter(g, plan)
         _, cm = oracle.encode(g, plan, vm)
         assert np.all((cm & ~vm) == 0)
+
+
+@pytest.mark.parametrize("kind", ["rmat", "rmat_uniform", "er", "er_zipf"])
+def test_oracle_generators_equal_the_library(kind):
+    """The oracle's own restatement of the seeded generators (used by the CPU
+    baseline so that it loads nothing of the library) gives the library's
+    graphs bit for bit."""
+    from clustersm_gb300.native import HostGraph
+    if kind.startswith("rmat"):
+        z = kind == "rmat"
+        a, b = oracle.Graph.rmat(13, 12, 7, 3, zipf=z), HostGraph.rmat(13, 12, 7, seed=3, zipf=z)
+    else:
+        z = kind == "er_zipf"
+        a, b = oracle.Graph.er(2000, 9000, 5, 4, zipf=z), HostGraph.er(2000, 9000, 5, seed=4, zipf=z)
+    assert np.array_equal(a.offsets(), b.offsets())
+    assert np.array_equal(a.neighbors(), b.neighbors())
+    assert np.array_equal(a.labels(), b.labels())
