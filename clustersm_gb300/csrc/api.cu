@@ -811,7 +811,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
     st->h2d += c->fdev->host.size() + nq * (sizeof(FilterQuery) + sizeof(JoinQuery));
     uint64_t walk_launches = 0;
     for (uint32_t ng : c->fdev->phase_count)
-      if (ng) walk_launches += (ng + 65534) / 65535 + 1;  // walk + chunk pass
+      if (ng) walk_launches += 3;  // work list, walk, chunk pass
     const uint64_t launches = 2 * ((nq + 65534) / 65535) + walk_launches + 2;
     st->launches += launches;
     if (key) {

@@ -224,34 +224,95 @@ __device__ __forceinline__ uint32_t queue_tail_chunks(uint32_t tag, uint32_t v, 
   return e1;
 }
 
-// A warp takes 32 candidates of the group's core, one per lane: each lane
-// applies the group's steps to its own candidate (core slot, merge tests,
-// combine rule), then the warp walks the neighbour runs of all 32 as one
-// segmented stream (an entry finds its candidate by a binary search over the
-// lanes' run offsets), so short runs still fill the warp.  Runs longer than
-// kWalkChunk hand their tail to the chunk pass.
+// Candidates of a group's core that its step group walks, clamped to the
+// core's segment of the candidate list.
+__device__ __forceinline__ uint32_t group_candidates(const StepGroup &G, const FilterQuery &Q) {
+  uint32_t cnt = *(volatile const uint32_t *)(Q.cand_cnt + G.core);
+  if (!SMG_DCHECK(Q.cand_off[G.core] + cnt <= Q.cand_off[G.core + 1], 202, cnt, G.core)) cnt = 0;
+  return cnt;
+}
+
+// The walk's work list of one phase: group g owns 32-candidate chunks
+// [chunk_start[g], chunk_start[g + 1]); chunk_start[ng] is the total.  The
+// groups of a phase differ in size by orders of magnitude (a frequent label's
+// core has millions of candidates, a rare one's a few), so the walk's warps
+// take chunks from one counter instead of a fixed share of blocks per group.
+__global__ void __launch_bounds__(1024) k_walk_plan(const StepGroup *__restrict__ groups, uint32_t ng,
+                                                    const FilterQuery *__restrict__ qs,
+                                                    uint32_t *__restrict__ chunk_start) {
+  __shared__ uint32_t warp_sum[32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t per = (ng + blockDim.x - 1) / blockDim.x;
+  const uint32_t lo = min(ng, threadIdx.x * per), hi = min(ng, lo + per);
+  uint32_t own = 0;
+  for (uint32_t g = lo; g < hi; ++g) own += (group_candidates(groups[g], qs[groups[g].query]) + 31) / 32;
+  uint32_t incl = own;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= static_cast<uint32_t>(o)) incl += t;
+  }
+  if (lane == 31) warp_sum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < (blockDim.x >> 5) ? warp_sum[lane] : 0u;
+    uint32_t wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+      if (lane >= static_cast<uint32_t>(o)) wi += t;
+    }
+    warp_sum[lane] = wi - w;
+    if (lane == 31) chunk_start[ng] = wi;
+  }
+  __syncthreads();
+  uint32_t run = warp_sum[warp] + incl - own;
+  for (uint32_t g = lo; g < hi; ++g) {
+    chunk_start[g] = run;
+    run += (group_candidates(groups[g], qs[groups[g].query]) + 31) / 32;
+  }
+}
+
+// A warp takes a chunk of 32 candidates of one group's core, one per lane:
+// each lane applies the group's steps to its own candidate (core slot, merge
+// tests, combine rule), then the warp walks the neighbour runs of all 32 as
+// one segmented stream (an entry finds its candidate by a binary search over
+// the lanes' run offsets), so short runs still fill the warp.  Runs longer
+// than kWalkChunk hand their tail to the chunk pass.  Chunks come from one
+// counter over the whole phase (k_walk_plan's work list).
 __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict__ off,
                                                       const uint32_t *__restrict__ adj,
-                                                      const StepGroup *__restrict__ groups, uint32_t group_base,
+                                                      const StepGroup *__restrict__ groups, uint32_t ng,
+                                                      const uint32_t *__restrict__ chunk_start,
+                                                      unsigned int *next,
                                                       const ClusterStep *__restrict__ steps,
                                                       const uint32_t *__restrict__ aux,
                                                       const FilterQuery *__restrict__ qs, WalkOverflow ov) {
-  const uint32_t gi = group_base + blockIdx.y;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t chunks = chunk_start[ng];
+  while (true) {
+  uint32_t item = 0;
+  if (lane == 0) item = atomicAdd(next, 1u);
+  item = __shfl_sync(0xFFFFFFFFu, item, 0);
+  if (item >= chunks) break;
+  // the group owning the chunk: the last g with chunk_start[g] <= item
+  uint32_t glo = 0, ghi = ng;
+  while (ghi - glo > 1) {
+    const uint32_t mid = (glo + ghi) >> 1;
+    if (chunk_start[mid] <= item) glo = mid;
+    else ghi = mid;
+  }
+  const uint32_t gi = glo;
   const StepGroup G = groups[gi];
   const FilterQuery &Q = qs[G.query];
-  const uint32_t lane = threadIdx.x & 31;
   const uint32_t W = Q.words;
   uint32_t *const enc = Q.enc;
   uint32_t *const list = Q.cand + Q.cand_off[G.core];
-  uint32_t cnt = *(volatile const uint32_t *)(Q.cand_cnt + G.core);
-  if (!SMG_DCHECK(Q.cand_off[G.core] + cnt <= Q.cand_off[G.core + 1], 202, cnt, G.core)) cnt = 0;
+  const uint32_t cnt = group_candidates(G, Q);
   const uint32_t kind = steps[G.first].kind;
   const bool by_label = G.nlab && ov.adjl;
   const uint32_t nruns = by_label ? G.nlab : 1;
-  const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
   unsigned long long scanned = 0;
-  for (uint64_t i0 = (static_cast<uint64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; i0 < cnt;
-       i0 += warps * 32) {
+  {
+    const uint64_t i0 = static_cast<uint64_t>(item - chunk_start[gi]) * 32;
     const uint64_t i = i0 + lane;
     uint32_t v = 0, pass = 0;
     bool act = false;
@@ -342,6 +403,7 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
   }
   for (int o = 16; o; o >>= 1) scanned += __shfl_down_sync(0xFFFFFFFFu, scanned, o);
   if (lane == 0 && scanned) atomicAdd(Q.stat + 1, scanned);
+  }  // chunks
 }
 
 // Chunks of long neighbour lists queued by k_cluster_walk: one warp each.
@@ -630,8 +692,9 @@ smg_status FilterDev::upload(const FilterBatch &fb, cudaStream_t s) {
   const size_t bytes_steps = fb.steps.size() * sizeof(ClusterStep);
   const size_t bytes_groups = flat.size() * sizeof(StepGroup);
   const size_t bytes_aux = fb.aux.size() * sizeof(uint32_t);
+  const size_t bytes_cs = (flat.size() + phase_count.size()) * sizeof(uint32_t);  // walk work lists
   auto al256 = [](size_t x) { return (x + 255) & ~size_t(255); };
-  const size_t need = al256(bytes_steps) + al256(bytes_groups) + al256(bytes_aux) + 256;
+  const size_t need = al256(bytes_steps) + al256(bytes_groups) + al256(bytes_aux) + al256(bytes_cs) + 256;
   if (need > cap) {
     if (buf) cudaFree(buf);
     buf = nullptr;
@@ -650,9 +713,13 @@ smg_status FilterDev::upload(const FilterBatch &fb, cudaStream_t s) {
   const size_t os = put(fb.steps.data(), bytes_steps);
   const size_t og = put(flat.data(), bytes_groups);
   const size_t oa = put(fb.aux.data(), bytes_aux);
+  const size_t oc = o;  // written on the device by k_walk_plan
+  std::memset(host.data() + oc, 0, bytes_cs);
+  o = (o + bytes_cs + 255) & ~size_t(255);
   steps = reinterpret_cast<ClusterStep *>(static_cast<char *>(buf) + os);
   groups = reinterpret_cast<StepGroup *>(static_cast<char *>(buf) + og);
   aux = reinterpret_cast<uint32_t *>(static_cast<char *>(buf) + oa);
+  chunk_start = reinterpret_cast<uint32_t *>(static_cast<char *>(buf) + oc);
   SMG_CUDA(cudaMemcpyAsync(buf, host.data(), o, cudaMemcpyHostToDevice, s));
   // the staging buffer must outlive the copy
   SMG_CUDA(cudaStreamSynchronize(s));
@@ -703,13 +770,13 @@ smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const Filter
     po.lab_of = g.lab_of;
     po.lab_off = g.lab_off;
     po.lab_buckets = g.lab_buckets;
-    const uint32_t wx = std::max<uint32_t>(1, std::min<uint32_t>(2048, (num_sms * 16u + ng - 1) / ng));
-    for (uint32_t y0 = 0; y0 < ng; y0 += 65535) {
-      const uint32_t ny = std::min<uint32_t>(65535, ng - y0);
-      k_cluster_walk<<<dim3(wx, ny), 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p], y0, fd.steps,
-                                                  fd.aux, d_qs, po);
-      SMG_CUDA(cudaGetLastError());
-    }
+    uint32_t *cs = fd.chunk_start + fd.phase_first[p] + p;  // ng + 1 entries per phase
+    k_walk_plan<<<1, 1024, 0, s>>>(fd.groups + fd.phase_first[p], ng, d_qs, cs);
+    SMG_CUDA(cudaGetLastError());
+    // the phase's second zeroed counter hands out the chunks
+    k_cluster_walk<<<num_sms * 8, 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p], ng, cs, po.count + 1,
+                                               fd.steps, fd.aux, d_qs, po);
+    SMG_CUDA(cudaGetLastError());
     k_walk_chunks<<<num_sms * 8, 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p], fd.steps, fd.aux,
                                                 d_qs, po);
     SMG_CUDA(cudaGetLastError());

@@ -46,6 +46,7 @@ struct FilterDev {
   ClusterStep *steps = nullptr;
   StepGroup *groups = nullptr;
   uint32_t *aux = nullptr;
+  uint32_t *chunk_start = nullptr;  // per phase: its walk work list (k_walk_plan), ng + 1 entries
   std::vector<uint32_t> phase_first, phase_count;
   smg_status upload(const FilterBatch &fb, cudaStream_t s);
   // Grows the device buffer ahead of time, so that an upload of at most
