@@ -25,7 +25,7 @@ STATUS = {0: "SMG_OK", 1: "SMG_ERR_INVALID", 2: "SMG_ERR_IO", 3: "SMG_ERR_FORMAT
           13: "SMG_ERR_INTERNAL"}
 SHAPES = {"tree": 0, "sparse": 1, "dense": 2, "induced": 3}
 LABELS_UNIFORM, LABELS_ZIPF1 = 0, 1
-FLAG_EMIT, FLAG_PROFILE, FLAG_NO_GRAPH = 1, 2, 4
+FLAG_EMIT, FLAG_PROFILE, FLAG_NO_GRAPH, FLAG_MODEL = 1, 2, 4, 8
 
 
 class SmgError(RuntimeError):

@@ -276,7 +276,14 @@ def test_model_counter_leaves_counts(ctx):
     from clustersm_gb300.native import HostGraph
     host = HostGraph.er(1000, 4000, 4, seed=1)
     dev = DeviceGraph(ctx, host)
-    qs = [Query.generate(host, k, sh, seed=40 + k) for k in (3, 4, 5) for sh in ("tree", "sparse")]
+    qs = []
+    for k in (3, 4, 5):
+        for sh in ("tree", "sparse"):
+            try:
+                qs.append(Query.generate(host, k, sh, seed=40 + k))
+            except native.SmgError:
+                pass  # no walk of that shape from this seed
+    assert len(qs) >= 3
     plans = [Plan(q) for q in qs]
     c0, s0 = native.match_batch(ctx, dev, plans)
     c1, s1 = native.match_batch(ctx, dev, plans, model=True)
