@@ -267,6 +267,37 @@ def c4_leg(ctx, peak, scale=25, avg_degree=32, labels=64, seed=1, draws=64, k=12
     return out
 
 
+def random_sector_peak(device, gib=8, reads=1 << 29, reps=3):
+    """Throughput ceiling of random 32-byte sector reads on this GPU: a seeded
+    random gather of 4-byte words from a buffer far larger than L2 (each word
+    costs one DRAM sector), timed with CUDA events; reported as sectors x 32 B
+    per second.  The join's DRAM traffic is such sectors, so this, not the
+    streaming copy peak, is the ceiling its traffic can approach."""
+    import torch
+    n = (gib << 30) // 4
+    buf = torch.ones(n, dtype=torch.int32, device=device)
+    g = torch.Generator(device=device)
+    g.manual_seed(12345)
+    idx = torch.randint(0, n, (reads,), device=device, dtype=torch.int64, generator=g)
+    out = torch.empty(reads, dtype=torch.int32, device=device)
+    torch.index_select(buf, 0, idx, out=out)  # warm-up
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        torch.index_select(buf, 0, idx, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del buf, idx, out
+    torch.cuda.empty_cache()
+    return {"gbs": reads * 32 / (best / 1e3) / 1e9, "unit": "GB/s",
+            "how": f"torch.index_select of {reads} random int32 words from a {gib} GiB buffer, best of {reps}, "
+                   "32 B per read (one DRAM sector)"}
+
+
 def wide_leg(ctx, dev, stream, flush, steps=3, warmup=2):
     """Batched path on the rmat22_k4to7 queries against the resident 2^22
     graph (the same graph as rmat22): device time of `steps` passes after
@@ -582,6 +613,7 @@ def main():
 
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
+    rpeak = random_sector_peak(f"cuda:{local}") if world == 1 else None
     achieved = jbytes / (join_ms / 1e3) / 1e9 if join_ms > 0 else 0.0
     traffic = None  # k_join DRAM bytes per step from an ncu capture of this workload
     tf = ROOT / "profiles" / "traffic.txt"
@@ -616,7 +648,11 @@ def main():
                          # DRAM traffic of the same kernel (one ncu capture) over its event-timed duration
                          "traffic_gbs": traffic / (join_ms / args.steps / 1e3) / 1e9 if traffic and join_ms else None,
                          "traffic_frac": traffic / (join_ms / args.steps / 1e3) / 1e9 / peak if traffic and join_ms
-                         else None},
+                         else None,
+                         # the same DRAM traffic against the measured ceiling of random 32-byte sector reads
+                         "random_sector_peak": rpeak,
+                         "traffic_frac_of_random_peak": traffic / (join_ms / args.steps / 1e3) / 1e9 / rpeak["gbs"]
+                         if traffic and join_ms and rpeak else None},
             # the same join time against the per-level byte model of a breadth-first
             # table join over the same partial matches (rows read and written,
             # anchors' whole lists, adjacency scans per back edge): what the

@@ -76,8 +76,9 @@ WORKLOADS = {
     "rmat24": Workload("rmat24", "rmat", scale=24, avg_degree=16, labels=32, seed=1,
                        queries_file="tests/golden/workload_rmat24.json",
                        description="R-MAT(0.57,0.19,0.19,0.05) 2^24 vertices, avg degree 16, 32 Zipf labels, "
-                                   "256 4-5-vertex tree/sparse/dense walk queries of at most 10^7 embeddings "
-                                   "(the serving configuration)"),
+                                   "170 4-5-vertex sparse/dense walk queries of at most 10^7 embeddings "
+                                   "(the serving configuration; 34,384 draws filled 170 of 256 slots, no "
+                                   "tree stays within 10^7)"),
     "rmat22_k4to7": Workload("rmat22_k4to7", "rmat", scale=22, avg_degree=16, labels=32, seed=1,
                              queries_file="tests/golden/workload_rmat22_k4to7.json",
                              description="R-MAT(0.57,0.19,0.19,0.05) 2^22 vertices, avg degree 16, 32 Zipf labels, "
