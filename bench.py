@@ -215,7 +215,7 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
                     # submit -> admission, and admission -> result
                     "wait_p50_ms": wait[n // 2], "wait_p99_ms": wait[(99 * (n - 1)) // 100],
                     "run_p50_ms": run[n // 2], "run_p99_ms": run[(99 * (n - 1)) // 100],
-                    "slices": ss.slices, "bells": ss.bells,
+                    "slices": ss.slices, "bells": ss.bells, "admitted_live": ss.admitted_live,
                     "retired_in_slice": ss.retired_in_slice, "carried_tasks": ss.carried_tasks,
                     "slice_s": ss.slice_s, "between_s": ss.between_s})
     return out

@@ -237,7 +237,7 @@ __device__ __forceinline__ uint32_t group_candidates(const StepGroup &G, const F
 // groups of a phase differ in size by orders of magnitude (a frequent label's
 // core has millions of candidates, a rare one's a few), so the walk's warps
 // take chunks from one counter instead of a fixed share of blocks per group.
-__global__ void __launch_bounds__(1024) k_walk_plan(const StepGroup *__restrict__ groups, uint32_t ng,
+__global__ void __launch_bounds__(256) k_walk_plan(const StepGroup *__restrict__ groups, uint32_t ng,
                                                     const FilterQuery *__restrict__ qs,
                                                     uint32_t *__restrict__ chunk_start) {
   __shared__ uint32_t warp_sum[32];
@@ -771,7 +771,8 @@ smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const Filter
     po.lab_off = g.lab_off;
     po.lab_buckets = g.lab_buckets;
     uint32_t *cs = fd.chunk_start + fd.phase_first[p] + p;  // ng + 1 entries per phase
-    k_walk_plan<<<1, 1024, 0, s>>>(fd.groups + fd.phase_first[p], ng, d_qs, cs);
+    // 256 threads, so that a served request's plan fits beside a running join
+    k_walk_plan<<<1, 256, 0, s>>>(fd.groups + fd.phase_first[p], ng, d_qs, cs);
     SMG_CUDA(cudaGetLastError());
     // the phase's second zeroed counter hands out the chunks
     k_cluster_walk<<<num_sms * 8, 256, 0, s>>>(g.off, g.adj, fd.groups + fd.phase_first[p], ng, cs, po.count + 1,
@@ -781,6 +782,25 @@ smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const Filter
                                                 d_qs, po);
     SMG_CUDA(cudaGetLastError());
   }
+  return SMG_OK;
+}
+
+// Zeroes `bytes` (a multiple of 16) at p with 256-thread blocks: a server
+// zeroes an admitted request's buffers on its admission stream while the
+// join runs, and the driver's memset may not fit beside the join's blocks.
+__global__ void __launch_bounds__(256) k_zero(uint4 *p, uint64_t n16) {
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n16;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    p[i] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+smg_status launch_zero(void *p, size_t bytes, cudaStream_t s, int num_sms) {
+  if (!bytes) return SMG_OK;
+  if (bytes % 16 || reinterpret_cast<uintptr_t>(p) % 16) return fail(SMG_ERR_INTERNAL, "launch_zero: unaligned range");
+  const uint64_t n16 = bytes / 16;
+  const uint32_t blocks = static_cast<uint32_t>(std::min<uint64_t>((n16 + 255) / 256, static_cast<uint64_t>(num_sms) * 4));
+  k_zero<<<blocks, 256, 0, s>>>(static_cast<uint4 *>(p), n16);
+  SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }
 

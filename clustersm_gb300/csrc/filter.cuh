@@ -59,6 +59,8 @@ struct FilterDev {
 };
 
 smg_status launch_build_nlc(DevGraph &g, cudaStream_t s, int num_sms);
+// Zeroes bytes (a multiple of 16, 16-byte aligned) with 256-thread blocks.
+smg_status launch_zero(void *p, size_t bytes, cudaStream_t s, int num_sms);
 // Query constants (not the device pointers) of one plan.
 smg_status fill_filter_query(const Plan &P, const DevGraph &g, FilterQuery &fq);
 smg_status append_filter_steps(const Plan &P, uint32_t query_index, FilterBatch &fb);

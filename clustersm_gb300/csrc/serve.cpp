@@ -386,17 +386,22 @@ smg_status admit(smg_server *s, cudaStream_t st) {
     rc = smg::append_filter_steps(*sl.plan, i, fb);
     if (rc) return rc;
     hseed[i] = idx;
-    SMG_CUDA(cudaMemsetAsync(b.vmask, 0, fps[i].vmask, st));  // the filter writes candidates only
-    SMG_CUDA(cudaMemsetAsync(b.enc, 0, fps[i].enc, st));
-    SMG_CUDA(cudaMemsetAsync(b.cbits, 0, fps[i].cbits, st));
-    SMG_CUDA(cudaMemsetAsync(b.counters, 0, sizeof(smg::QCounters), st));
+    // the filter writes candidates only; zeroed by a kernel that fits beside
+    // a running join (live admission)
+    const int sms = s->ctx->num_sms;
+    rc = smg::launch_zero(b.vmask, fps[i].vmask, st, sms);
+    if (!rc) rc = smg::launch_zero(b.enc, fps[i].enc, st, sms);
+    if (!rc) rc = smg::launch_zero(b.cbits, fps[i].cbits, st, sms);
+    if (!rc) rc = smg::launch_zero(b.counters, sizeof(smg::QCounters), st, sms);
+    if (rc) return rc;
     SMG_CUDA(cudaMemcpyAsync(s->d_jq + idx, hj + i, sizeof(smg::JoinQuery), cudaMemcpyHostToDevice, st));
   }
   smg_status rc = s->fdev.upload(fb, st);
   if (rc) return rc;
   SMG_CUDA(cudaMemcpyAsync(s->d_fq_new, hf, n * sizeof(smg::FilterQuery), cudaMemcpyHostToDevice, st));
   SMG_CUDA(cudaMemcpyAsync(s->d_seed, hseed, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-  SMG_CUDA(cudaMemsetAsync(s->walk_count, 0, smg::kMaxWalkPhases * 2 * sizeof(unsigned int), st));
+  rc = smg::launch_zero(s->walk_count, smg::kMaxWalkPhases * 2 * sizeof(unsigned int), st, s->ctx->num_sms);
+  if (rc) return rc;
   rc = smg::launch_filter(g, s->d_fq_new, n, s->fdev, walk_overflow(s), st, s->ctx->num_sms);
   if (rc) return rc;
   smg::JoinLaunch jl = join_launch(s);
