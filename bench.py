@@ -605,8 +605,19 @@ def main():
             sdev = DeviceGraph.build(ctx, 1 << swl.scale, native.HostGraph.rmat_pairs(swl.scale, swl.avg_degree,
                                                                                       swl.seed),
                                      native.HostGraph.labels_for(1 << swl.scale, swl.labels, swl.seed))
+            splans = [Plan(q) for q in sq]
+            # the batch path on the same requests (about 1,024 per batch), the
+            # server's capacity to compare the sustained rates with
+            bplans = splans * max(1, 1024 // len(splans))
+            native.match_batch(ctx, sdev, bplans)
+            t0 = time.perf_counter()
+            bcounts, _ = native.match_batch(ctx, sdev, bplans)
+            batch_s = time.perf_counter() - t0
+            bwant = swant * max(1, 1024 // len(splans))
             serve = {"workload": swl.name, "description": swl.description,
-                     "rates": serving(ctx, sdev, [Plan(q) for q in sq], swant, rates)}
+                     "batch_qps": len(bplans) / batch_s,
+                     "batch_counts_ok": sum(int(c) == int(w) for c, w in zip(bcounts, bwant) if w is not None),
+                     "rates": serving(ctx, sdev, splans, swant, rates)}
             sdev.free()
         else:
             serve = {"workload": wl.name, "rates": serving(ctx, dev, plans, want, rates)}

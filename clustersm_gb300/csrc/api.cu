@@ -96,6 +96,13 @@ void drop_graph(smg_ctx *c) {
   c->graph_gen = ~0ull;
 }
 
+void release_batch_memory(smg_ctx *c) {
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
+  c->arena.~Arena();
+  new (&c->arena) Arena();
+}
+
 uint64_t time_limit_ns() {
   const char *s = std::getenv("SMG_TIME_LIMIT_S");
   double v = s ? std::atof(s) : 120.0;
@@ -194,10 +201,7 @@ void *smg_ctx_stream(smg_ctx *c) { return c ? static_cast<void *>(c->stream) : n
 void smg_close(smg_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
-  if (c->stream) cudaStreamSynchronize(c->stream);
-  drop_graph(c);
-  c->arena.~Arena();
-  new (&c->arena) Arena();
+  release_batch_memory(c);
   c->fdev.reset();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);

@@ -115,6 +115,10 @@ struct smg_graph {
 namespace smg {
 // Forgets the captured batch graph of a context.
 void drop_graph(smg_ctx *c);
+// Frees a context's batch scratch (the arena grows to what the largest batch
+// needed, up to all free memory) and the captured batch graph; the next batch
+// allocates again.
+void release_batch_memory(smg_ctx *c);
 // Device buffers holding one query's filter state and results.
 struct QueryBuffers {
   uint32_t *vmask = nullptr, *enc = nullptr, *cand = nullptr, *roots = nullptr;

@@ -24,7 +24,9 @@
 //     SMG_SLICE_MIN_MS (default 2 ms) have passed, when the host rings a
 //     doorbell in host-mapped memory: without live admission because
 //     requests are waiting and slots are free, with it when the queue has
-//     used half its slots.  At the end of a slice every warp writes the
+//     used half its slots, or when requests wait that no free slot or memory
+//     can take while slots retired in the slice are held (an admission batch
+//     of them, or any after 10 ms).  At the end of a slice every warp writes the
 //     unfinished part of its depth-first stack into the next slice's queue,
 //     and the untaken tasks follow;
 //   * a query is finished when its count of queued and running tasks reaches
@@ -487,6 +489,16 @@ smg_status live_step(smg_server *s) {
       s->admitting = true;
     }
   }
+  // Slots retired during the slice are held until it ends.  When requests
+  // still wait after the admission above (no free slot, or no memory), end
+  // the slice once an admission batch of slots is held, or any is held and
+  // the slice has run 10 ms, so that the next slice takes them.
+  if (open && !s->admitting && !s->bell_rung && !s->waiting.empty() && !s->freed_slots.empty() &&
+      (s->freed_slots.size() >= s->admit_batch || now_s() - s->slice_start_s > 0.010)) {
+    __atomic_store_n(s->h_bell, 1u, __ATOMIC_RELEASE);
+    s->bell_rung = true;
+    ++s->stats.bells;
+  }
   if (open && !s->admitting && s->waiting.empty() && s->running == 0)
     __atomic_store_n(s->h_hold, 0u, __ATOMIC_RELEASE);
   return SMG_OK;
@@ -566,6 +578,9 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   s->admit_batch = std::max<uint32_t>(1, static_cast<uint32_t>(env_ms("SMG_ADMIT_BATCH", s->cfg.max_inflight / 8.0)));
   const size_t tw = task_words(s.get());
   const uint32_t m = s->cfg.max_inflight;
+  // the context's batch scratch may hold the memory the server needs (it
+  // grows to what the largest batch used): free it first
+  if (free_b < s->cfg.memory_budget_bytes + (8ull << 30)) smg::release_batch_memory(c);
   SMG_CUDA(cudaMalloc(&s->pool_mem, s->cfg.memory_budget_bytes));
   s->pool.init(s->pool_mem, s->cfg.memory_budget_bytes);
   SMG_CUDA(cudaMalloc(&s->d_fq_new, m * sizeof(smg::FilterQuery)));
