@@ -335,15 +335,13 @@ __host__ __device__ inline uint32_t scalar_words(uint32_t K) { return (13 * K + 
 constexpr uint32_t kHoistCap = 256;
 constexpr uint32_t kHoistInvalid = 0xFFFFFFFFu;  // xlen: not built for this prefix
 constexpr uint32_t kHoistTooBig = 0xFFFFFFFEu;   // xlen: larger than kHoistCap
-//   wj, wc, we    per level, two window slots (see accept_window): back edge
-//                 (kWinFromL: its run lies in adjl), cursor and end
 __host__ __device__ inline uint32_t warp_words(uint32_t K) {
-  return scalar_words(K) + 2 * K + 32 * K + 7 * 32 + kHoistCap + 2 + 32 * K + 6 * K;
+  return scalar_words(K) + 2 * K + 32 * K + 7 * 32 + kHoistCap + 2 + 32 * K;
 }
 
 struct WarpView {
   uint32_t *m, *beg, *deg, *hub, *cur, *end, *bcnt, *bidx, *piv, *ord, *bmask, *slab, *lbk, *batch;
-  uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv, *xs, *xlen, *bpos, *wj, *wc, *we;
+  uint32_t *sv, *sbeg, *sdeg, *shub, *sbase, *spre, *spiv, *xs, *xlen, *bpos;
   uint32_t xcap = kHoistCap;  // entries xs holds (xs may be moved to a global buffer)
   const uint32_t **lbase;
   __device__ WarpView(uint32_t *W, uint32_t K) {
@@ -373,17 +371,12 @@ struct WarpView {
     xs = spiv + 32;
     xlen = xs + kHoistCap;
     bpos = xlen + 2;  // [K][32] list position of each batch entry
-    wj = bpos + 32 * K;
-    wc = wj + 2 * K;
-    we = wc + 2 * K;
   }
 };
 
 constexpr uint32_t kFromLabelIndex = 1u << 31;  // spiv flag: segment in adjl
 constexpr uint32_t kHoistScan = 1u << 30;       // spiv flag: keep entries found in the hoisted set
 constexpr uint32_t kHoistSet = 1u << 29;        // spiv flag: the segment is the hoisted set itself
-constexpr uint32_t kWinUnset = 0xFFFFFFFEu;     // wj: the level's window slots are not chosen yet
-constexpr uint32_t kWinFromL = 1u << 31;        // wj flag: the window's list is a run in adjl
 
 #ifdef SMG_CHECKED
 // Self-checking build: does `e` point into adj or adjl?
@@ -581,140 +574,6 @@ __device__ __forceinline__ uint32_t accept_multi(const WarpView &S, const JoinLa
     }
   }
   return live;
-}
-
-// Window probes.  A refill tests 32 consecutive entries of the level's list,
-// so their ids ascend over the lanes.  For a back neighbour without a hub
-// bitmap whose list (the run of the level's label, or its whole list) is not
-// much longer than the level's list, the warp walks that list once, 32
-// entries a load, beside the level's list: a cursor per level and back edge
-// stays at or below the next value asked, and each refill moves it past the
-// largest.  One coalesced load per 32 entries of the back neighbour's list
-// replaces a binary search per entry (a chain of dependent loads each).
-
-// Index of the first entry >= x in the sorted B[lo, hi) (hi when none), the
-// whole warp searching together: 32 segment ends per load, so a list of
-// 32^r entries takes r + 1 loads.  Every lane gets the same result.
-__device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t *B, uint32_t lo, uint32_t hi, uint32_t x,
-                                                     uint32_t lane, uint32_t &probes) {
-  while (lo < hi && hi - lo > 32) {
-    const uint32_t len = hi - lo, step = (len + 31) >> 5, s0 = lane * step;
-    bool below = false;
-    if (s0 < len) {
-      ++probes;
-      below = __ldg(B + lo + min(s0 + step, len) - 1) < x;
-    }
-    lo += __popc(__ballot_sync(0xFFFFFFFFu, below)) * step;  // those segments lie wholly below x
-    if (lo >= hi) return hi;
-    hi = min(hi, lo + step);
-  }
-  if (lo >= hi) return hi;
-  bool below = false;
-  if (lane < hi - lo) {
-    ++probes;
-    below = __ldg(B + lo + lane) < x;
-  }
-  return lo + __popc(__ballot_sync(0xFFFFFFFFu, below));
-}
-
-// Which lanes' values ws are in the sorted list B[c, e)?  ws ascends over the
-// lanes (0xFFFFFFFF past the list's end); `live` (non-zero) marks the lanes
-// asking.  On entry c is at most the index of the smallest asked value's
-// lower bound; on return it is past every entry <= the largest asked value.
-__device__ __forceinline__ uint32_t window_probe(const uint32_t *B, uint32_t &c, uint32_t e, uint32_t ws,
-                                                 uint32_t live, uint32_t lane, uint32_t &probes) {
-  const uint32_t wmin = __shfl_sync(0xFFFFFFFFu, ws, __ffs(live) - 1);
-  const uint32_t wmax = __shfl_sync(0xFFFFFFFFu, ws, 31 - __clz(live));
-  uint32_t found = 0;
-  while (c < e) {
-    const bool in = c + lane < e;
-    uint32_t b = 0xFFFFFFFFu;
-    if (in) {
-      ++probes;
-      b = __ldg(B + c + lane);
-    }
-    if (__ballot_sync(0xFFFFFFFFu, b < wmin) == 0xFFFFFFFFu) {
-      // the whole window lies below the values asked: search ahead
-      c = warp_lower_bound(B, c + 32, e, wmin, lane, probes);
-      continue;
-    }
-    // lower bound of b among the lanes' values, by shuffles
-    uint32_t pos = 0;
-#pragma unroll
-    for (uint32_t st = 16; st; st >>= 1)
-      if (__shfl_sync(0xFFFFFFFFu, ws, pos + st - 1) < b) pos += st;
-    const uint32_t at = __shfl_sync(0xFFFFFFFFu, ws, pos);  // every lane takes part
-    const bool hit = in && at == b;
-    found |= __reduce_or_sync(0xFFFFFFFFu, hit ? 1u << pos : 0u);
-    const uint32_t adv = __popc(__ballot_sync(0xFFFFFFFFu, b <= wmax));
-    c += adv;
-    if (adv < 32) break;
-  }
-  return found & live;
-}
-
-// Chooses the window slots of `level` on its first refill: up to two back
-// neighbours other than the pivot, without a hub bitmap, whose list the
-// level's label narrows them to is at most window_x8 / 8 times as long as the
-// pivot's (or 32 entries, whichever is longer).  Their cursors start at their
-// lists' starts.
-__device__ __forceinline__ void window_setup(WarpView &S, const JoinLaunch &p, bool use_labels, uint32_t level,
-                                             uint32_t lane) {
-  if (lane == 0) {
-    const uint32_t piv = S.piv[level];
-    const uint32_t plen = max(32u, run_len(p, S, use_labels, level, S.m[piv], S.deg[piv]));
-    uint32_t slot = 0;
-    for (uint32_t b = S.bmask[level] & ~(1u << piv); b && slot < 2; b &= b - 1) {
-      const uint32_t j = __ffs(b) - 1;
-      if (S.hub[j] != kNone) continue;  // a bitmap probe is one load
-      uint32_t len = 0;
-      const uint32_t *lst = scan_list(p, S, use_labels, level, S.m[j], S.beg[j], S.deg[j], len);
-      if (8ull * len > static_cast<uint64_t>(p.window_x8) * plen) continue;
-      const bool from_l = lst != p.adj + S.beg[j];
-      const uint32_t start = static_cast<uint32_t>(lst - (from_l ? p.adjl : p.adj));
-      S.wj[2 * level + slot] = j | (from_l ? kWinFromL : 0u);
-      S.wc[2 * level + slot] = start;
-      S.we[2 * level + slot] = start + len;
-      ++slot;
-    }
-    for (; slot < 2; ++slot) S.wj[2 * level + slot] = kNone;
-  }
-  __syncwarp();
-}
-
-// accept() for one refill with window probes: entry w of this lane (valid:
-// within the refill), the same tests in the same order, the back edges with
-// a window slot answered for the whole warp at once.
-__device__ __forceinline__ bool accept_window(WarpView &S, const JoinLaunch &p, const CandView &cv, bool use_labels,
-                                              uint32_t level, uint32_t w, bool valid, uint32_t lane,
-                                              uint32_t &probes) {
-  bool good = valid && SMG_DCHECK(w < p.n, 105, w, level) && cv.has(S.ord[level], w);
-  for (uint32_t b = S.slab[level]; b && good; b &= b - 1) good = S.m[__ffs(b) - 1] != w;
-  if (S.wj[2 * level] == kWinUnset) window_setup(S, p, use_labels, level, lane);
-  const uint32_t ws = valid ? w : 0xFFFFFFFFu;
-  uint32_t handled = 0;
-  for (uint32_t slot = 0; slot < 2; ++slot) {
-    const uint32_t ent = S.wj[2 * level + slot];
-    if (ent == kNone) break;
-    const uint32_t j = ent & 31u;
-    handled |= 1u << j;
-    const uint32_t live = __ballot_sync(0xFFFFFFFFu, good);
-    if (!live) break;  // nothing asked: the cursors stay valid for later values
-    uint32_t c = S.wc[2 * level + slot];
-    const uint32_t e = S.we[2 * level + slot];
-    if (!SMG_DCHECK(e <= p.m2 && c <= e, 117, c, e)) return false;
-    const uint32_t found = window_probe((ent & kWinFromL) ? p.adjl : p.adj, c, e, ws, live, lane, probes);
-    __syncwarp();
-    if (lane == 0) S.wc[2 * level + slot] = c;
-    good = good && ((found >> lane) & 1u);
-  }
-  __syncwarp();
-  const uint32_t bucket = use_labels ? S.lbk[level] : kNone;
-  for (uint32_t b = S.bmask[level] & ~(1u << S.piv[level]) & ~handled; b && good; b &= b - 1) {
-    const uint32_t j = __ffs(b) - 1;
-    good = is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes);
-  }
-  return good;
 }
 
 // A last-level list longer than the query's split length (split_len, default
@@ -1299,7 +1158,6 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         S.lbase[0] = Q.roots;
         S.cur[L0] = lo;
         S.end[L0] = hi;
-        S.wj[0] = kWinUnset;
       } else {
         const uint32_t pv = choose_pivot(p, S, Q.use_labels, L0);
         uint32_t len = 0;
@@ -1307,7 +1165,6 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         S.lbase[L0] = scan_list(p, S, Q.use_labels, L0, S.m[pv], S.beg[pv], S.deg[pv], len);
         S.cur[L0] = lo;
         S.end[L0] = hi == kNone ? len : min(hi, len);
-        S.wj[2 * L0] = kWinUnset;
         // a split-off batch candidate: its row was never expanded by the donor
         if (p.count_model && hi == kNone) model += 4ull * L0 + level_model(S, L0);
       }
@@ -1433,7 +1290,6 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
             S.lbase[nl] = scan_list(p, S, Q.use_labels, nl, S.m[pv], S.beg[pv], S.deg[pv], len);
             S.cur[nl] = 0;
             S.end[nl] = len;
-            S.wj[2 * nl] = kWinUnset;
             S.bcnt[nl] = 0;
             S.bidx[nl] = 0;
             if (nl == P) *S.xlen = kHoistInvalid;  // the prefix m[0..P-1] changed
@@ -1464,12 +1320,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
             if (SMG_DCHECK(w[i] < p.n, 112, w[i], level)) live |= 1u << i;
           }
         }
-        if (level != 0) {
-          if (kWays == 1 && p.window_x8)
-            live = accept_window(S, p, cv, Q.use_labels, level, w[0], lane < n, lane, probes) ? 1u : 0u;
-          else
-            live = accept_multi(S, p, cv, Q.use_labels, level, w, live, probes);
-        }
+        if (level != 0) live = accept_multi(S, p, cv, Q.use_labels, level, w, live, probes);
         uint32_t taken = 0, stop = n;
 #pragma unroll
         for (int i = 0; i < kWays; ++i) {
@@ -1714,23 +1565,11 @@ uint32_t hoist_scan_x8() {
   return v;
 }
 
-// Window probes of intermediate levels (SMG_WINDOW_RATIO, in eighths of the
-// pivot's list length; 0: off).
-uint32_t window_x8() {
-  static const uint32_t v = [] {
-    const char *e = std::getenv("SMG_WINDOW_RATIO");
-    const long c = e ? std::strtol(e, nullptr, 10) : 0;
-    return static_cast<uint32_t>(std::min(std::max(c, 0L), 1L << 20));
-  }();
-  return v;
-}
-
 smg_status launch_persistent(const JoinLaunch &jl_in, cudaStream_t s, int num_sms) {
   JoinLaunch jl = jl_in;
   jl.probe_runs = probe_runs() && jl.adjl != nullptr;
   jl.hoist = hoist_enabled();
   jl.hoist_scan_x8 = hoist_scan_x8();
-  jl.window_x8 = window_x8();
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);
   const JoinKernel kern = join_kernel(smem);
   if (smem > 48 * 1024)

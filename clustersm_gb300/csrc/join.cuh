@@ -55,10 +55,6 @@ struct JoinLaunch {
   // scanned when 8 x its length <= hoist_scan_x8 x |X|, else X is walked
   // (SMG_HOIST_SCAN_RATIO, in eighths; 8 walks the shorter side)
   uint32_t hoist_scan_x8;
-  // window probes of a refill (SMG_WINDOW_RATIO, in eighths; 0: off): a back
-  // neighbour's list at most window_x8 / 8 times as long as the pivot's is
-  // walked beside it instead of searched per entry
-  uint32_t window_x8;
   // per resident warp, room for a stored hoisted set of xcap entries (global
   // memory, [blocks x warps per block][xcap]); null: the warp's shared
   // memory, 256 entries

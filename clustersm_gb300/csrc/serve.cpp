@@ -25,8 +25,8 @@
 //     doorbell in host-mapped memory: without live admission because
 //     requests are waiting and slots are free, with it when the queue has
 //     used half its slots, or when requests wait that no free slot or memory
-//     can take while slots retired in the slice are held (an admission batch
-//     of them, or any after 10 ms).  At the end of a slice every warp writes the
+//     can take while at least as many requests retired in the slice are held
+//     as still run.  At the end of a slice every warp writes the
 //     unfinished part of its depth-first stack into the next slice's queue,
 //     and the untaken tasks follow;
 //   * a query is finished when its count of queued and running tasks reaches
@@ -491,10 +491,13 @@ smg_status live_step(smg_server *s) {
   }
   // Slots retired during the slice are held until it ends.  When requests
   // still wait after the admission above (no free slot, or no memory), end
-  // the slice once an admission batch of slots is held, or any is held and
-  // the slice has run 10 ms, so that the next slice takes them.
+  // the slice once at least as many requests are held as still run: ending
+  // a slice hands every running warp's stack back as tasks, so it pays only
+  // once a good part of the admitted work is done (ringing at every eighth
+  // of the slots held measured 449 queries/s under overload, against 634
+  // for no ringing at all).
   if (open && !s->admitting && !s->bell_rung && !s->waiting.empty() && !s->freed_slots.empty() &&
-      (s->freed_slots.size() >= s->admit_batch || now_s() - s->slice_start_s > 0.010)) {
+      s->freed_slots.size() >= s->running) {
     __atomic_store_n(s->h_bell, 1u, __ATOMIC_RELEASE);
     s->bell_rung = true;
     ++s->stats.bells;
