@@ -357,6 +357,7 @@ void smg_graph_free(smg_graph *G) {
   if (g.lverts) cudaFree(g.lverts);
   if (g.hub_of) cudaFree(g.hub_of);
   if (g.hub_bits) cudaFree(g.hub_bits);
+  if (g.adjr) cudaFree(g.adjr);
   if (g.adjl) cudaFree(g.adjl);
   if (g.lab_of) cudaFree(g.lab_of);
   if (g.lab_off) cudaFree(g.lab_off);
@@ -400,7 +401,10 @@ struct Chunk {
   std::vector<uint64_t> cand_total;
 };
 
-size_t cbits_bytes(const DevGraph &g, uint32_t k) { return static_cast<size_t>(k) * ((g.n + 31ull) / 32) * 4; }
+// k id-indexed rows, and k rank-indexed ones when the graph has entry ranks
+size_t cbits_bytes(const DevGraph &g, uint32_t k) {
+  return static_cast<size_t>(k) * ((g.n + 31ull) / 32) * 4 * (g.adjr ? 2 : 1);
+}
 
 }  // namespace
 
@@ -595,8 +599,10 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
   if (b.cbits) {
     f.cbits = b.cbits;  // k_collect writes them with the final masks
     f.cwords = (g.n + 31ull) / 32;
+    f.rank_rows = g.adjr ? 1u : 0u;
     j.cbits = b.cbits;
     j.cwords = (g.n + 31ull) / 32;
+    j.crow = g.adjr ? b.cbits + static_cast<size_t>(P.k) * j.cwords : nullptr;
     j.lastcnt = b.vmask;
     const uint32_t last_back = j.back_mask[P.k - 1];
     if (last_back && !(last_back & (last_back - 1))) {
@@ -893,7 +899,12 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
     // in collect; per candidate appended, per walked entry, per root
     st->filter_bytes += 4ull * g.n + lab * (4 + 8 + 32 + 4 + 4 + 4) + 8ull * q.initial_cands +
                         8ull * q.walk_entries + 4ull * q.num_roots;
-    st->filter_bytes += cbits_bytes(g, P.k);  // candidate bitmap rows written by collect
+    // candidate bitmap rows written by collect: k id-indexed rows of n bits,
+    // and with entry ranks k rank-indexed rows of the label's group size
+    st->filter_bytes += static_cast<uint64_t>(P.k) * ((g.n + 31ull) / 32) * 4;
+    if (g.adjr)
+      for (uint32_t u = 0; u < P.k; ++u)
+        if (P.label[u] < g.label_count.size()) st->filter_bytes += (g.label_count[P.label[u]] + 31) / 32 * 4;
   }
   st->tasks += hq->tasks_done;
   st->donations += hq->donations;

@@ -60,6 +60,12 @@ struct DevGraph {
   uint32_t *lab_of = nullptr;   // [n] row of the vertex's run table, or kNone
   uint32_t *lab_off = nullptr;  // [indexed][lab_buckets + 1]
   uint32_t lab_buckets = 0, lab_indexed = 0;
+  // When every bucket holds one label (at most kMaxLabels labels): the rank of
+  // each adjl entry within its label's vertex group (its position in lverts
+  // after the group's start).  A join level that scans a label run tests its
+  // entries in the query's rank-indexed candidate rows (JoinQuery::crow),
+  // whose rows are only as long as the label's group.  Null: not built.
+  uint32_t *adjr = nullptr;     // [2|E|]
   // Optional hub bitmap layout by label bucket (SMG_HUB_LAYOUT=label, with
   // the label index): the bit of neighbour w sits at word
   // bucket_word_off[bucket(w)] + lab_rank[w] / 32 of the hub's row, where
@@ -149,6 +155,9 @@ struct FilterQuery {
   unsigned long long *stat;       // [0] sum over u of final |C(u)|, [1] walk list entries
   uint32_t *cbits;               // the join's candidate bitmaps, written by collect (null: none)
   uint64_t cwords;               // words per bitmap row, ceil(n / 32)
+  // rank-indexed rows after the k id-indexed ones (cbits + (k + u) * cwords,
+  // bit r: the r-th vertex of u's label group is a candidate of u); 0: none
+  uint32_t rank_rows;
   // the query's distinct labels present in the graph: their vertex groups in
   // DevGraph::lverts ([grp_lo, grp_hi)) and the query vertices carrying them
   uint32_t ngrp;
@@ -169,6 +178,13 @@ struct JoinQuery {
   // candmask (caller-provided masks, smg_join_noalloc).
   uint32_t *cbits;
   uint64_t cwords;
+  // The same candidates by rank within the query vertex's label group:
+  // crow[u * cwords + r / 32] bit r % 32 for the r-th vertex of u's label
+  // (DevGraph::lverts order).  Only the first |label group| / 32 words of a
+  // row are used, so the rows a query's label runs touch are a fraction of
+  // cbits' (a tenth on average under Zipf labels) and stay in L2 longer.
+  // Null: every test reads cbits.
+  const uint32_t *crow;
   // Count-only runs with fast_last set: the last level's per-vertex
   // neighbour counts (see k_last_counts), written over candmask once cbits
   // holds the candidates.

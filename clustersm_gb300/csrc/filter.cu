@@ -76,15 +76,17 @@ __global__ void k_build_nlc(uint32_t n, const uint32_t *__restrict__ off, const 
 
 // ------------------------------------------------------------ initial filter
 // A query's vertices to visit: its label groups laid end to end.  Returns the
-// vertex at position t (< total) and the query vertices carrying its label.
+// vertex at position t (< total), the query vertices carrying its label and
+// its rank within its label's group.
 __device__ __forceinline__ uint32_t group_vertex(const FilterQuery &Q, const uint32_t *__restrict__ lverts, uint32_t t,
-                                                 uint32_t &same) {
+                                                 uint32_t &same, uint32_t &rank) {
   uint32_t i = 0;
   while (t >= Q.grp_hi[i] - Q.grp_lo[i]) {
     t -= Q.grp_hi[i] - Q.grp_lo[i];
     ++i;
   }
   same = Q.grp_mask[i];
+  rank = t;
   return lverts[Q.grp_lo[i] + t];
 }
 
@@ -113,8 +115,8 @@ __global__ void __launch_bounds__(256) k_nlc_filter(const uint32_t *__restrict__
     const uint32_t t = base + threadIdx.x;
     uint32_t mask = 0, v = 0;
     if (t < total) {
-      uint32_t same = 0;
-      v = group_vertex(Q, lverts, t, same);
+      uint32_t same = 0, rank = 0;
+      v = group_vertex(Q, lverts, t, same, rank);
       const uint32_t dv = off[v + 1] - off[v];
       const uint8_t *row = nlc + static_cast<size_t>(v) * stride;
       for (uint32_t b = same; b; b &= b - 1) {
@@ -453,8 +455,8 @@ __global__ void __launch_bounds__(256) k_collect(const uint32_t *__restrict__ lv
     const uint32_t t = base + threadIdx.x;
     uint32_t cm = 0, v = 0;
     if (t < total) {
-      uint32_t same = 0;
-      v = group_vertex(Q, lverts, t, same);
+      uint32_t same = 0, rank = 0;
+      v = group_vertex(Q, lverts, t, same, rank);
       const uint32_t m0 = vmask[v];
       for (uint32_t b = m0; b; b &= b - 1) {
         const uint32_t u = __ffs(b) - 1;
@@ -464,8 +466,12 @@ __global__ void __launch_bounds__(256) k_collect(const uint32_t *__restrict__ lv
       ncand += __popc(cm);
       // the join's candidate bitmaps (zero on entry): one bit per (u, v)
       if (Q.cbits)
-        for (uint32_t b = cm; b; b &= b - 1)
-          atomicOr(Q.cbits + (__ffs(b) - 1) * Q.cwords + (v >> 5), 1u << (v & 31));
+        for (uint32_t b = cm; b; b &= b - 1) {
+          const uint32_t u = __ffs(b) - 1;
+          atomicOr(Q.cbits + u * Q.cwords + (v >> 5), 1u << (v & 31));
+          // u's rank-indexed row: u carries v's label, so rank is v's place in that group
+          if (Q.rank_rows) atomicOr(Q.cbits + (Q.k + u) * Q.cwords + (rank >> 5), 1u << (rank & 31));
+        }
     }
     const bool is_root = (cm >> root) & 1u;
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, is_root);

@@ -202,9 +202,22 @@ struct CandView {
   const uint32_t *bits;  // cbits
   uint64_t words;        // cwords
   const uint32_t *mask;  // candmask
+  const uint32_t *crow;  // rank-indexed rows (null: none)
   __device__ __forceinline__ bool has(uint32_t u, uint32_t w) const {
     if (bits) return (__ldg(bits + u * words + (w >> 5)) >> (w & 31)) & 1u;
     return (__ldg(mask + w) >> u) & 1u;
+  }
+  // the same test for an entry of a label run of u's label, by its rank r
+  // within that label's group
+  __device__ __forceinline__ bool has_rank(uint32_t u, uint32_t r) const {
+    return (__ldg(crow + u * words + (r >> 5)) >> (r & 31)) & 1u;
+  }
+  // rank array of the entries of `list` when the tests can use the
+  // rank-indexed rows: the list is a label run in adjl (so every entry
+  // carries the level's label) and the graph has entry ranks; else null
+  __device__ __forceinline__ const uint32_t *ranks_of(const JoinLaunch &p, const uint32_t *list) const {
+    if (!crow || !p.adjr || list < p.adjl || list >= p.adjl + p.m2) return nullptr;
+    return p.adjr + (list - p.adjl);
   }
 };
 
@@ -505,7 +518,8 @@ constexpr int kWays = 1;
 // is resolved.
 __device__ __forceinline__ uint32_t accept_multi(const WarpView &S, const JoinLaunch &p, const CandView &cv,
                                                  bool use_labels, uint32_t level, const uint32_t (&w)[kWays],
-                                                 uint32_t live, uint32_t &probes) {
+                                                 const uint32_t (&r)[kWays], bool ranked, uint32_t live,
+                                                 uint32_t &probes) {
   const uint32_t u = S.ord[level];
   // candidate bits
   uint32_t word[kWays];
@@ -517,12 +531,15 @@ __device__ __forceinline__ uint32_t accept_multi(const WarpView &S, const JoinLa
         live &= ~(1u << i);
         continue;
       }
-      word[i] = cv.bits ? __ldg(cv.bits + u * cv.words + (w[i] >> 5)) : __ldg(cv.mask + w[i]);
+      if (ranked)
+        word[i] = __ldg(cv.crow + u * cv.words + (r[i] >> 5));
+      else
+        word[i] = cv.bits ? __ldg(cv.bits + u * cv.words + (w[i] >> 5)) : __ldg(cv.mask + w[i]);
     }
   }
 #pragma unroll
   for (int i = 0; i < kWays; ++i) {
-    const uint32_t bit = cv.bits ? (w[i] & 31) : u;
+    const uint32_t bit = ranked ? (r[i] & 31) : cv.bits ? (w[i] & 31) : u;
     if (!((word[i] >> bit) & 1u)) live &= ~(1u << i);
   }
   // injectivity against the matched vertices of the same label
@@ -647,6 +664,7 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
   scanned += hi - lo;
   const uint32_t u = S.ord[L], back = S.bmask[L] & ~(1u << piv), same = S.slab[L];
   const uint32_t lt = (1u << lane) - 1;
+  const uint32_t *rk = cv.ranks_of(p, base);
   unsigned long long cnt = 0;
   for (uint32_t t0 = lo; t0 < hi; t0 += 32) {
     const uint32_t t = t0 + lane;
@@ -654,7 +672,7 @@ __device__ unsigned long long last_level_range(WarpView &S, const JoinLaunch &p,
     uint32_t w = 0;
     if (t < hi) {
       w = __ldg(base + t);
-      good = SMG_DCHECK(w < p.n, 115, w, t) && cv.has(u, w);
+      good = SMG_DCHECK(w < p.n, 115, w, t) && (rk ? cv.has_rank(u, __ldg(rk + t)) : cv.has(u, w));
       for (uint32_t b = same; b && good; b &= b - 1) good = S.m[__ffs(b) - 1] != w;
       for (uint32_t b = back; b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
@@ -719,6 +737,7 @@ __device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery 
   const uint32_t *lst = scan_list(p, S, Q.use_labels, L, S.m[a], S.beg[a], S.deg[a], len);
   const uint32_t u = S.ord[L], same = S.slab[L] & ((1u << P) - 1), others = fixed & ~(1u << a);
   const uint32_t lt = (1u << lane) - 1;
+  const uint32_t *rk = cv.ranks_of(p, lst);
   uint32_t n = 0;
   scanned += len;
   for (uint32_t t0 = 0; t0 < len; t0 += 32) {
@@ -727,7 +746,7 @@ __device__ void build_hoisted(WarpView &S, const JoinLaunch &p, const JoinQuery 
     uint32_t w = 0;
     if (t < len) {
       w = __ldg(lst + t);
-      good = SMG_DCHECK(w < p.n, 116, w, t) && cv.has(u, w);
+      good = SMG_DCHECK(w < p.n, 116, w, t) && (rk ? cv.has_rank(u, __ldg(rk + t)) : cv.has(u, w));
       for (uint32_t b = same; b && good; b &= b - 1) good = S.m[__ffs(b) - 1] != w;
       for (uint32_t b = others; b && good; b &= b - 1) {
         const uint32_t j = __ffs(b) - 1;
@@ -908,7 +927,8 @@ __device__ unsigned long long last_level(WarpView &S, const JoinLaunch &p, const
         if (sp & kHoistScan) {  // a neighbour of v: is it in the hoisted set?
           good = in_adj && in_hoisted(S, xn, w);
         } else {
-          good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) && cv.has(u, w);
+          good = in_adj && SMG_DCHECK(w < p.n, 108, w, ai) &&
+                 ((sp & kFromLabelIndex) && cv.crow && p.adjr ? cv.has_rank(u, __ldg(p.adjr + ai)) : cv.has(u, w));
           for (uint32_t b = same; b && good; b &= b - 1) {
             const uint32_t j = __ffs(b) - 1;
             good = (j == P ? vi : S.m[j]) != w;
@@ -1161,6 +1181,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
     cv.bits = Q.cbits;
     cv.words = Q.cwords;
     cv.mask = Q.candmask;
+    cv.crow = Q.crow;
     unsigned long long cnt = 0;
     bool aborted = false, preempted = false;
     uint32_t iter = 0;  // steps of this task (work limit)
@@ -1325,17 +1346,20 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         const uint32_t n = min(32u * kWays, e - c);
         scanned += n;
         const uint32_t *base = S.lbase[level];
-        uint32_t w[kWays], live = 0;
+        const uint32_t *rk = level != 0 ? cv.ranks_of(p, base) : nullptr;
+        uint32_t w[kWays], r[kWays], live = 0;
 #pragma unroll
         for (int i = 0; i < kWays; ++i) {
           const uint32_t t = 32u * i + lane;
           w[i] = 0;
+          r[i] = 0;
           if (t < n && SMG_DCHECK(level == 0 ? c + t < *Q.num_roots : in_lists(p, base + c + t), 114, c + t, level)) {
             w[i] = __ldg(base + c + t);
+            if (rk) r[i] = __ldg(rk + c + t);
             if (SMG_DCHECK(w[i] < p.n, 112, w[i], level)) live |= 1u << i;
           }
         }
-        if (level != 0) live = accept_multi(S, p, cv, Q.use_labels, level, w, live, probes);
+        if (level != 0) live = accept_multi(S, p, cv, Q.use_labels, level, w, r, rk != nullptr, live, probes);
         uint32_t taken = 0, stop = n;
 #pragma unroll
         for (int i = 0; i < kWays; ++i) {
@@ -1499,6 +1523,7 @@ void set_graph(JoinLaunch &jl, const DevGraph &g) {
   jl.lab_of = g.lab_of;
   jl.lab_off = g.lab_off;
   jl.lab_buckets = g.lab_buckets;
+  jl.adjr = g.adjr;
   jl.label = g.label;
   jl.lverts = g.lverts;
   jl.lab_rank = g.hub_by_label ? g.lab_rank : nullptr;
@@ -1699,12 +1724,29 @@ smg_status build_label_index(DevGraph &g, const uint64_t *offsets, const uint32_
     SMG_CUDA(cudaMemcpyAsync(g.bucket_word_off, bwo.data(), (B + 1) * 4, cudaMemcpyHostToDevice, s));
     g.bytes += static_cast<size_t>(n) * 4 + (B + 1) * 4;
   }
+  // each entry's rank within its label's vertex group (ids ascending, as
+  // lverts orders them), when every bucket is one label; SMG_RANK_ROWS=0
+  // leaves it out (every candidate test reads the id-indexed rows)
+  std::vector<uint32_t> adjr;
+  const char *rr = std::getenv("SMG_RANK_ROWS");
+  if (g.num_labels <= B && !(rr && std::string(rr) == "0")) {
+    std::vector<uint32_t> lrank(n), cnt(B, 0);
+    for (uint32_t v = 0; v < n; ++v) lrank[v] = cnt[labels[v]]++;
+    adjr.resize(g.m2);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < static_cast<int64_t>(g.m2); ++e) adjr[e] = lrank[adjl[e]];
+  }
   SMG_CUDA(cudaMalloc(&g.adjl, g.m2 * 4));
   SMG_CUDA(cudaMalloc(&g.lab_of, static_cast<size_t>(n) * 4));
   SMG_CUDA(cudaMalloc(&g.lab_off, lab_off.size() * 4));
   SMG_CUDA(cudaMemcpyAsync(g.adjl, adjl.data(), g.m2 * 4, cudaMemcpyHostToDevice, s));
   SMG_CUDA(cudaMemcpyAsync(g.lab_of, lab_of.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, s));
   SMG_CUDA(cudaMemcpyAsync(g.lab_off, lab_off.data(), lab_off.size() * 4, cudaMemcpyHostToDevice, s));
+  if (!adjr.empty()) {
+    SMG_CUDA(cudaMalloc(&g.adjr, g.m2 * 4));
+    SMG_CUDA(cudaMemcpyAsync(g.adjr, adjr.data(), g.m2 * 4, cudaMemcpyHostToDevice, s));
+    g.bytes += g.m2 * 4;
+  }
   SMG_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
   g.bytes += g.m2 * 4 + static_cast<size_t>(n) * 4 + lab_off.size() * 4;
   return SMG_OK;

@@ -46,6 +46,7 @@ struct JoinLaunch {
   const uint32_t *adjl;      // label index (DevGraph::adjl, lab_of, lab_off)
   const uint32_t *lab_of, *lab_off;
   uint32_t lab_buckets;
+  const uint32_t *adjr;      // rank of each adjl entry within its label (DevGraph::adjr; null: none)
   const uint32_t *label;     // vertex labels (bucket of a probed vertex without a level bucket)
   const uint32_t *lverts;    // vertex ids grouped by label (DevGraph::lverts)
   const uint32_t *lab_rank, *bucket_word_off;  // hub bitmap layout by label (null: by id)
