@@ -207,14 +207,16 @@ def test_other_join_orders_give_same_counts(ctx, mode):
     assert r.returncode == 0, r.stdout + r.stderr
 
 
-@pytest.mark.parametrize("min_degree,enabled", [("1", "1"), ("64", "0")])
-def test_label_index_every_vertex_or_none(ctx, monkeypatch, min_degree, enabled):
+@pytest.mark.parametrize("min_degree,enabled,rank_rows", [("1", "1", "1"), ("1", "1", "0"), ("64", "0", "1")])
+def test_label_index_every_vertex_or_none(ctx, monkeypatch, min_degree, enabled, rank_rows):
     """The label index (neighbour lists ordered by label, with per-label run
-    tables) given to every vertex, and left out: cluster bitmaps stay
-    bit-exact and counts equal the oracle's either way.  The settings are read
-    when a graph is uploaded."""
+    tables) given to every vertex, and left out; with every vertex indexed,
+    the candidate tests of label-run entries by rank (the default) and by id:
+    cluster bitmaps stay bit-exact and counts equal the oracle's either way.
+    The settings are read when a graph is uploaded."""
     monkeypatch.setenv("SMG_LABEL_INDEX_MIN_DEGREE", min_degree)
     monkeypatch.setenv("SMG_LABEL_INDEX", enabled)
+    monkeypatch.setenv("SMG_RANK_ROWS", rank_rows)
     host = HostGraph.rmat(12, 16, 8, seed=7)
     dev = DeviceGraph(ctx, host)
     checked = 0
