@@ -511,7 +511,8 @@ def main():
     if not args.no_tune:  # setup, outside the timed region
         t_tune = time.perf_counter()
         tuning = {"classes": [{"shape_class": e.shape_class, "root_chunk": e.root_chunk, "donate_min": e.donate_min,
-                               "split_len": e.split_len, "hoist_cap": e.hoist_cap, "samples": e.samples,
+                               "split_len": e.split_len, "hoist_cap": e.hoist_cap, "bfs_depth": e.bfs_depth,
+                               "samples": e.samples,
                                "best_ms": e.best_ms, "default_ms": e.default_ms}
                               for e in native.autotune(ctx, dev, plans) if e.samples]}
         tuning["seconds"] = time.perf_counter() - t_tune
@@ -529,7 +530,8 @@ def main():
         native.match_batch(ctx, dev, plans, profile=True)
 
     step_ms, join_ms, filt_ms, jbytes, fbytes, launches = [], 0.0, 0.0, 0, 0, 0
-    work = {"scanned": 0, "descents": 0, "probes": 0, "last_count_entries": 0, "donations": 0, "tasks": 0}
+    work = {"scanned": 0, "descents": 0, "probes": 0, "last_count_entries": 0, "donations": 0, "bfs_tasks": 0,
+            "tasks": 0}
     h2d = d2h = 0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):

@@ -763,6 +763,7 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
       const TuneSetting &t = o.tuning[plan_class(P)];
       if (t.valid) apply_tuning(t, hj[i]);
     }
+    if (o.bfs_depth) hj[i].bfs_depth = o.bfs_depth;
     st = append_filter_steps(P, i, fb);
     if (st) return st;
   }
@@ -791,6 +792,16 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
   jl.root_chunk = o.root_chunk;
   jl.max_seed_tasks = seed_tasks(c, o, nq);
   jl.donate_min = 2;
+  // breadth-first levels may queue a few tasks per resident join warp beyond
+  // the root tasks (SMG_BFS_SLOTS_PER_WARP, default 16), at most half the
+  // queue: enough to spread every query's first levels over the grid, while
+  // the deeper levels stay depth-first and split on demand
+  static const uint64_t per_warp = [] {
+    const char *e = std::getenv("SMG_BFS_SLOTS_PER_WARP");
+    return static_cast<uint64_t>(e ? std::max(0L, std::atol(e)) : 16L);
+  }();
+  jl.bfs_budget = std::min<uint64_t>(ch.cap / 2, static_cast<uint64_t>(nq) * jl.max_seed_tasks +
+                                                     per_warp * 32u * static_cast<uint64_t>(c->num_sms));
   jl.time_limit_ns = time_limit_ns();
   jl.emit = ch.emb != nullptr;
   jl.xbuf = ch.xbuf;
@@ -912,6 +923,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
   }
   st->tasks += hq->tasks_done;
   st->donations += hq->donations;
+  st->bfs_tasks += hq->bfs_tasks;
   st->scanned += hq->scanned;
   st->descents += hq->descents;
   st->probes += hq->probes;
@@ -989,6 +1001,7 @@ smg_status run_queries(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.work_limit)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.profile)));
       key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.model)));
+      key.push_back(reinterpret_cast<const void *>(static_cast<uintptr_t>(o.bfs_depth)));
       for (uint32_t i = 0; i < nq; ++i) key.push_back(plans[i]);
     }
     s = run_chunk(c, g, plans, ch, o, out, st, key.empty() ? nullptr : &key);
@@ -1012,6 +1025,7 @@ smg_status smg_match(smg_ctx *c, const smg_graph *G, const smg_plan *p, const sm
   if (opts) {
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
+    o.bfs_depth = opts->bfs_depth;
     o.count_limit = opts->max_count;
     o.work_limit = opts->max_work;
     if (opts->flags & SMG_FLAG_EMIT) {
@@ -1055,6 +1069,7 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
   if (opts) {
     o.profile = (opts->flags & SMG_FLAG_PROFILE) != 0;
     o.root_chunk = opts->root_chunk;
+    o.bfs_depth = opts->bfs_depth;
     o.count_limit = opts->max_count;
     o.work_limit = opts->max_work;
     o.use_graph = (opts->flags & SMG_FLAG_NO_GRAPH) == 0;
@@ -1086,6 +1101,7 @@ smg_status smg_match_batch(smg_ctx *c, const smg_graph *G, const smg_plan *const
     stats->probes = st.probes;
     stats->last_count_entries = st.last_count_entries;
     stats->donations = st.donations;
+    stats->bfs_tasks = st.bfs_tasks;
     stats->model_bytes = st.model_bytes;
   }
   return SMG_OK;
@@ -1139,6 +1155,7 @@ smg_status smg_set_tuning(smg_ctx *c, const smg_tune_entry *e, uint32_t n) {
     t.donate_min = e[i].donate_min;
     t.split_len = e[i].split_len;
     t.hoist_cap = e[i].hoist_cap;
+    t.bfs_depth = e[i].bfs_depth;
     t.valid = e[i].samples > 0;
   }
   ++c->run_gen;  // the settings are staged into the query records: a captured batch is stale
@@ -1152,6 +1169,7 @@ smg_status smg_autotune(smg_ctx *c, const smg_graph *G, const smg_plan *const *p
   static const uint32_t kDonate[] = {2, 33, 129};
   static const uint32_t kSplits[] = {8192, 2048, 32768};
   static const uint32_t kHoists[] = {4096, 1024, 256};
+  static const uint32_t kBfs[] = {0, 2, 3};
   std::vector<std::vector<const Plan *>> by_class(SMG_TUNE_CLASSES);
   for (uint32_t i = 0; i < n; ++i)
     if (plans[i] && by_class[plan_class(plans[i]->p)].size() < 32) by_class[plan_class(plans[i]->p)].push_back(&plans[i]->p);
@@ -1182,9 +1200,10 @@ smg_status smg_autotune(smg_ctx *c, const smg_graph *G, const smg_plan *const *p
       best.donate_min = kDonate[0];
       best.split_len = kSplits[0];
       best.hoist_cap = kHoists[0];
+      best.bfs_depth = kBfs[0];
       float best_ms = -1.f;
       // one knob group at a time, each from the best of the groups before
-      for (int group = 0; group < 3; ++group) {
+      for (int group = 0; group < 4; ++group) {
         std::vector<TuneSetting> cands;
         if (group == 0) {
           for (uint32_t rc : kChunks)
@@ -1195,9 +1214,10 @@ smg_status smg_autotune(smg_ctx *c, const smg_graph *G, const smg_plan *const *p
               cands.push_back(t);
             }
         } else {
-          for (uint32_t v : group == 1 ? kSplits : kHoists) {
+          const uint32_t *vals = group == 1 ? kSplits : group == 2 ? kHoists : kBfs;
+          for (int vi = 0; vi < 3; ++vi) {
             TuneSetting t = best;
-            (group == 1 ? t.split_len : t.hoist_cap) = v;
+            (group == 1 ? t.split_len : group == 2 ? t.hoist_cap : t.bfs_depth) = vals[vi];
             cands.push_back(t);
           }
         }
@@ -1221,6 +1241,7 @@ smg_status smg_autotune(smg_ctx *c, const smg_graph *G, const smg_plan *const *p
       e.donate_min = best.donate_min;
       e.split_len = best.split_len;
       e.hoist_cap = best.hoist_cap;
+      e.bfs_depth = best.bfs_depth;
       e.samples = static_cast<uint32_t>(sample.size());
       e.best_ms = best_ms;
       TuneSetting &t = c->tuning[cls];

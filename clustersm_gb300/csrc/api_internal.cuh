@@ -48,7 +48,7 @@ uint64_t time_limit_ns();
 
 // Options of one run (plain path: one query; batched: many).
 struct TuneSetting {
-  uint32_t root_chunk = 0, donate_min = 0, split_len = 0, hoist_cap = 0;
+  uint32_t root_chunk = 0, donate_min = 0, split_len = 0, hoist_cap = 0, bfs_depth = 0;
   bool valid = false;
 };
 // The tuned knobs of a shape class into a query's join record.
@@ -57,6 +57,7 @@ inline void apply_tuning(const TuneSetting &t, JoinQuery &j) {
   j.donate_min = t.donate_min;
   j.split_len = t.split_len;
   j.hoist_cap = t.hoist_cap;
+  j.bfs_depth = t.bfs_depth;
 }
 uint32_t plan_class(const Plan &P);
 
@@ -71,6 +72,7 @@ struct RunOpts {
   uint64_t count_limit = 0;      // 0: none
   uint64_t work_limit = 0;       // 0: none
   bool model = false;            // count the breadth-first byte model
+  uint32_t bfs_depth = 0;        // 0: the tuned depth (none when untuned)
 };
 
 struct QueryOut {
@@ -82,6 +84,7 @@ struct QueryOut {
 struct RunStats {
   float filter_ms = 0, join_ms = 0;
   uint64_t tasks = 0, donations = 0, scanned = 0, descents = 0, probes = 0, last_count_entries = 0;
+  uint64_t bfs_tasks = 0;
   uint64_t model_bytes = 0;
   uint64_t filter_bytes = 0, join_bytes = 0;
   uint64_t launches = 0, h2d = 0, d2h = 0;

@@ -204,6 +204,12 @@ struct JoinQuery {
   uint32_t donate_min;        // shortest list worth splitting off (0: launch default)
   uint32_t split_len;         // last-level lists are cut into slices this long (0: 8,192)
   uint32_t hoist_cap;         // stored hoisted sets hold at most this many (0: the warp's buffer)
+  // Breadth-first prefix: a warp that fills a batch of accepted candidates
+  // at a level below bfs_depth (and below the last two levels) queues every
+  // one as a task instead of descending into it, while the launch's
+  // breadth-first budget of queue slots lasts; deeper levels run depth-first.
+  // 0: depth-first from the root tasks.
+  uint32_t bfs_depth;
   // Completion notice (serving; null: none).  The warp that finishes the
   // query's last task writes the final count to done_count and then `gen` to
   // done_gen, both in host-mapped memory, so the host sees the result while

@@ -26,6 +26,11 @@
 //    the level before it (a segmented scan), so short lists fill the warp;
 //  * a warp with a long remaining list donates half of it to the queue while
 //    more warps wait than tasks are queued (work splitting for hubs);
+//  * the first JoinQuery::bfs_depth levels may run breadth-first, as the
+//    reference's join does for every level: a warp queues each batch of
+//    accepted candidates as tasks one level deeper instead of descending,
+//    within a bounded number of queue slots (JoinLaunch::bfs_budget), so the
+//    frontier kept in memory stays bounded and deeper levels run depth-first;
 //  * every wait is bounded: a claimed-but-unpublished task, an idle grid and
 //    the whole run have time limits after which the kernel records an error
 //    and returns.
@@ -1028,6 +1033,49 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, unsigne
   return pushed != 0;
 }
 
+// Breadth-first level: the batch of `taken` accepted candidates of `level`
+// (< P) becomes `taken` tasks one level deeper (prefix m[0..level-1] plus the
+// candidate, the whole list of the next level), appended behind every task
+// queued so far, instead of being descended into one by one.  Only while the
+// queue's tail stays within the launch's breadth-first budget: past it the
+// warp keeps its batch and goes on depth-first, so the frontier held in the
+// queue is bounded.  Returns true when the batch was queued.
+__device__ __noinline__ bool bfs_push(const WarpView &S, const JoinLaunch &p, uint32_t q, unsigned long long *qpending,
+                         uint32_t level, uint32_t taken, uint32_t lane) {
+  QueueState *qs = p.qs;
+  unsigned long long first = 0;
+  int ok = 0;
+  if (lane == 0 && !*reinterpret_cast<volatile int *>(&qs->closing) && vload(qs->tail) + taken <= p.bfs_budget) {
+    first = atomicAdd(&qs->tail.v, static_cast<unsigned long long>(taken));
+    if (first + taken <= p.cap) {
+      ok = 1;
+      atomicAdd(&qs->pending.v, static_cast<unsigned long long>(taken));
+      atomicAdd(qpending, static_cast<unsigned long long>(taken));
+    } else {
+      // no room: the slot numbers taken stay unpublished and are never waited
+      // for beyond the end of the run (their tickets see pending reach zero)
+      atomicExch(&qs->full, 1);
+    }
+  }
+  ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+  if (!ok) return false;
+  first = __shfl_sync(0xFFFFFFFFu, first, 0);
+  if (lane < taken) {
+    uint32_t *T = p.tasks + (first + lane) * (4 + p.kmax);
+    T[0] = q;
+    T[1] = level + 1;
+    T[2] = 0;
+    T[3] = kNone;
+    for (uint32_t j = 0; j < level; ++j) T[4 + j] = S.m[j];
+    T[4 + level] = S.batch[level * 32 + lane];
+    __threadfence();
+    atomicExch(p.ready + first + lane, 1u);
+  }
+  if (lane == 0) atomicAdd(&qs->bfs_tasks, static_cast<unsigned long long>(taken));
+  __syncwarp();
+  return true;
+}
+
 // End of a time slice: every part of this warp's stack that is not done
 // becomes a task of the next slice's queue: the unscanned rest of each level's
 // list, and each untried batch candidate (as a task one level deeper).  The
@@ -1378,6 +1426,13 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
           }
         }
         __syncwarp();
+        // a breadth-first level queues the whole batch (one task per
+        // candidate) and goes on scanning its list
+        if (taken && p.bfs_budget && level < P && level < Q.bfs_depth &&
+            bfs_push(S, p, q, Q.pending, level, taken, lane)) {
+          descents += taken;
+          taken = 0;
+        }
         if (lane == 0) {
           S.bcnt[level] = taken;
           S.bidx[level] = 0;

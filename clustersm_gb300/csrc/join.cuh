@@ -25,6 +25,7 @@ struct QueueState {
   // matches (JoinLaunch::count_model; the per-level model of the join's
   // minimum traffic)
   unsigned long long model_bytes;
+  unsigned long long bfs_tasks;  // tasks queued by breadth-first levels (JoinQuery::bfs_depth)
   int error;  // JOIN_ERR_* below, first one wins
   int abort;  // set on error or deadline: every warp leaves
   int full;   // a donation found the queue full (load balance only)
@@ -73,6 +74,11 @@ struct JoinLaunch {
   uint32_t root_chunk;       // 0: derive from max_seed_tasks
   uint32_t max_seed_tasks;   // initial tasks per query at most
   uint32_t donate_min;       // shortest remaining list worth donating
+  // Queue slots breadth-first levels may fill: a warp queues a batch of
+  // partial matches only while the tail stays within this many slots, else
+  // it descends into them itself, so the breadth-first frontier is bounded
+  // by the queue (0: no breadth-first levels in this launch).
+  uint64_t bfs_budget;
   uint64_t time_limit_ns;    // device-side deadline for the whole run
   int emit;
   // Time-sliced runs (serving).  A slice closes after slice_ns, or after

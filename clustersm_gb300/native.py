@@ -61,7 +61,7 @@ class PlanView(C.Structure):
 
 
 class MatchOpts(C.Structure):
-    _fields_ = [("flags", C.c_uint32), ("reserved0", C.c_uint32), ("root_chunk", C.c_uint32),
+    _fields_ = [("flags", C.c_uint32), ("bfs_depth", C.c_uint32), ("root_chunk", C.c_uint32),
                 ("reserved", C.c_uint32), ("max_embeddings", C.c_uint64), ("embeddings", u32p),
                 ("max_count", C.c_uint64), ("max_work", C.c_uint64)]
 
@@ -80,13 +80,14 @@ class BatchStats(C.Structure):
                 ("d2h_bytes", C.c_uint64), ("filter_bytes", C.c_uint64), ("join_bytes", C.c_uint64),
                 ("chunks", C.c_uint32), ("reserved", C.c_uint32), ("scanned", C.c_uint64),
                 ("descents", C.c_uint64), ("probes", C.c_uint64), ("last_count_entries", C.c_uint64),
-                ("donations", C.c_uint64), ("model_bytes", C.c_uint64)]
+                ("donations", C.c_uint64), ("model_bytes", C.c_uint64), ("bfs_tasks", C.c_uint64)]
 
 
 class TuneEntry(C.Structure):
     _fields_ = [("shape_class", C.c_uint32), ("root_chunk", C.c_uint32), ("donate_min", C.c_uint32),
                 ("samples", C.c_uint32), ("best_ms", C.c_float), ("default_ms", C.c_float),
-                ("split_len", C.c_uint32), ("hoist_cap", C.c_uint32)]
+                ("split_len", C.c_uint32), ("hoist_cap", C.c_uint32), ("bfs_depth", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class GraphStats(C.Structure):
@@ -454,9 +455,10 @@ class DeviceGraph:
 
 
 def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=False,
-          root_chunk=0, max_count=0, max_work=0):
+          root_chunk=0, max_count=0, max_work=0, bfs_depth=0):
     """Plain path.  Returns (MatchResult, embeddings array or None)."""
     opts = MatchOpts()
+    opts.bfs_depth = bfs_depth
     opts.max_count = max_count
     opts.max_work = max_work
     opts.flags = (FLAG_EMIT if emit else 0) | (FLAG_PROFILE if profile else 0)
@@ -474,7 +476,7 @@ def match(ctx: Context, graph: DeviceGraph, plan: Plan, emit: int = 0, profile=F
 
 
 def match_batch(ctx: Context, graph: DeviceGraph, plans, root_chunk=0, profile=False, max_count=0,
-                use_graph=True, max_work=0, model=False):
+                use_graph=True, max_work=0, model=False, bfs_depth=0):
     """Batched path.  Returns (counts, BatchStats); with max_count or
     max_work, queries over a limit report 2**64-1."""
     n = len(plans)
@@ -483,6 +485,7 @@ def match_batch(ctx: Context, graph: DeviceGraph, plans, root_chunk=0, profile=F
     opts = MatchOpts()
     opts.flags = (FLAG_PROFILE if profile else 0) | (0 if use_graph else FLAG_NO_GRAPH) | (FLAG_MODEL if model else 0)
     opts.root_chunk = root_chunk
+    opts.bfs_depth = bfs_depth
     opts.max_count = max_count
     opts.max_work = max_work
     st = BatchStats()

@@ -252,8 +252,15 @@ smg_status smg_graph_get_stats(const smg_graph *g, smg_graph_stats *out);
 
 typedef struct smg_match_opts {
   uint32_t flags;
-  uint32_t reserved0;     /* must be 0 (the join is depth-first from a
-                             work queue; it has no breadth-first phase)   */
+  uint32_t bfs_depth;     /* breadth-first levels before the join turns
+                             depth-first: a warp queues every partial
+                             match of the first bfs_depth levels as a
+                             task (within half of the task queue; past
+                             that it descends itself); 0 = the tuned
+                             depth of the query's shape class, none when
+                             untuned.  Counts do not depend on it.  The
+                             reference joins every level breadth-first
+                             (join.cu:290-435).                            */
   uint32_t root_chunk;    /* root candidates per initial task; 0 = auto    */
   uint32_t reserved;
   uint64_t max_embeddings; /* rows of k ids the embeddings buffer can hold */
@@ -317,6 +324,7 @@ typedef struct smg_batch_stats {
                                 degree + (8 + 4 x degree) per other back
                                 edge, plus 4r written where a row is made;
                                 0 otherwise                               */
+  uint64_t bfs_tasks;        /* tasks queued by breadth-first levels       */
 } smg_batch_stats;
 smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
                            const smg_plan *const *plans, uint32_t n,
@@ -330,7 +338,8 @@ smg_status smg_match_batch(smg_ctx *ctx, const smg_graph *g,
  * settings, one knob group at a time from the defaults: root candidates per
  * seeded task x shortest list worth splitting off to an idle warp (3 x 3),
  * then the slice length of long last-level lists (2,048 / 8,192 / 32,768),
- * then the cap on stored hoisted sets (256 / 1,024 / 4,096 entries).  It
+ * then the cap on stored hoisted sets (256 / 1,024 / 4,096 entries), then
+ * the breadth-first depth before the join turns depth-first (0 / 2 / 3).  It
  * keeps the fastest setting per class in the context and reports it; later
  * smg_match / smg_match_batch calls and servers on this context apply it. */
 #define SMG_TUNE_CLASSES 12u
@@ -343,6 +352,8 @@ typedef struct smg_tune_entry {
   float default_ms;  /* device time of the sample under the default setting */
   uint32_t split_len; /* last-level list slice length (0: 8,192)           */
   uint32_t hoist_cap; /* entries of a stored hoisted set (0: the warp's buffer) */
+  uint32_t bfs_depth; /* breadth-first levels before depth-first (0: none) */
+  uint32_t reserved;
 } smg_tune_entry;
 smg_status smg_autotune(smg_ctx *ctx, const smg_graph *g, const smg_plan *const *plans, uint32_t n,
                         smg_tune_entry *out /* [SMG_TUNE_CLASSES] or NULL */);

@@ -84,6 +84,9 @@ struct Matcher {
   uint64_t *budget_used = nullptr;
   uint64_t budget = 0, local = 0;
   bool aborted = false;
+  // level 1 scans only entries [l1_lo, l1_hi) of the root's list (its only
+  // back neighbour is the root), so that one root's work can be split
+  uint64_t l1_lo = 0, l1_hi = ~0ull;
 
   bool ok_vertex(uint32_t lvl, uint32_t v) const {
     uint32_t u = Q.order[lvl];
@@ -106,7 +109,12 @@ struct Matcher {
       }
     }
     const uint32_t pv = m[pivot];
-    for (uint64_t e = g->offsets[pv]; e < g->offsets[pv + 1]; ++e) {
+    uint64_t e0 = g->offsets[pv], e1 = g->offsets[pv + 1];
+    if (lvl == 1) {
+      e1 = std::min(e1, e0 + std::min(l1_hi, e1 - e0));
+      e0 += std::min(l1_lo, e1 - e0);
+    }
+    for (uint64_t e = e0; e < e1; ++e) {
       uint32_t w = g->neighbors[e];
       if (!ok_vertex(lvl, w)) continue;
       bool good = true;
@@ -149,10 +157,29 @@ uint64_t count_range(const smg_csr *g, const QueryInfo &Q, const uint32_t *candm
 #else
   nt = 1;
 #endif
+  // units of work: a root, or a slice of a long root list at level 1 (the
+  // counts of disjoint slices add up), so that hub roots spread over threads
+  constexpr uint64_t kSlice = 256;
+  struct Unit {
+    uint32_t root;
+    uint64_t lo, hi;
+  };
+  std::vector<Unit> units;
+  for (uint64_t r = lo; r < hi; ++r) {
+    const uint32_t v = roots[r];
+    const uint64_t d = g->offsets[v + 1] - g->offsets[v];
+    if (d <= 2 * kSlice) {
+      units.push_back({v, 0, ~0ull});
+    } else {
+      for (uint64_t a = 0; a < d; a += kSlice) units.push_back({v, a, std::min(d, a + kSlice)});
+    }
+  }
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : total) num_threads(nt)
-  for (int64_t r = static_cast<int64_t>(lo); r < static_cast<int64_t>(hi); ++r) {
+  for (int64_t i = 0; i < static_cast<int64_t>(units.size()); ++i) {
     Matcher mt{g, Q, candmask};
-    mt.m[0] = roots[r];
+    mt.m[0] = units[i].root;
+    mt.l1_lo = units[i].lo;
+    mt.l1_hi = units[i].hi;
     mt.extend(1);
     total += mt.count;
   }

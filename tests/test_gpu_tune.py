@@ -21,6 +21,7 @@ def test_autotune_keeps_counts():
         assert e.best_ms <= e.default_ms + 1e-6
         assert e.root_chunk in (1, 8, 64) and e.donate_min in (2, 33, 129)
         assert e.split_len in (2048, 8192, 32768) and e.hoist_cap in (256, 1024, 4096)
+        assert e.bfs_depth in (0, 2, 3)
     counts, _ = native.match_batch(ctx, dev, plans)
     assert counts.tolist() == want
     ctx.close()
