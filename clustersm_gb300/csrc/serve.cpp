@@ -37,6 +37,7 @@
 // smg_server_step never blocks while a slice is on the device; between
 // slices it synchronises once (counters, queue state, admission staging).
 #include <chrono>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
@@ -580,11 +581,14 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   // task slots of each of the two queues.  A slice's queue is linear and the
   // doorbell ends a slice once half of it is used, so the size sets how often
   // every running warp is preempted: at 1,000 requests/s on the 2^24 R-MAT
-  // graph, 2^21 slots ended 20 slices in 2 s (p50 33.6 ms, p99 208 ms) and
-  // 2^23 slots 11 (p50 13.8 ms, p99 117 ms).  2^23 slots of 4 + 32 words are
-  // 1.2 GB per queue.
-  s->cap = static_cast<uint32_t>(std::min(env_ms("SMG_SERVE_QUEUE_TASKS", static_cast<double>(8u << 20)),
-                                          static_cast<double>(1u << 28)));
+  // graph, 2^21 slots ended 20 slices in 2 s (p50 33.6 ms, p99 208 ms), 2^23
+  // slots 11 (p50 12.1 ms, p99 98.9 ms) and 2^25 slots 4 (p50 9.7 ms, p99
+  // 89.9 ms).  Default: 2^25 slots, at most 4 GiB per queue.
+  {
+    const double tw_bytes = 4.0 * (4 + s->kmax);
+    const double dflt = std::min(static_cast<double>(1u << 25), std::floor((4.0 * (1ull << 30)) / tw_bytes));
+    s->cap = static_cast<uint32_t>(std::min(env_ms("SMG_SERVE_QUEUE_TASKS", dflt), static_cast<double>(1u << 28)));
+  }
   s->admit_batch = std::max<uint32_t>(1, static_cast<uint32_t>(env_ms("SMG_ADMIT_BATCH", s->cfg.max_inflight / 8.0)));
   const size_t tw = task_words(s.get());
   const uint32_t m = s->cfg.max_inflight;

@@ -44,8 +44,27 @@ def test_workload_counts(ctx, name):
     assert c1.tolist() + c2.tolist() == want
 
 
+def test_wide_workload_counts(ctx):
+    """The 4..7-vertex queries of the 2^22 graph (up to 10^9 embeddings each,
+    every count recomputed by the CPU oracle): batched, batched at a
+    breadth-first depth of 2, and plain on a spread sample."""
+    if not available("rmat22_k4to7"):
+        pytest.skip("workload_rmat22_k4to7.json not generated")
+    wl = load("rmat22_k4to7")
+    queries, want, meta = wl.queries()
+    assert sorted({q["k"] for q in meta["queries"]}) == [4, 5, 6, 7]
+    dev = DeviceGraph(ctx, wl.graph())
+    plans = [Plan(q) for q in queries]
+    counts, st = native.match_batch(ctx, dev, plans)
+    assert counts.tolist() == want
+    counts2, _ = native.match_batch(ctx, dev, plans, bfs_depth=2)
+    assert counts2.tolist() == want
+    for i in np.linspace(0, len(plans) - 1, num=8).astype(int):
+        assert native.match(ctx, dev, plans[i])[0].count == want[i], i
+
+
 def test_workload_fixture_meta():
-    for name in ["er1k", "rmat20", "rmat22"]:
+    for name in ["er1k", "rmat20", "rmat22", "rmat22_k4to7"]:
         if not available(name):
             continue
         meta = json.loads((GOLD / f"workload_{name}.json").read_text())
