@@ -179,18 +179,26 @@ def serving(ctx, dev, plans, want, rates, seconds=2.0, max_requests=2048):
     smg_server_step.  Latency = finish - submit as the server stamps them;
     sustained rate = requests / (last finish - first submit)."""
     import random
+    from clustersm_gb300 import native
     from clustersm_gb300.native import Server
     out = []
     for rate in rates:
         rng = random.Random(f"serve-{rate}")
         n = max(64, min(max_requests, int(rate * seconds)))
         # request state for up to 1,024 requests: 160 GB (measured 1,749
-        # sustained at 5,000/s offered, against 1,501 with 96 GB), or what the
-        # device has free less 24 GB for the server's queues and the filter
+        # sustained at 5,000/s offered, against 1,501 with 96 GB), or the
+        # device's memory less the resident graph and 40 GB for the server's
+        # queues, the filter and other allocations (the server frees the
+        # context's batch scratch when it needs the room)
         import torch
-        budget = min(160 << 30, max(16 << 30, torch.cuda.mem_get_info()[0] - (24 << 30)))
-        srv = Server(ctx, dev, max_inflight=1024, memory_budget_bytes=budget,
-                     max_query_vertices=max(p.view.k for p in plans))
+        total = torch.cuda.mem_get_info()[1]
+        budget = min(160 << 30, max(16 << 30, total - dev.stats().device_bytes - (40 << 30)))
+        kq = max(p.view.k for p in plans)
+        try:
+            srv = Server(ctx, dev, max_inflight=1024, memory_budget_bytes=budget, max_query_vertices=kq)
+        except native.SmgError:  # less room than expected: what is free now, less 24 GB
+            budget = max(16 << 30, torch.cuda.mem_get_info()[0] - (24 << 30))
+            srv = Server(ctx, dev, max_inflight=1024, memory_budget_bytes=budget, max_query_vertices=kq)
         tickets = []
         t_next = time.perf_counter()
         while len(tickets) < n:

@@ -156,7 +156,8 @@ smg_status finish_resident(smg_ctx *c, DevGraph &g, const uint64_t *offsets, con
   SMG_CUDA(cudaMalloc(&g.label, b_lab));
   SMG_CUDA(cudaMalloc(&g.nlc, b_nlc));
   SMG_CUDA(cudaMalloc(&g.lverts, b_lab));
-  g.bytes += 2 * b_lab + b_nlc;
+  SMG_CUDA(cudaMalloc(&g.ldeg, b_lab));
+  g.bytes += 3 * b_lab + b_nlc;
   if (n) SMG_CUDA(cudaMemcpyAsync(g.label, labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
   if (n) SMG_CUDA(cudaMemcpyAsync(g.lverts, lverts.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
   smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
@@ -359,6 +360,7 @@ void smg_graph_free(smg_graph *G) {
   if (g.label) cudaFree(g.label);
   if (g.nlc) cudaFree(g.nlc);
   if (g.lverts) cudaFree(g.lverts);
+  if (g.ldeg) cudaFree(g.ldeg);
   if (g.hub_of) cudaFree(g.hub_of);
   if (g.hub_bits) cudaFree(g.hub_bits);
   if (g.adjr) cudaFree(g.adjr);

@@ -46,7 +46,11 @@ struct DevGraph {
   uint32_t *off = nullptr;    // [n+1]  (2|E| < 2^32 is required)
   uint32_t *adj = nullptr;    // [2|E|] sorted per vertex
   uint32_t *label = nullptr;  // [n]
-  uint8_t *nlc = nullptr;     // [n][nlc_stride] neighbour-label counts, saturated at 255
+  // [n][nlc_stride] neighbour-label counts, saturated at 255, one row per
+  // position of `lverts` (row p: vertex lverts[p]), so that a sweep over a
+  // label group reads consecutive rows; ldeg[p] is that vertex's degree
+  uint8_t *nlc = nullptr;
+  uint32_t *ldeg = nullptr;   // [n]
   uint32_t *hub_of = nullptr; // [n] index of the vertex's neighbour bitmap, or kNone
   uint32_t *hub_bits = nullptr;  // [num_hubs][hub_words]
   uint32_t num_hubs = 0;

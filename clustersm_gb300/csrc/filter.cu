@@ -51,35 +51,41 @@ __device__ __forceinline__ void enc_clear(uint32_t *enc, uint32_t W, uint32_t v,
 }
 
 // ---------------------------------------------------------------- NLC table
-// One warp per vertex: lanes stride the neighbour list and count labels in a
-// per-warp shared histogram, then write saturated bytes.
+// One warp per position p of the label groups (vertex v = lverts[p]): lanes
+// stride v's neighbour list and count labels in a per-warp shared histogram,
+// then write saturated bytes to row p and v's degree to ldeg[p].  Rows follow
+// the label groups so that the initial filter, which sweeps a group, reads
+// consecutive rows and degrees instead of one scattered row per vertex.
 __global__ void k_build_nlc(uint32_t n, const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                            const uint32_t *__restrict__ label, uint32_t ncols, uint32_t stride,
-                            uint8_t *__restrict__ nlc) {
+                            const uint32_t *__restrict__ label, const uint32_t *__restrict__ lverts, uint32_t ncols,
+                            uint32_t stride, uint8_t *__restrict__ nlc, uint32_t *__restrict__ ldeg) {
   extern __shared__ uint32_t hist[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   uint32_t *h = hist + wib * ncols;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t v = blockIdx.x * (blockDim.x >> 5) + wib; v < n; v += warps) {
+  for (uint32_t pos = blockIdx.x * (blockDim.x >> 5) + wib; pos < n; pos += warps) {
+    const uint32_t v = lverts[pos];
     for (uint32_t c = lane; c < ncols; c += 32) h[c] = 0;
     __syncwarp();
-    for (uint32_t e = off[v] + lane; e < off[v + 1]; e += 32) {
+    const uint32_t e0 = off[v], e1 = off[v + 1];
+    for (uint32_t e = e0 + lane; e < e1; e += 32) {
       const uint32_t l = label[adj[e]];
       if (l < ncols) atomicAdd_block(&h[l], 1u);
     }
     __syncwarp();
-    uint8_t *row = nlc + static_cast<size_t>(v) * stride;
+    uint8_t *row = nlc + static_cast<size_t>(pos) * stride;
     for (uint32_t c = lane; c < stride; c += 32) row[c] = c < ncols ? static_cast<uint8_t>(min(h[c], 255u)) : 0;
+    if (lane == 0) ldeg[pos] = e1 - e0;
     __syncwarp();
   }
 }
 
 // ------------------------------------------------------------ initial filter
 // A query's vertices to visit: its label groups laid end to end.  Returns the
-// vertex at position t (< total), the query vertices carrying its label and
-// its rank within its label's group.
+// vertex at position t (< total), the query vertices carrying its label, its
+// rank within its label's group and its position in lverts.
 __device__ __forceinline__ uint32_t group_vertex(const FilterQuery &Q, const uint32_t *__restrict__ lverts, uint32_t t,
-                                                 uint32_t &same, uint32_t &rank) {
+                                                 uint32_t &same, uint32_t &rank, uint32_t &pos) {
   uint32_t i = 0;
   while (t >= Q.grp_hi[i] - Q.grp_lo[i]) {
     t -= Q.grp_hi[i] - Q.grp_lo[i];
@@ -87,7 +93,8 @@ __device__ __forceinline__ uint32_t group_vertex(const FilterQuery &Q, const uin
   }
   same = Q.grp_mask[i];
   rank = t;
-  return lverts[Q.grp_lo[i] + t];
+  pos = Q.grp_lo[i] + t;
+  return lverts[pos];
 }
 
 __device__ __forceinline__ uint32_t group_total(const FilterQuery &Q) {
@@ -100,7 +107,7 @@ __device__ __forceinline__ uint32_t group_total(const FilterQuery &Q) {
 // other vertices are never touched).  Candidates are appended to per-u lists
 // with one atomic per warp and query vertex.
 __global__ void __launch_bounds__(256) k_nlc_filter(const uint32_t *__restrict__ lverts,
-                                                    const uint32_t *__restrict__ off,
+                                                    const uint32_t *__restrict__ ldeg,
                                                     const uint8_t *__restrict__ nlc, uint32_t stride,
                                                     const FilterQuery *__restrict__ qs) {
   __shared__ FilterQuery Q;
@@ -115,10 +122,10 @@ __global__ void __launch_bounds__(256) k_nlc_filter(const uint32_t *__restrict__
     const uint32_t t = base + threadIdx.x;
     uint32_t mask = 0, v = 0;
     if (t < total) {
-      uint32_t same = 0, rank = 0;
-      v = group_vertex(Q, lverts, t, same, rank);
-      const uint32_t dv = off[v + 1] - off[v];
-      const uint8_t *row = nlc + static_cast<size_t>(v) * stride;
+      uint32_t same = 0, rank = 0, pos = 0;
+      v = group_vertex(Q, lverts, t, same, rank, pos);
+      const uint32_t dv = ldeg[pos];
+      const uint8_t *row = nlc + static_cast<size_t>(pos) * stride;
       for (uint32_t b = same; b; b &= b - 1) {
         const uint32_t u = __ffs(b) - 1;
         if (Q.deg[u] > dv) continue;
@@ -455,8 +462,8 @@ __global__ void __launch_bounds__(256) k_collect(const uint32_t *__restrict__ lv
     const uint32_t t = base + threadIdx.x;
     uint32_t cm = 0, v = 0;
     if (t < total) {
-      uint32_t same = 0, rank = 0;
-      v = group_vertex(Q, lverts, t, same, rank);
+      uint32_t same = 0, rank = 0, pos = 0;
+      v = group_vertex(Q, lverts, t, same, rank, pos);
       const uint32_t m0 = vmask[v];
       for (uint32_t b = m0; b; b &= b - 1) {
         const uint32_t u = __ffs(b) - 1;
@@ -500,7 +507,8 @@ smg_status launch_build_nlc(DevGraph &g, cudaStream_t s, int num_sms) {
   const int threads = 256;
   const size_t smem = static_cast<size_t>(threads / 32) * ncols * sizeof(uint32_t);
   const uint32_t blocks = std::max<uint32_t>(1, std::min<uint64_t>((g.n + 7) / 8, static_cast<uint64_t>(num_sms) * 16));
-  if (g.n) k_build_nlc<<<blocks, threads, smem, s>>>(g.n, g.off, g.adj, g.label, ncols, g.nlc_stride, g.nlc);
+  if (g.n) k_build_nlc<<<blocks, threads, smem, s>>>(g.n, g.off, g.adj, g.label, g.lverts, ncols, g.nlc_stride, g.nlc,
+                                                     g.ldeg);
   SMG_CUDA(cudaGetLastError());
   return SMG_OK;
 }
@@ -755,7 +763,7 @@ smg_status launch_nlc_filter(const DevGraph &g, const FilterQuery *d_qs, uint32_
   if (!nq || !g.n) return SMG_OK;
   for (uint32_t y0 = 0; y0 < nq; y0 += 65535) {
     const uint32_t ny = std::min<uint32_t>(65535, nq - y0);
-    k_nlc_filter<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.lverts, g.off, g.nlc, g.nlc_stride,
+    k_nlc_filter<<<dim3(vertex_blocks(g, nq, num_sms), ny), 256, 0, s>>>(g.lverts, g.ldeg, g.nlc, g.nlc_stride,
                                                                          d_qs + y0);
     SMG_CUDA(cudaGetLastError());
   }
