@@ -17,8 +17,10 @@ the device-resident data graph.  Prints one JSON line (rank 0).
   cpu_baseline  the CPU oracle (backtracking, all host cores) on a bounded
              sample of the same queries
   serving    p50 / p99 latency and sustained rate of the continuous-batching
-             server (smg_server_*) under seeded Poisson arrivals of the same
-             queries at 100, 1,000 and 5,000 queries/s offered
+             server (smg_server_*) on the 2^24-vertex R-MAT graph under seeded
+             Poisson arrivals of its 4..5-vertex requests at 100, 1,000 and
+             5,000 queries/s offered, and of its 4..7-vertex requests (up to
+             10^9 embeddings each, workload rmat24_k4to7) at 25 and 50/s
 
   wide       the batched path on the 4..7-vertex queries of the same 2^22
              graph (workload rmat22_k4to7, the widest query sizes with
@@ -77,6 +79,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-rates", default="100,1000,5000")
+    ap.add_argument("--serve-wide-rates", default="25,50",
+                    help="offered rates of the 4..7-vertex serving requests (empty: skip them)")
     ap.add_argument("--no-wide", action="store_true", help="skip the 4..7-vertex query leg")
     ap.add_argument("--no-c4", action="store_true", help="skip the 2^25-vertex graph leg")
     ap.add_argument("--c4-scale", type=int, default=25)
@@ -638,6 +642,22 @@ def main():
                      "batch_qps": len(bplans) / batch_s,
                      "batch_counts_ok": sum(int(c) == int(w) for c, w in zip(bcounts, bwant) if w is not None),
                      "rates": serving(ctx, sdev, splans, swant, rates)}
+            # the same graph's widest decidable requests (4..7 vertices, up to
+            # 10^9 embeddings each), at rates about a quarter and half of
+            # their batch rate
+            wwl = load("rmat24_k4to7")
+            wide_rates = [float(r) for r in args.serve_wide_rates.split(",") if r]
+            if (ROOT / wwl.queries_file).exists() and wide_rates:
+                wq, wwant, _ = wwl.queries()
+                wplans = [Plan(q) for q in wq]
+                native.match_batch(ctx, sdev, wplans)
+                t0 = time.perf_counter()
+                wcounts, _ = native.match_batch(ctx, sdev, wplans)
+                wbatch_s = time.perf_counter() - t0
+                serve["wide"] = {"workload": wwl.name, "description": wwl.description,
+                                 "batch_qps": len(wplans) / wbatch_s,
+                                 "batch_counts_ok": sum(int(c) == int(w) for c, w in zip(wcounts, wwant)),
+                                 "rates": serving(ctx, sdev, wplans, wwant, wide_rates, seconds=4.0)}
             sdev.free()
         else:
             if dev_freed:

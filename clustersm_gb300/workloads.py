@@ -84,4 +84,11 @@ WORKLOADS = {
                              description="R-MAT(0.57,0.19,0.19,0.05) 2^22 vertices, avg degree 16, 32 Zipf labels, "
                                          "64 walk queries of 4, 5, 6 and 7 vertices (16 each; tree/sparse/dense "
                                          "where decidable, else dense) of at most 10^9 embeddings"),
+    "rmat24_k4to7": Workload("rmat24_k4to7", "rmat", scale=24, avg_degree=16, labels=32, seed=1,
+                             queries_file="tests/golden/workload_rmat24_k4to7.json",
+                             description="R-MAT(0.57,0.19,0.19,0.05) 2^24 vertices, avg degree 16, 32 Zipf labels, "
+                                         "47 walk queries of 4, 5 and 6 vertices (tree/sparse/dense where "
+                                         "decidable, else dense) of at most 10^9 embeddings: the serving graph's "
+                                         "widest decidable requests (no 7-vertex draw within 10^9 embeddings in "
+                                         "420 s of screening)"),
 }

@@ -255,11 +255,13 @@ typedef struct smg_match_opts {
   uint32_t bfs_depth;     /* breadth-first levels before the join turns
                              depth-first: a warp queues every partial
                              match of the first bfs_depth levels as a
-                             task (within half of the task queue; past
-                             that it descends itself); 0 = the tuned
-                             depth of the query's shape class, none when
-                             untuned.  Counts do not depend on it.  The
-                             reference joins every level breadth-first
+                             task, while the queue holds at most the root
+                             tasks plus SMG_BFS_SLOTS_PER_WARP (16) slots
+                             per resident join warp; past that it
+                             descends itself.  0 = the tuned depth of the
+                             query's shape class, none when untuned.
+                             Counts do not depend on it.  The reference
+                             joins every level breadth-first
                              (join.cu:290-435).                            */
   uint32_t root_chunk;    /* root candidates per initial task; 0 = auto    */
   uint32_t reserved;

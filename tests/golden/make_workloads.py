@@ -59,16 +59,18 @@ SPECS = {
     # the serving graph (R-MAT 2^24): requests of the sizes that stay exact
     # within a serving budget (at most 10^7 embeddings each)
     "rmat24": (256, [4, 5], ["tree", "sparse", "dense"], 10**7),
+    # the serving graph's widest decidable requests, drawn like rmat22_k4to7
+    "rmat24_k4to7": (64, [4, 5, 6, 7], ["tree", "sparse", "dense"], 10**9),
 }
 # join steps a screened query may take (bounds the draws whose count is out of reach)
-WORK_LIMIT = {"rmat22_k4to7": 1 << 30}
+WORK_LIMIT = {"rmat22_k4to7": 1 << 30, "rmat24_k4to7": 1 << 30}
 
 
 def slot_shape(name, slot):
     """(k, shape) of a slot: the wide workload cycles k first, then shapes;
     the others draw k at random and cycle shapes."""
     nq, ks, shapes, _ = SPECS[name]
-    if name == "rmat22_k4to7":
+    if name.endswith("_k4to7"):
         return ks[slot % len(ks)], shapes[(slot // len(ks)) % len(shapes)]
     return None, shapes[slot % len(shapes)]
 
@@ -96,7 +98,7 @@ def phases(name):
     their shape, and then to 4-vertex dense ones."""
     if name in ("rmat22", "rmat24"):
         return [(64, None, None), (256, 4, None), (64, 4, "dense")]
-    if name == "rmat22_k4to7":
+    if name.endswith("_k4to7"):
         # trees of 6 or more vertices and most sparse ones are out of reach:
         # such slots fall back to dense queries of their size (at k = 7 about
         # one dense draw in 800 has at most 10^9 embeddings)
