@@ -1040,8 +1040,8 @@ __device__ bool try_donate(WarpView &S, const JoinLaunch &p, uint32_t q, unsigne
 // queue's tail stays within the launch's breadth-first budget: past it the
 // warp keeps its batch and goes on depth-first, so the frontier held in the
 // queue is bounded.  Returns true when the batch was queued.
-__device__ __noinline__ bool bfs_push(const WarpView &S, const JoinLaunch &p, uint32_t q, unsigned long long *qpending,
-                         uint32_t level, uint32_t taken, uint32_t lane) {
+__device__ __noinline__ bool bfs_push(const WarpView &S, const JoinLaunch &p, uint32_t q,
+                                      unsigned long long *qpending, uint32_t level, uint32_t taken, uint32_t lane) {
   QueueState *qs = p.qs;
   unsigned long long first = 0;
   int ok = 0;
