@@ -157,9 +157,16 @@ smg_status finish_resident(smg_ctx *c, DevGraph &g, const uint64_t *offsets, con
   SMG_CUDA(cudaMalloc(&g.nlc, b_nlc));
   SMG_CUDA(cudaMalloc(&g.lverts, b_lab));
   SMG_CUDA(cudaMalloc(&g.ldeg, b_lab));
-  g.bytes += 3 * b_lab + b_nlc;
+  SMG_CUDA(cudaMalloc(&g.pos_of, b_lab));
+  SMG_CUDA(cudaMalloc(&g.lvstart, g.lvert_start.size() * 4));
+  g.bytes += 4 * b_lab + b_nlc + g.lvert_start.size() * 4;
+  std::vector<uint32_t> pos_of(std::max<uint32_t>(n, 1));
+  for (uint32_t p = 0; p < n; ++p) pos_of[lverts[p]] = p;
   if (n) SMG_CUDA(cudaMemcpyAsync(g.label, labels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
   if (n) SMG_CUDA(cudaMemcpyAsync(g.lverts, lverts.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
+  if (n) SMG_CUDA(cudaMemcpyAsync(g.pos_of, pos_of.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, c->stream));
+  SMG_CUDA(cudaMemcpyAsync(g.lvstart, g.lvert_start.data(), g.lvert_start.size() * 4, cudaMemcpyHostToDevice,
+                           c->stream));
   smg_status st = launch_build_nlc(g, c->stream, c->num_sms);
   if (st) return st;
   if (label_index_enabled()) {
@@ -361,6 +368,8 @@ void smg_graph_free(smg_graph *G) {
   if (g.nlc) cudaFree(g.nlc);
   if (g.lverts) cudaFree(g.lverts);
   if (g.ldeg) cudaFree(g.ldeg);
+  if (g.pos_of) cudaFree(g.pos_of);
+  if (g.lvstart) cudaFree(g.lvstart);
   if (g.hub_of) cudaFree(g.hub_of);
   if (g.hub_bits) cudaFree(g.hub_bits);
   if (g.adjr) cudaFree(g.adjr);
@@ -609,7 +618,7 @@ smg_status make_query_records(const Plan &P, const DevGraph &g, const QueryBuffe
     j.cbits = b.cbits;
     j.cwords = (g.n + 31ull) / 32;
     j.crow = g.adjr ? b.cbits + static_cast<size_t>(P.k) * j.cwords : nullptr;
-    j.lastcnt = b.vmask;
+    j.lastcnt = b.enc;
     const uint32_t last_back = j.back_mask[P.k - 1];
     if (last_back && !(last_back & (last_back - 1))) {
       j.fast_last = static_cast<uint32_t>(__builtin_ctz(last_back)) + 1;
@@ -912,9 +921,9 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
         lab += g.label_count[P.label[u]];
       }
     // masks cleared (4 B a vertex); per vertex of the query's labels: group
-    // entry, offsets, NLC sector, mask write, then group entry and mask read
-    // in collect; per candidate appended, per walked entry, per root
-    st->filter_bytes += 4ull * g.n + lab * (4 + 8 + 32 + 4 + 4 + 4) + 8ull * q.initial_cands +
+    // entry, degree, NLC row, mask write, then group entry and mask read in
+    // collect; per candidate appended, per walked entry, per root
+    st->filter_bytes += 4ull * g.n + lab * (4 + 4 + g.nlc_stride + 4 + 4 + 4) + 8ull * q.initial_cands +
                         8ull * q.walk_entries + 4ull * q.num_roots;
     // candidate bitmap rows written by collect: k id-indexed rows of n bits,
     // and with entry ranks k rank-indexed rows of the label's group size
@@ -1124,21 +1133,30 @@ smg_status smg_filter_inspect(smg_ctx *c, const smg_graph *G, const smg_plan *p,
   ++c->run_gen;  // invalidates a captured batch graph
   s = stage_chunk(c, g, &pl, ch, o);
   if (s) return s;
+  // the filter keeps its masks and bitmap by position in the label groups;
+  // the caller gets them by vertex id
+  const size_t n = g.n, W = pl->num_words;
+  std::vector<uint32_t> lv(std::max<size_t>(n, 1)), m0(vmask0 ? n : 0), enc(encodings ? n * W : 0),
+      cm(candmask ? n : 0);
   SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
   s = launch_nlc_filter(g, ch.fq, 1, c->stream, c->num_sms);
   if (s) return s;
-  if (vmask0)
-    SMG_CUDA(cudaMemcpyAsync(vmask0, ch.vmask[0], static_cast<size_t>(g.n) * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (vmask0 && n)
+    SMG_CUDA(cudaMemcpyAsync(m0.data(), ch.vmask[0], n * 4, cudaMemcpyDeviceToHost, c->stream));
   s = launch_walks(g, ch.fq, *c->fdev, walk_overflow(ch), c->stream, c->num_sms);
   if (s) return s;
   s = launch_collect(g, ch.fq, 1, c->stream, c->num_sms);
   if (s) return s;
-  if (encodings)
-    SMG_CUDA(cudaMemcpyAsync(encodings, ch.enc[0], static_cast<size_t>(g.n) * pl->num_words * 4,
-                             cudaMemcpyDeviceToHost, c->stream));
-  if (candmask)
-    SMG_CUDA(cudaMemcpyAsync(candmask, ch.vmask[0], static_cast<size_t>(g.n) * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (encodings && n) SMG_CUDA(cudaMemcpyAsync(enc.data(), ch.enc[0], n * W * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (candmask && n) SMG_CUDA(cudaMemcpyAsync(cm.data(), ch.vmask[0], n * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (n) SMG_CUDA(cudaMemcpyAsync(lv.data(), g.lverts, n * 4, cudaMemcpyDeviceToHost, c->stream));
   SMG_CUDA(cudaStreamSynchronize(c->stream));
+  for (size_t q = 0; q < n; ++q) {
+    const uint32_t v = lv[q];
+    if (vmask0) vmask0[v] = m0[q];
+    if (candmask) candmask[v] = cm[q];
+    if (encodings) std::memcpy(encodings + static_cast<size_t>(v) * W, enc.data() + q * W, W * 4);
+  }
   return SMG_OK;
 }
 

@@ -87,6 +87,11 @@ struct DevGraph {
   // the per-query filter sweeps visit only the vertices of the query's labels.
   uint32_t *lverts = nullptr;              // [n]
   std::vector<uint32_t> lvert_start;       // [min(num_labels, kMaxLabels) + 1]
+  // Device copies for the filter, whose per-query masks and cluster bitmaps
+  // are indexed by position in lverts: where each label's group starts
+  // (lvert_start), and each vertex's position (the inverse of lverts).
+  uint32_t *lvstart = nullptr;             // [lvert_start.size()]
+  uint32_t *pos_of = nullptr;              // [n]
   uint64_t bytes = 0;
 };
 
@@ -154,6 +159,10 @@ struct FilterQuery {
   uint32_t last_slot[kMaxK];
   uint32_t root;
   uint64_t cand_off[kMaxK + 1];
+  // vmask (initial, then final candidate masks) and enc (the cluster
+  // bitmap, `words` per vertex) are indexed by the vertex's position in
+  // DevGraph::lverts, so that a sweep over a label group reads and writes them
+  // in order; cand holds positions too; roots holds vertex ids (the join's)
   uint32_t *vmask, *enc, *cand, *cand_cnt, *roots, *num_roots;
   uint64_t root_cap;             // entries `roots` can hold
   unsigned long long *stat;       // [0] sum over u of final |C(u)|, [1] walk list entries
@@ -174,7 +183,10 @@ struct JoinQuery {
   uint32_t order[kMaxK];      // query vertex matched at each level
   uint32_t back_mask[kMaxK];  // earlier levels adjacent to the level's vertex
   uint32_t same_label[kMaxK]; // earlier levels with the same label (injectivity)
-  const uint32_t *candmask;   // [n] final candidate masks (bit u: may take query vertex u)
+  // [n] final candidate masks (bit u: may take query vertex u); by vertex id
+  // when the caller provides them (smg_join_noalloc), by position in
+  // DevGraph::lverts when the filter wrote them (the join then tests cbits)
+  const uint32_t *candmask;
   // The same candidates as one bitmap per query vertex, cbits[u * cwords +
   // v / 32] bit v % 32, built after the filter: a random candidate test then
   // reads a 512 KB row (at 2^22 vertices) instead of a 16 MB mask array, so
@@ -190,8 +202,8 @@ struct JoinQuery {
   // Null: every test reads cbits.
   const uint32_t *crow;
   // Count-only runs with fast_last set: the last level's per-vertex
-  // neighbour counts (see k_last_counts), written over candmask once cbits
-  // holds the candidates.
+  // neighbour counts by vertex id (see k_last_counts), written over the
+  // query's cluster bitmap, which nothing reads after the filter.
   uint32_t *lastcnt;
   const uint32_t *roots;      // root candidates
   const uint32_t *num_roots;  // device counter

@@ -120,10 +120,10 @@ __global__ void __launch_bounds__(256) k_nlc_filter(const uint32_t *__restrict__
   const uint32_t step = gridDim.x * blockDim.x;
   for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += step) {
     const uint32_t t = base + threadIdx.x;
-    uint32_t mask = 0, v = 0;
+    uint32_t mask = 0, pos = 0;
     if (t < total) {
-      uint32_t same = 0, rank = 0, pos = 0;
-      v = group_vertex(Q, lverts, t, same, rank, pos);
+      uint32_t same = 0, rank = 0;
+      group_vertex(Q, lverts, t, same, rank, pos);
       const uint32_t dv = ldeg[pos];
       const uint8_t *row = nlc + static_cast<size_t>(pos) * stride;
       for (uint32_t b = same; b; b &= b - 1) {
@@ -133,19 +133,20 @@ __global__ void __launch_bounds__(256) k_nlc_filter(const uint32_t *__restrict__
         for (uint32_t i = 0; i < Q.nnlc[u] && ok; ++i) ok = row[Q.nlc_label[u][i]] >= Q.nlc_count[u][i];
         if (ok) mask |= 1u << u;
       }
-      if (mask) Q.vmask[v] = mask;
+      if (mask) Q.vmask[pos] = mask;
     }
-    // warp-aggregated appends, one atomic per query vertex present in the warp
+    // warp-aggregated appends of positions, one atomic per query vertex
+    // present in the warp
     uint32_t any = __reduce_or_sync(0xFFFFFFFFu, mask);
     for (; any; any &= any - 1) {
       const uint32_t u = __ffs(any) - 1;
       const uint32_t bal = __ballot_sync(0xFFFFFFFFu, (mask >> u) & 1u);
-      uint32_t pos = 0;
-      if (lane == 0) pos = atomicAdd(Q.cand_cnt + u, __popc(bal));
-      pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+      uint32_t first = 0;
+      if (lane == 0) first = atomicAdd(Q.cand_cnt + u, __popc(bal));
+      first = __shfl_sync(0xFFFFFFFFu, first, 0);
       if ((mask >> u) & 1u) {
-        const uint64_t at = Q.cand_off[u] + pos + __popc(bal & ((1u << lane) - 1));
-        if (SMG_DCHECK(at < Q.cand_off[u + 1], 201, at, u)) Q.cand[at] = v;
+        const uint64_t at = Q.cand_off[u] + first + __popc(bal & ((1u << lane) - 1));
+        if (SMG_DCHECK(at < Q.cand_off[u + 1], 201, at, u)) Q.cand[at] = pos;
       }
     }
   }
@@ -169,9 +170,10 @@ __device__ __forceinline__ void spread_slots(const ClusterStep &st, uint32_t xm,
   }
 }
 
-// One neighbour w of a candidate that passed steps `pass` of its group: set
-// the neighbour slots of those steps (star / merge), or apply the combine
-// rule (AND of the other clusters' slots) to w.
+// One neighbour of a candidate, at position w of the label groups, that
+// passed steps `pass` of its group: set the neighbour slots of those steps
+// (star / merge), or apply the combine rule (AND of the other clusters'
+// slots) to it.
 __device__ __forceinline__ void walk_entry(uint32_t w, const StepGroup &G, const ClusterStep *__restrict__ steps,
                                            const uint32_t *__restrict__ aux, const FilterQuery &Q, uint32_t kind,
                                            uint32_t pass) {
@@ -199,16 +201,16 @@ __device__ __forceinline__ void walk_entry(uint32_t w, const StepGroup &G, const
 }
 
 // Neighbour part of a step group for candidate v over adj[e0, e1), one
-// entry per lane.
+// entry per lane (each neighbour's position looked up in pos_of).
 __device__ __forceinline__ void walk_neighbors(const uint32_t *__restrict__ adj, const StepGroup &G,
                                                const ClusterStep *__restrict__ steps,
                                                const uint32_t *__restrict__ aux, const FilterQuery &Q,
                                                uint32_t kind, uint32_t pass, uint32_t e0, uint32_t e1,
-                                               uint32_t lane, uint32_t n) {
+                                               uint32_t lane, uint32_t n, const uint32_t *__restrict__ pos_of) {
   for (uint32_t e = e0 + lane; e < e1; e += 32) {
     const uint32_t w = adj[e];
     if (!SMG_DCHECK(w < n, 207, w, e)) continue;
-    walk_entry(w, G, steps, aux, Q, kind, pass);
+    walk_entry(__ldg(pos_of + w), G, steps, aux, Q, kind, pass);
   }
 }
 
@@ -326,20 +328,22 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
     uint32_t v = 0, pass = 0;
     bool act = false;
     if (i < cnt) {
-      v = list[i];
-      if (v != kNone && SMG_DCHECK(v < ov.n, 203, v, i)) {
+      // the list holds the candidates' positions; v is the vertex itself
+      const uint32_t pv = list[i];
+      if (pv != kNone && SMG_DCHECK(pv < ov.n, 203, pv, i)) {
+        v = __ldg(ov.lverts + pv);
         if (kind == 0) {
           const ClusterStep &st = steps[G.first];
-          enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+          enc_set(enc, W, pv, st.core_slot >> 5, 1u << (st.core_slot & 31));
           pass = 1;
           act = true;
         } else if (kind == 1) {
           bool alive = true;
           for (uint32_t j = 0; j < G.count && alive; ++j) {
             const ClusterStep &st = steps[G.first + j];
-            if (enc_bit(enc, W, v, st.left_pos) && enc_bit(enc, W, v, st.right_pos)) {
+            if (enc_bit(enc, W, pv, st.left_pos) && enc_bit(enc, W, pv, st.right_pos)) {
               pass |= 1u << j;
-              enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+              enc_set(enc, W, pv, st.core_slot >> 5, 1u << (st.core_slot & 31));
             } else {
               alive = false;
             }
@@ -349,11 +353,11 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
         } else {
           const ClusterStep &st = steps[G.first];
           bool all = true;
-          for (uint32_t o = 0; o < st.num_others && all; ++o) all = enc_bit(enc, W, v, aux[st.others_off + o]);
+          for (uint32_t o = 0; o < st.num_others && all; ++o) all = enc_bit(enc, W, pv, aux[st.others_off + o]);
           if (st.type == 0) {
-            if (all) enc_set(enc, W, v, st.core_slot >> 5, 1u << (st.core_slot & 31));
+            if (all) enc_set(enc, W, pv, st.core_slot >> 5, 1u << (st.core_slot & 31));
           } else if (!all) {
-            enc_clear(enc, W, v, st.core_slot);
+            enc_clear(enc, W, pv, st.core_slot);
           }
           act = true;
         }
@@ -367,6 +371,11 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
       else if (by_label) li = __ldg(ov.lab_of + v);
     }
     for (uint32_t r = 0; r < nruns; ++r) {
+      // an entry of the run of the group's r-th label sits at position
+      // lvstart[label] + its rank (adjr) when each bucket is one label
+      const uint32_t lab_r = by_label ? static_cast<uint32_t>(G.lab[r]) : kNone;
+      const bool ranked = ov.adjr && lab_r < ov.num_groups_l && lab_r < ov.lab_buckets;
+      const uint32_t run_base = ranked ? __ldg(ov.lvstart + lab_r) : 0u;
       // this lane's segment: the run of the group's r-th label when its
       // candidate has a run table (only those neighbours can change), else
       // (r = 0 only) its whole list
@@ -404,8 +413,12 @@ __global__ void __launch_bounds__(256) k_cluster_walk(const uint32_t *__restrict
         const uint32_t sb = __shfl_sync(0xFFFFFFFFu, s0, src), sp = __shfl_sync(0xFFFFFFFFu, pre, src);
         const uint32_t spass = __shfl_sync(0xFFFFFFFFu, pass, src), sfl = __shfl_sync(0xFFFFFFFFu, fl, src);
         if (t < total) {
-          const uint32_t w = (sfl ? ov.adjl : adj)[sb + (t - sp)];
-          if (SMG_DCHECK(w < ov.n, 207, w, sb)) walk_entry(w, G, steps, aux, Q, kind, spass);
+          const uint32_t e = sb + (t - sp);
+          const uint32_t w = (sfl ? ov.adjl : adj)[e];
+          if (SMG_DCHECK(w < ov.n, 207, w, sb)) {
+            const uint32_t pw = sfl && ranked ? run_base + __ldg(ov.adjr + e) : __ldg(ov.pos_of + w);
+            if (SMG_DCHECK(pw < ov.n, 209, pw, w)) walk_entry(pw, G, steps, aux, Q, kind, spass);
+          }
         }
       }
     }
@@ -436,7 +449,7 @@ __global__ void __launch_bounds__(256) k_walk_chunks(const uint32_t *__restrict_
     // next runs: those neighbours carry none of the group's labels, so their
     // slots do not change
     const uint32_t e1 = min(it.w + kWalkChunk, off[it.y + 1]);
-    walk_neighbors((it.x >> 31) ? ov.adjl : adj, G, steps, aux, Q, kind, it.z, it.w, e1, lane, ov.n);
+    walk_neighbors((it.x >> 31) ? ov.adjl : adj, G, steps, aux, Q, kind, it.z, it.w, e1, lane, ov.n, ov.pos_of);
   }
 }
 
@@ -464,12 +477,12 @@ __global__ void __launch_bounds__(256) k_collect(const uint32_t *__restrict__ lv
     if (t < total) {
       uint32_t same = 0, rank = 0, pos = 0;
       v = group_vertex(Q, lverts, t, same, rank, pos);
-      const uint32_t m0 = vmask[v];
+      const uint32_t m0 = vmask[pos];
       for (uint32_t b = m0; b; b &= b - 1) {
         const uint32_t u = __ffs(b) - 1;
-        if (enc_bit(enc, W, v, last_slot[u])) cm |= 1u << u;
+        if (enc_bit(enc, W, pos, last_slot[u])) cm |= 1u << u;
       }
-      if (m0 != cm) vmask[v] = cm;
+      if (m0 != cm) vmask[pos] = cm;
       ncand += __popc(cm);
       // the join's candidate bitmaps (zero on entry): one bit per (u, v)
       if (Q.cbits)
@@ -784,6 +797,11 @@ smg_status launch_walks(const DevGraph &g, const FilterQuery *d_qs, const Filter
     po.lab_of = g.lab_of;
     po.lab_off = g.lab_off;
     po.lab_buckets = g.lab_buckets;
+    po.lverts = g.lverts;
+    po.pos_of = g.pos_of;
+    po.lvstart = g.lvstart;
+    po.adjr = g.adjl ? g.adjr : nullptr;
+    po.num_groups_l = static_cast<uint32_t>(g.lvert_start.size()) - 1;
     uint32_t *cs = fd.chunk_start + fd.phase_first[p] + p;  // ng + 1 entries per phase
     // 256 threads, so that a served request's plan fits beside a running join
     k_walk_plan<<<1, 256, 0, s>>>(fd.groups + fd.phase_first[p], ng, d_qs, cs);

@@ -26,6 +26,11 @@ struct WalkOverflow {
   // the graph's label index (set by launch_walks; adjl null: none)
   const uint32_t *adjl, *lab_of, *lab_off;
   uint32_t lab_buckets;
+  // positions in the label groups (set by launch_walks): lverts, its inverse
+  // pos_of, the groups' starts lvstart (num_groups_l + 1 entries) and the
+  // entries' ranks within their label adjr (null: look positions up in pos_of)
+  const uint32_t *lverts, *pos_of, *lvstart, *adjr;
+  uint32_t num_groups_l;
 };
 
 // Steps of the cluster bitmap for a batch of queries, grouped into phases:

@@ -232,10 +232,11 @@ struct CandView {
 // candidates of u_L (which implies u_L's label) and differ from the matched
 // vertices of u_L's label.  Its count is therefore the number of such
 // neighbours of m[b], stored once per query for every candidate of order[b],
-// less the same-label matched vertices among them.  The counts overwrite the
-// final masks (the join tests candidates in the bitmaps); kNone marks a
-// vertex whose count is not stored (degree above kLastCountMaxDeg), whose
-// list the join scans as before.
+// less the same-label matched vertices among them.  The counts go to an
+// id-indexed array (JoinQuery::lastcnt, over the query's cluster bitmap,
+// which nothing reads after the filter); kNone marks a vertex whose count is
+// not stored (degree above kLastCountMaxDeg), whose list the join scans as
+// before.
 constexpr uint32_t kLastCountMaxDeg = 8192;
 
 // A warp takes 32 consecutive vertices, picks the candidates of order[b]
@@ -260,12 +261,12 @@ __global__ void __launch_bounds__(256) k_last_counts(const JoinQuery *__restrict
     const uint32_t ub = Q.order[Q.fast_last - 1], ul = Q.order[Q.k - 1];
     const uint32_t *row = Q.cbits + ul * Q.cwords;
     const uint32_t bk = Q.level_bucket[Q.k - 1];
-    uint32_t *cnt = Q.lastcnt;
+    uint32_t *cnt = Q.lastcnt;  // by vertex id
     // the candidates of order[b] all carry its label: walk that label's group
     for (uint32_t t0 = Q.lc_lo + warp * 32; t0 < Q.lc_hi; t0 += nwarps * 32) {
       const uint32_t t = t0 + lane;
       const uint32_t v = t < Q.lc_hi ? __ldg(lverts + t) : 0u;
-      const uint32_t mine = t < Q.lc_hi ? cnt[v] : 0u;  // the final mask, until overwritten below
+      const uint32_t mine = t < Q.lc_hi ? __ldg(Q.candmask + t) : 0u;  // the final mask, by position
       for (uint32_t bal = __ballot_sync(0xFFFFFFFFu, (mine >> ub) & 1u); bal; bal &= bal - 1) {
         const uint32_t src = __ffs(bal) - 1;
         const uint32_t x = __shfl_sync(0xFFFFFFFFu, v, src);
