@@ -497,31 +497,18 @@ __device__ __forceinline__ unsigned long long level_model(const WarpView &S, uin
   return 4ull * level + 8ull + 8ull * dmin + (scans - 8ull - 4ull * dmin);
 }
 
-// Candidate test for list entry w at `level` (>= 1, not the last level).
-__device__ __forceinline__ bool accept(const WarpView &S, const JoinLaunch &p, const CandView &cv, bool use_labels,
-                                       uint32_t level, uint32_t w, uint32_t &probes) {
-  if (!SMG_DCHECK(w < p.n, 105, w, level)) return false;
-  const uint32_t bucket = use_labels ? S.lbk[level] : kNone;
-  if (!cv.has(S.ord[level], w)) return false;
-  for (uint32_t b = S.slab[level]; b; b &= b - 1)
-    if (S.m[__ffs(b) - 1] == w) return false;
-  for (uint32_t b = S.bmask[level] & ~(1u << S.piv[level]); b; b &= b - 1) {
-    const uint32_t j = __ffs(b) - 1;
-    if (!is_neighbor(p, S.m[j], S.beg[j], S.deg[j], S.hub[j], bucket, w, probes)) return false;
-  }
-  return true;
-}
-
 // Entries a lane tests per refill of an intermediate level.  The tests are
 // chains of dependent loads (candidate bit, then a hub bitmap word or a
 // binary search per back edge); a lane runs kWays chains in lockstep so that
 // their loads are in flight together.
 constexpr int kWays = 1;
 
-// accept() for the kWays entries w[i] of a lane whose bit i of `live` is set;
-// returns the entries that pass.  The same tests in the same order as
-// accept(), with every step issued for all live entries before any of them
-// is resolved.
+// Candidate tests at an intermediate level (>= 1, not the last) for the kWays
+// entries w[i] of a lane whose bit i of `live` is set: the candidate bit,
+// injectivity against the matched vertices of the level's label, then
+// membership in the lists of the back neighbours other than the pivot.
+// Returns the entries that pass.  Every step is issued for all live entries
+// before any of them is resolved.
 __device__ __forceinline__ uint32_t accept_multi(const WarpView &S, const JoinLaunch &p, const CandView &cv,
                                                  bool use_labels, uint32_t level, const uint32_t (&w)[kWays],
                                                  const uint32_t (&r)[kWays], bool ranked, uint32_t live,
