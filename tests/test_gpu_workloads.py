@@ -64,7 +64,7 @@ def test_wide_workload_counts(ctx):
 
 
 def test_workload_fixture_meta():
-    for name in ["er1k", "rmat20", "rmat22", "rmat22_k4to7"]:
+    for name in ["er1k", "rmat20", "rmat22", "rmat22_k4to7", "rmat24_k4to7"]:
         if not available(name):
             continue
         meta = json.loads((GOLD / f"workload_{name}.json").read_text())
