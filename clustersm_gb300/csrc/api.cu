@@ -17,6 +17,9 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
 
 #include "api_internal.cuh"
 #include "filter.cuh"
@@ -413,6 +416,15 @@ struct Chunk {
   FilterQuery *fq = nullptr;
   JoinQuery *jq = nullptr;
   std::vector<uint32_t *> vmask, enc, cand, roots, cbits;
+  // What a batch clears before the filter: the queue state, ready flags and
+  // counters, each query's candidate bitmaps, and its masks and cluster
+  // bitmap only over the positions of its own label groups (the filter and
+  // the join read nothing else of them).  A device plan for k_zero_ranges:
+  // zero_plan[0 .. nr] word prefix sums, zero_plan[nr + 1 ..] byte offsets.
+  std::vector<size_t> o_enc, o_vm, o_cb;
+  size_t head_bytes = 0, zero_plan_cap = 0;
+  uint64_t *zero_plan = nullptr;
+  uint32_t zero_ranges = 0;
   std::vector<uint64_t> cand_total;
 };
 
@@ -686,7 +698,12 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   off += al(nq * sizeof(QCounters));
   const size_t o_wcnt = off;
   off += al(kMaxWalkPhases * 2 * sizeof(unsigned int));
-  std::vector<size_t> o_enc(nq), o_vm(nq), o_cand(nq), o_root(nq), o_cb(nq);
+  ch.head_bytes = off;
+  std::vector<size_t> &o_enc = ch.o_enc, &o_vm = ch.o_vm, &o_cb = ch.o_cb;
+  o_enc.assign(nq, 0);
+  o_vm.assign(nq, 0);
+  o_cb.assign(nq, 0);
+  std::vector<size_t> o_cand(nq), o_root(nq);
   // the filter writes masks and candidate bitmaps only for vertices of the
   // query's labels: they start at zero with the cluster bitmaps
   for (uint32_t i = 0; i < nq; ++i) {
@@ -718,6 +735,11 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   off += al(nq * sizeof(FilterQuery));
   const size_t o_jq = off;
   off += al(nq * sizeof(JoinQuery));
+  // the zero plan: at most the head, then per query its bitmaps and two
+  // ranges per label group
+  ch.zero_plan_cap = 1 + static_cast<size_t>(nq) * (2 * kMaxK + 1);
+  const size_t o_zplan = off;
+  off += al((2 * ch.zero_plan_cap + 1) * sizeof(uint64_t));
   const size_t o_emb = off;
   if (o.emb_host && o.emb_cap) off += al(o.emb_cap * ch.kmax * 4);
   ch.total = off;
@@ -733,6 +755,7 @@ smg_status layout_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans,
   ch.xbuf = reinterpret_cast<uint32_t *>(B + o_xbuf);
   ch.fq = reinterpret_cast<FilterQuery *>(B + o_fq);
   ch.jq = reinterpret_cast<JoinQuery *>(B + o_jq);
+  ch.zero_plan = reinterpret_cast<uint64_t *>(B + o_zplan);
   ch.emb = (o.emb_host && o.emb_cap) ? reinterpret_cast<uint32_t *>(B + o_emb) : nullptr;
   ch.vmask.resize(nq);
   ch.enc.resize(nq);
@@ -783,6 +806,42 @@ smg_status stage_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, 
   if (st) return st;
   SMG_CUDA(cudaMemcpyAsync(ch.fq, hf, nq * sizeof(FilterQuery), cudaMemcpyHostToDevice, c->stream));
   SMG_CUDA(cudaMemcpyAsync(ch.jq, hj, nq * sizeof(JoinQuery), cudaMemcpyHostToDevice, c->stream));
+  // The zero plan (see Chunk): the head, then per query the positions of its
+  // label groups in its cluster bitmap and masks, and its candidate bitmaps
+  // whole.  SMG_ZERO=full clears the whole region instead.
+  ch.zero_ranges = 0;
+  static const bool full_zero = [] {
+    const char *e = std::getenv("SMG_ZERO");
+    return e && std::string(e) == "full";
+  }();
+  if (!full_zero) {
+    std::vector<std::pair<uint64_t, uint64_t>> rg;  // (byte offset, bytes)
+    rg.emplace_back(0, ch.head_bytes);
+    for (uint32_t i = 0; i < nq; ++i) {
+      const Plan &P = *plans[ch.a + i];
+      const uint64_t W = P.num_words;
+      for (uint32_t gi = 0; gi < hf[i].ngrp; ++gi) {
+        const uint64_t lo = hf[i].grp_lo[gi], hi = hf[i].grp_hi[gi];
+        if (hi <= lo || hi > g.n) continue;
+        rg.emplace_back(ch.o_enc[i] + lo * W * 4, (hi - lo) * W * 4);
+        rg.emplace_back(ch.o_vm[i] + lo * 4, (hi - lo) * 4);
+      }
+      rg.emplace_back(ch.o_cb[i], cbits_bytes(g, P.k));
+    }
+    std::sort(rg.begin(), rg.end());
+    const size_t plan_bytes = (2 * rg.size() + 1) * sizeof(uint64_t);
+    uint64_t *hz = reinterpret_cast<uint64_t *>(hj + nq);
+    if (rg.size() <= ch.zero_plan_cap && need + plan_bytes <= kPinnedBytes) {
+      const size_t nr = rg.size();
+      hz[0] = 0;
+      for (size_t r = 0; r < nr; ++r) {
+        hz[r + 1] = hz[r] + rg[r].second / 4;
+        hz[nr + 1 + r] = rg[r].first;
+      }
+      SMG_CUDA(cudaMemcpyAsync(ch.zero_plan, hz, plan_bytes, cudaMemcpyHostToDevice, c->stream));
+      ch.zero_ranges = static_cast<uint32_t>(nr);
+    }
+  }
   // the staging buffer is reused by the read-back: finish the copies first
   SMG_CUDA(cudaStreamSynchronize(c->stream));
   return SMG_OK;
@@ -828,7 +887,13 @@ JoinLaunch make_join_launch(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunO
 smg_status enqueue_chunk(smg_ctx *c, const DevGraph &g, Chunk &ch, const RunOpts &o, bool capturing) {
   const uint32_t nq = ch.b - ch.a;
   const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-  SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
+  if (ch.zero_ranges) {
+    smg_status z = launch_zero_ranges(c->arena.base, ch.zero_plan, ch.zero_plan + ch.zero_ranges + 1, ch.zero_ranges,
+                                      c->stream, c->num_sms);
+    if (z) return z;
+  } else {
+    SMG_CUDA(cudaMemsetAsync(c->arena.base, 0, ch.zero_bytes, c->stream));
+  }
   if (o.profile) SMG_CUDA(cudaEventRecordWithFlags(c->ev[0], c->stream, ev_flags));
   smg_status s = launch_filter(g, ch.fq, nq, *c->fdev, walk_overflow(ch), c->stream, c->num_sms);
   if (s) return s;
@@ -855,7 +920,7 @@ smg_status run_chunk(smg_ctx *c, const DevGraph &g, const Plan *const *plans, Ch
     uint64_t walk_launches = 0;
     for (uint32_t ng : c->fdev->phase_count)
       if (ng) walk_launches += 3;  // work list, walk, chunk pass
-    const uint64_t launches = 2 * ((nq + 65534) / 65535) + walk_launches + 2;
+    const uint64_t launches = 2 * ((nq + 65534) / 65535) + walk_launches + 2 + (ch.zero_ranges ? 1 : 0);
     st->launches += launches;
     if (key) {
       drop_graph(c);

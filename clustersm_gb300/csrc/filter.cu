@@ -826,6 +826,41 @@ __global__ void __launch_bounds__(256) k_zero(uint4 *p, uint64_t n16) {
     p[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
+// Zeroes a list of disjoint byte ranges of `base` (offsets and lengths
+// multiples of 4): prefix[r] is the first 4-byte word of range r counted over
+// all ranges (prefix[nr] the total), off[r] its byte offset.  Each block takes
+// chunks of `chunk` consecutive words, finds the range holding the first by
+// binary search and walks on from there, so ranges of any size cost only
+// their words.
+__global__ void __launch_bounds__(256) k_zero_ranges(char *base, const uint64_t *__restrict__ prefix,
+                                                     const uint64_t *__restrict__ off, uint32_t nr, uint64_t chunk) {
+  const uint64_t total = prefix[nr];
+  for (uint64_t c0 = blockIdx.x * chunk; c0 < total; c0 += static_cast<uint64_t>(gridDim.x) * chunk) {
+    const uint64_t c1 = min(total, c0 + chunk);
+    uint32_t lo = 0, hi = nr;  // the last range starting at or before c0
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (prefix[mid] <= c0)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    for (uint32_t r = lo; r < nr && prefix[r] < c1; ++r) {
+      const uint64_t a = max(c0, prefix[r]), b = min(c1, prefix[r + 1]);
+      uint32_t *w = reinterpret_cast<uint32_t *>(base + off[r]);
+      for (uint64_t t = a + threadIdx.x; t < b; t += blockDim.x) w[t - prefix[r]] = 0u;
+    }
+  }
+}
+
+smg_status launch_zero_ranges(char *base, const uint64_t *prefix, const uint64_t *off, uint32_t nr, cudaStream_t s,
+                              int num_sms) {
+  if (!nr) return SMG_OK;
+  k_zero_ranges<<<static_cast<uint32_t>(std::max(num_sms, 1)) * 8, 256, 0, s>>>(base, prefix, off, nr, 1u << 16);
+  SMG_CUDA(cudaGetLastError());
+  return SMG_OK;
+}
+
 smg_status launch_zero(void *p, size_t bytes, cudaStream_t s, int num_sms) {
   if (!bytes) return SMG_OK;
   if (bytes % 16 || reinterpret_cast<uintptr_t>(p) % 16) return fail(SMG_ERR_INTERNAL, "launch_zero: unaligned range");

@@ -66,6 +66,11 @@ struct FilterDev {
 smg_status launch_build_nlc(DevGraph &g, cudaStream_t s, int num_sms);
 // Zeroes bytes (a multiple of 16, 16-byte aligned) with 256-thread blocks.
 smg_status launch_zero(void *p, size_t bytes, cudaStream_t s, int num_sms);
+// Zeroes nr disjoint byte ranges of base, sorted by offset: range r starts at
+// byte off[r] and holds prefix[r + 1] - prefix[r] 4-byte words (both arrays
+// in device memory, prefix[0] = 0).
+smg_status launch_zero_ranges(char *base, const uint64_t *prefix, const uint64_t *off, uint32_t nr, cudaStream_t s,
+                              int num_sms);
 // Query constants (not the device pointers) of one plan.
 smg_status fill_filter_query(const Plan &P, const DevGraph &g, FilterQuery &fq);
 smg_status append_filter_steps(const Plan &P, uint32_t query_index, FilterBatch &fb);
