@@ -36,6 +36,7 @@
 //
 // smg_server_step never blocks while a slice is on the device; between
 // slices it synchronises once (counters, queue state, admission staging).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -143,6 +144,10 @@ struct smg_server {
   smg::JoinQuery *d_jq = nullptr;        // [max_inflight], indexed by slot
   smg::QCounters *d_cnt = nullptr;       // [max_inflight]
   uint32_t *d_seed = nullptr;            // slots to seed
+  // what an admission clears (launch_zero_ranges): word prefix sums, then byte
+  // offsets from zero_base, of up to zplan_cap ranges
+  uint64_t *d_zplan = nullptr;
+  size_t zplan_cap = 0;
   uint32_t *tasks[2] = {nullptr, nullptr};
   uint32_t *ready[2] = {nullptr, nullptr};
   unsigned int *next_count = nullptr;    // tasks preempted into the other queue
@@ -185,7 +190,8 @@ struct smg_server {
     cudaSetDevice(device);
     cudaDeviceSynchronize();
     for (void *p : {static_cast<void *>(pool_mem), static_cast<void *>(d_fq_new), static_cast<void *>(d_jq),
-                    static_cast<void *>(d_cnt), static_cast<void *>(d_seed), static_cast<void *>(tasks[0]),
+                    static_cast<void *>(d_cnt), static_cast<void *>(d_seed), static_cast<void *>(d_zplan),
+                    static_cast<void *>(tasks[0]),
                     static_cast<void *>(tasks[1]), static_cast<void *>(ready[0]), static_cast<void *>(ready[1]),
                     static_cast<void *>(next_count), static_cast<void *>(qs), static_cast<void *>(walk_count),
                     static_cast<void *>(walk_items), static_cast<void *>(xbuf)})
@@ -367,6 +373,12 @@ smg_status admit(smg_server *s, cudaStream_t st) {
   smg::FilterQuery *hf = static_cast<smg::FilterQuery *>(s->stage);
   smg::JoinQuery *hj = reinterpret_cast<smg::JoinQuery *>(hf + n);
   uint32_t *hseed = reinterpret_cast<uint32_t *>(hj + n);
+  // What the admitted requests' filter and join read must start at zero: the
+  // counters, the candidate bitmaps, and the masks and cluster bitmap over
+  // the positions of each request's label groups.  Offsets are from the
+  // lower of the two allocations involved.
+  char *const zbase = std::min(s->pool.base, reinterpret_cast<char *>(s->d_cnt));
+  std::vector<std::pair<uint64_t, uint64_t>> zr;  // (byte offset from zbase, bytes)
   smg::FilterBatch fb;
   for (uint32_t i = 0; i < n; ++i) {
     const uint32_t idx = fresh[i];
@@ -389,15 +401,35 @@ smg_status admit(smg_server *s, cudaStream_t st) {
     rc = smg::append_filter_steps(*sl.plan, i, fb);
     if (rc) return rc;
     hseed[i] = idx;
-    // the filter writes candidates only; zeroed by a kernel that fits beside
-    // a running join (live admission)
-    const int sms = s->ctx->num_sms;
-    rc = smg::launch_zero(b.vmask, fps[i].vmask, st, sms);
-    if (!rc) rc = smg::launch_zero(b.enc, fps[i].enc, st, sms);
-    if (!rc) rc = smg::launch_zero(b.cbits, fps[i].cbits, st, sms);
-    if (!rc) rc = smg::launch_zero(b.counters, sizeof(smg::QCounters), st, sms);
-    if (rc) return rc;
+    const uint64_t W = sl.plan->num_words;
+    auto at = [&](const void *p) { return static_cast<uint64_t>(static_cast<const char *>(p) - zbase); };
+    for (uint32_t gi = 0; gi < hf[i].ngrp; ++gi) {
+      const uint64_t lo = hf[i].grp_lo[gi], hi = hf[i].grp_hi[gi];
+      if (hi <= lo || hi > g.n) continue;
+      zr.emplace_back(at(b.enc) + lo * W * 4, (hi - lo) * W * 4);
+      zr.emplace_back(at(b.vmask) + lo * 4, (hi - lo) * 4);
+    }
+    if (fps[i].cbits) zr.emplace_back(at(b.cbits), fps[i].cbits);
+    zr.emplace_back(at(b.counters), sizeof(smg::QCounters));
     SMG_CUDA(cudaMemcpyAsync(s->d_jq + idx, hj + i, sizeof(smg::JoinQuery), cudaMemcpyHostToDevice, st));
+  }
+  // one kernel clears them all, with 256-thread blocks that fit beside a
+  // running join (live admission)
+  std::sort(zr.begin(), zr.end());
+  if (zr.size() > s->zplan_cap) return fail(SMG_ERR_INTERNAL, "admission clears more ranges than planned");
+  {
+    const uintptr_t pa = (reinterpret_cast<uintptr_t>(hseed + n) + 7) & ~static_cast<uintptr_t>(7);
+    uint64_t *hz = reinterpret_cast<uint64_t *>(pa);
+    const size_t nr = zr.size();
+    hz[0] = 0;
+    for (size_t r = 0; r < nr; ++r) {
+      hz[r + 1] = hz[r] + zr[r].second / 4;
+      hz[nr + 1 + r] = zr[r].first;
+    }
+    SMG_CUDA(cudaMemcpyAsync(s->d_zplan, hz, (2 * nr + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    smg_status zrc = smg::launch_zero_ranges(zbase, s->d_zplan, s->d_zplan + nr + 1, static_cast<uint32_t>(nr), st,
+                                             s->ctx->num_sms);
+    if (zrc) return zrc;
   }
   smg_status rc = s->fdev.upload(fb, st);
   if (rc) return rc;
@@ -601,6 +633,9 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   SMG_CUDA(cudaMalloc(&s->d_jq, m * sizeof(smg::JoinQuery)));
   SMG_CUDA(cudaMalloc(&s->d_cnt, m * sizeof(smg::QCounters)));
   SMG_CUDA(cudaMalloc(&s->d_seed, m * sizeof(uint32_t)));
+  // per admitted request: two ranges per label group, its bitmaps and counters
+  s->zplan_cap = static_cast<size_t>(m) * (2 * s->kmax + 2);
+  SMG_CUDA(cudaMalloc(&s->d_zplan, (2 * s->zplan_cap + 1) * sizeof(uint64_t)));
   for (int i = 0; i < 2; ++i) {
     SMG_CUDA(cudaMalloc(&s->tasks[i], static_cast<size_t>(s->cap) * tw * 4));
     SMG_CUDA(cudaMalloc(&s->ready[i], static_cast<size_t>(s->cap) * 4));
@@ -614,7 +649,8 @@ smg_status smg_server_create(smg_ctx *c, const smg_graph *g, const smg_server_co
   SMG_CUDA(cudaHostAlloc(&s->h_qs, sizeof(smg::QueueState), cudaHostAllocDefault));
   SMG_CUDA(cudaHostAlloc(&s->h_bell, sizeof(uint32_t), cudaHostAllocMapped));
   SMG_CUDA(cudaHostAlloc(&s->h_done, m * sizeof(Done), cudaHostAllocMapped));
-  SMG_CUDA(cudaHostAlloc(&s->stage, m * per_rec + 4096, cudaHostAllocDefault));
+  SMG_CUDA(cudaHostAlloc(&s->stage, m * per_rec + 4096 + (2 * s->zplan_cap + 1) * sizeof(uint64_t),
+                         cudaHostAllocDefault));
   SMG_CUDA(cudaHostAlloc(&s->h_hold, sizeof(uint32_t), cudaHostAllocMapped));
   SMG_CUDA(cudaHostAlloc(&s->h_tail, sizeof(unsigned long long), cudaHostAllocDefault));
   SMG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_hold), s->h_hold, 0));
