@@ -20,8 +20,9 @@ atomicOr bits into the same word, so a bit can be lost.  A lost bit removes
 a candidate, never adds one, so a reference count may fall short of the
 oracle's and never exceed it, and the shortfall changes from run to run.  The
 tests assert that bound on every run, exact equality on at least 95% of them,
-and write the divergences to gpurun_out/ (when present) for the record.  They
-skip when the reference's sources are not available to build it.
+and, when SMG_TEST_RECORD_DIR names a directory, write the divergences there
+for the record.  They skip when the reference's sources are not available to
+build it.
 """
 import json
 import os
@@ -59,8 +60,8 @@ def judge(runs, name):
     lib_bad = [r for r in runs if r[4] != r[3]]
     over = [r for r in runs if r[2] > r[3]]
     short = [r for r in runs if r[2] < r[3]]
-    out = ROOT / "gpurun_out"
-    if out.is_dir():
+    out = Path(os.environ.get("SMG_TEST_RECORD_DIR", "")) if os.environ.get("SMG_TEST_RECORD_DIR") else None
+    if out is not None and out.is_dir():
         (out / f"reference_divergence_{name}.json").write_text(json.dumps(
             {"runs": len(runs), "short": [list(r) for r in short]}))
     fails = []
