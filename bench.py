@@ -586,7 +586,7 @@ def main():
         for _ in range(max(1, min(3, args.steps))):
             barrier()
             t = time.perf_counter()
-            ps = [Plan(q) for q in queries]
+            ps = Plan.batch(queries)  # smg_plan_create_batch: the plans on all host threads
             _, est = native.match_batch(ctx, dev, ps)
             e2e_t.append(time.perf_counter() - t)
             h2d, d2h = est.h2d_bytes, est.d2h_bytes

@@ -412,6 +412,33 @@ smg_status smg_plan_create(const smg_query_desc *q, smg_plan **out) {
 
 void smg_plan_free(smg_plan *p) { delete p; }
 
+smg_status smg_plan_create_batch(const smg_query_desc *queries, uint32_t n, smg_plan **out) {
+  if (n && (!queries || !out)) return fail(SMG_ERR_INVALID, "null argument");
+  std::vector<smg_status> st(n, SMG_OK);
+  // the plans are independent: one per thread
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) {
+    out[i] = nullptr;
+    std::unique_ptr<smg_plan> p(new smg_plan);
+    st[i] = build_plan(queries[i], p->p);
+    if (!st[i]) out[i] = p.release();
+  }
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!st[i]) continue;
+    // the first failing query again, on this thread, so that smg_last_error
+    // (thread-local) names its reason; then nothing is handed out
+    smg_plan *tmp = nullptr;
+    const smg_status s = smg_plan_create(queries + i, &tmp);
+    smg_plan_free(tmp);
+    for (uint32_t j = 0; j < n; ++j) {
+      smg_plan_free(out[j]);
+      out[j] = nullptr;
+    }
+    return s ? s : st[i];
+  }
+  return SMG_OK;
+}
+
 smg_status smg_plan_get(const smg_plan *pp, smg_plan_view *v) {
   if (!pp || !v) return fail(SMG_ERR_INVALID, "null argument");
   const Plan &P = pp->p;

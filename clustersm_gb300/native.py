@@ -137,6 +137,7 @@ def _load():
         "smg_gen_rmat_pairs": (st, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_int, u32p, u64p]),
         "smg_gen_labels": (st, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, u32p]),
         "smg_plan_create": (st, [C.POINTER(QueryDesc), C.POINTER(vp)]),
+        "smg_plan_create_batch": (st, [C.POINTER(QueryDesc), C.c_uint32, C.POINTER(vp)]),
         "smg_plan_free": (None, [vp]),
         "smg_plan_get": (st, [vp, C.POINTER(PlanView)]),
     }
@@ -331,12 +332,32 @@ class Query:
 class Plan:
     """Host-side plan of one query (spanning tree, clusters, matching order)."""
 
-    def __init__(self, query: Query):
+    def __init__(self, query: Query, handle=None):
         self.query = query
-        self._h = C.c_void_p()
-        check(lib.smg_plan_create(C.byref(query.desc), C.byref(self._h)), "smg_plan_create")
-        self.view = PlanView()
-        check(lib.smg_plan_get(self._h, C.byref(self.view)), "smg_plan_get")
+        if handle is None:
+            self._h = C.c_void_p()
+            check(lib.smg_plan_create(C.byref(query.desc), C.byref(self._h)), "smg_plan_create")
+        else:
+            self._h = handle
+        self._view = None
+
+    @property
+    def view(self) -> PlanView:
+        """The plan's read-only view (smg_plan_get), fetched on first use."""
+        if self._view is None:
+            v = PlanView()
+            check(lib.smg_plan_get(self._h, C.byref(v)), "smg_plan_get")
+            self._view = v
+        return self._view
+
+    @classmethod
+    def batch(cls, queries) -> list:
+        """Plans of many queries, made on all host threads (smg_plan_create_batch)."""
+        n = len(queries)
+        descs = (QueryDesc * n)(*[q.desc for q in queries])
+        hs = (C.c_void_p * n)()
+        check(lib.smg_plan_create_batch(descs, n, hs), "smg_plan_create_batch")
+        return [cls(q, C.c_void_p(h)) for q, h in zip(queries, hs)]
 
     @property
     def handle(self):

@@ -148,6 +148,12 @@ typedef struct smg_plan smg_plan;
  * from the core of the last cluster (main.cu:144). */
 smg_status smg_plan_create(const smg_query_desc *q, smg_plan **out);
 void smg_plan_free(smg_plan *p);
+/* smg_plan_create for queries[0 .. n) on all host threads: out[i] receives
+ * the plan of queries[i].  On the first failing query (in index order) it
+ * frees every plan, sets every out[i] to NULL and returns that query's
+ * status (smg_last_error names the reason).  The reference plans one query
+ * per process (runClusterSM.sh:9-13, main.cu:93-144). */
+smg_status smg_plan_create_batch(const smg_query_desc *queries, uint32_t n, smg_plan **out);
 
 /* Read-only view of a plan (arrays owned by the plan). */
 typedef struct smg_plan_view {

@@ -66,3 +66,26 @@ def test_rejected_queries(labels, edges):
     with pytest.raises(SmgError) as e:
         Plan(Query(labels, edges))
     assert e.value.status == 4
+
+
+def test_batch_plans_match_reference():
+    """smg_plan_create_batch (all host threads) gives every golden case the
+    same plan as the reference's own host code."""
+    qs = [Query(c["query"]["labels"], c["query"]["edges"]) for c in CASES]
+    for p, c in zip(Plan.batch(qs), CASES):
+        compare(p.to_dict(), c["ref"])
+
+
+def test_batch_plans_reject_like_single():
+    """A rejected query fails the whole batch with the first failing query's
+    status and reason, and no plan is handed out."""
+    good = Query([0, 1, 0], [0, 1, 1, 2])
+    bad = Query([0, 0], [0, 0])  # self-loop
+    with pytest.raises(SmgError) as single:
+        Plan(bad)
+    with pytest.raises(SmgError) as e:
+        Plan.batch([good, bad, good])
+    assert e.value.status == single.value.status == 4
+    # the same reason as the single call (the message past the call's name)
+    assert str(e.value).split(":", 1)[-1] == str(single.value).split(":", 1)[-1]
+    assert len(Plan.batch([])) == 0
