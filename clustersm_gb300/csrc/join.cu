@@ -1303,7 +1303,7 @@ __device__ __forceinline__ void join_body(const JoinLaunch &p) {
         }
       }
       // give the shallowest unexplored work of this stack to a waiting warp
-      if ((++tick & 3) == 0) {
+      if ((++tick & p.donate_every_mask) == 0) {
         if (try_donate(S, p, q, Q.pending, L0, level, P, lane, donate_min)) continue;
       }
       if (level == P) {
@@ -1651,6 +1651,17 @@ uint32_t hoist_scan_x8() {
 smg_status launch_persistent(const JoinLaunch &jl_in, cudaStream_t s, int num_sms) {
   JoinLaunch jl = jl_in;
   jl.probe_runs = probe_runs() && jl.adjl != nullptr;
+  // How often a warp looks for waiting warps to split work off to.  Batches
+  // look every second step: on 1,024 R-MAT 2^22 queries, same box, join
+  // 134.7-137.2 ms against 137.6-142.2 ms every fourth step, 146-154 ms every
+  // eighth and 158-159 ms every step.  Time-sliced (served) runs keep every
+  // fourth step, the setting their latencies were measured with.
+  static const long donate_env = [] {
+    const char *e = std::getenv("SMG_DONATE_EVERY");
+    return e ? std::atol(e) : 0L;
+  }();
+  const long every = donate_env > 0 ? donate_env : (jl.slice_ns ? 4 : 2);
+  jl.donate_every_mask = static_cast<uint32_t>(every >= 8 ? 7 : every >= 4 ? 3 : every >= 2 ? 1 : 0);
   jl.hoist = hoist_enabled();
   jl.hoist_scan_x8 = hoist_scan_x8();
   const size_t smem = static_cast<size_t>(kWarpsPerBlock) * warp_words(jl.kmax) * sizeof(uint32_t);

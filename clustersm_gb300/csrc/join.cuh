@@ -74,6 +74,9 @@ struct JoinLaunch {
   uint32_t root_chunk;       // 0: derive from max_seed_tasks
   uint32_t max_seed_tasks;   // initial tasks per query at most
   uint32_t donate_min;       // shortest remaining list worth donating
+  // a warp checks for waiting warps every (mask + 1) steps (SMG_DONATE_EVERY:
+  // 1, 2, 4 or 8; default 2, and 4 for time-sliced runs)
+  uint32_t donate_every_mask;
   // Queue slots breadth-first levels may fill: a warp queues a batch of
   // partial matches only while the tail stays within this many slots, else
   // it descends into them itself, so the breadth-first frontier is bounded

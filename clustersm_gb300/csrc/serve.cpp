@@ -377,7 +377,9 @@ smg_status admit(smg_server *s, cudaStream_t st) {
   // counters, the candidate bitmaps, and the masks and cluster bitmap over
   // the positions of each request's label groups.  Offsets are from the
   // lower of the two allocations involved.
-  char *const zbase = std::min(s->pool.base, reinterpret_cast<char *>(s->d_cnt));
+  char *const zbase = reinterpret_cast<uintptr_t>(s->pool.base) < reinterpret_cast<uintptr_t>(s->d_cnt)
+                          ? s->pool.base
+                          : reinterpret_cast<char *>(s->d_cnt);
   std::vector<std::pair<uint64_t, uint64_t>> zr;  // (byte offset from zbase, bytes)
   smg::FilterBatch fb;
   for (uint32_t i = 0; i < n; ++i) {
@@ -402,7 +404,9 @@ smg_status admit(smg_server *s, cudaStream_t st) {
     if (rc) return rc;
     hseed[i] = idx;
     const uint64_t W = sl.plan->num_words;
-    auto at = [&](const void *p) { return static_cast<uint64_t>(static_cast<const char *>(p) - zbase); };
+    auto at = [&](const void *p) {
+      return static_cast<uint64_t>(reinterpret_cast<uintptr_t>(p) - reinterpret_cast<uintptr_t>(zbase));
+    };
     for (uint32_t gi = 0; gi < hf[i].ngrp; ++gi) {
       const uint64_t lo = hf[i].grp_lo[gi], hi = hf[i].grp_hi[gi];
       if (hi <= lo || hi > g.n) continue;
