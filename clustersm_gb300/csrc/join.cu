@@ -1651,16 +1651,16 @@ uint32_t hoist_scan_x8() {
 smg_status launch_persistent(const JoinLaunch &jl_in, cudaStream_t s, int num_sms) {
   JoinLaunch jl = jl_in;
   jl.probe_runs = probe_runs() && jl.adjl != nullptr;
-  // How often a warp looks for waiting warps to split work off to.  Batches
-  // look every second step: on 1,024 R-MAT 2^22 queries, same box, join
-  // 134.7-137.2 ms against 137.6-142.2 ms every fourth step, 146-154 ms every
-  // eighth and 158-159 ms every step.  Time-sliced (served) runs keep every
-  // fourth step, the setting their latencies were measured with.
+  // How often a warp looks for waiting warps to split work off to: every
+  // second step.  On 1,024 R-MAT 2^22 queries, same box, join 134.7-137.2 ms
+  // against 137.6-142.2 ms every fourth step, 146-154 ms every eighth and
+  // 158-159 ms every step; served at 1,000 requests/s on the 2^24 graph, p99
+  // 52.7 ms against 87.6 ms every fourth step.
   static const long donate_env = [] {
     const char *e = std::getenv("SMG_DONATE_EVERY");
     return e ? std::atol(e) : 0L;
   }();
-  const long every = donate_env > 0 ? donate_env : (jl.slice_ns ? 4 : 2);
+  const long every = donate_env > 0 ? donate_env : 2;
   jl.donate_every_mask = static_cast<uint32_t>(every >= 8 ? 7 : every >= 4 ? 3 : every >= 2 ? 1 : 0);
   jl.hoist = hoist_enabled();
   jl.hoist_scan_x8 = hoist_scan_x8();

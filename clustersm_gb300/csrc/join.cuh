@@ -75,7 +75,7 @@ struct JoinLaunch {
   uint32_t max_seed_tasks;   // initial tasks per query at most
   uint32_t donate_min;       // shortest remaining list worth donating
   // a warp checks for waiting warps every (mask + 1) steps (SMG_DONATE_EVERY:
-  // 1, 2, 4 or 8; default 2, and 4 for time-sliced runs)
+  // 1, 2, 4 or 8; default 2)
   uint32_t donate_every_mask;
   // Queue slots breadth-first levels may fill: a warp queues a batch of
   // partial matches only while the tail stays within this many slots, else
