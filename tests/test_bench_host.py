@@ -13,6 +13,9 @@ def test_defaults_meet_timing_rules(monkeypatch):
     a = bench.parse()
     assert a.gpus == 1 and a.warmup >= 3 and a.steps >= 1
     assert a.workload == "rmat22" and a.impl == "gb300" and a.shape == ""
+    # the serving leg's offered rates: 4-5-vertex requests, then the widest ones
+    assert [float(r) for r in a.serve_rates.split(",")] == [100.0, 1000.0, 5000.0]
+    assert [float(r) for r in a.serve_wide_rates.split(",")] == [25.0, 50.0]
 
 
 def test_shape_choices(monkeypatch):
