@@ -21,6 +21,8 @@ def test_null_arguments_give_invalid():
     assert lib.smg_read_graph(b"x.in", None) == INVALID
     assert lib.smg_read_query(b"x.in", None) == INVALID
     assert lib.smg_plan_create(None, C.byref(out)) == INVALID
+    assert lib.smg_plan_create_batch(None, 1, None) == INVALID
+    assert lib.smg_plan_create_batch(None, 0, None) == 0  # nothing to plan
     assert lib.smg_plan_get(None, None) == INVALID
     assert lib.smg_graph_upload(None, None, C.byref(out)) == INVALID
     assert lib.smg_match(None, None, None, None, None) == INVALID
